@@ -1,0 +1,348 @@
+#!/usr/bin/env python3
+"""SA+BWT throughput of libsais_gb300 on one GB300 (or N independent replicas).
+
+A step = suffix array + BWT (with primary index) of one text.  Default
+workload: the repetitive genome-like uint8 text of n = 2^28 (order-2 Markov
+DNA, GC 0.41, 5% segmental duplications of 1 KiB-1 MiB with 0.1%
+substitutions, tandem repeats of period 2-64 x 10-500 copies), seeded
+synthetic data standing in for the genome corpora of libsais's benchmarks.
+
+  value    device-resident: text already in HBM, SA (int32) and BWT written to
+           HBM by gsais_sa_bwt_device; CUDA events on the launching stream.
+  e2e      the same step through the host C-ABI (gsais_sa_bwt) from pinned
+           host buffers: H2D of the text and D2H of SA and BWT are inside the
+           timed region.
+  roofline the onesweep radix-sort pass kernel (the dominant kernel): its
+           algorithmic bytes (every key/value pair read and written once)
+           over its CUDA-event time inside the timed region, against the
+           measured HBM copy bandwidth.
+  cpu_baseline  the CPU oracle port (SA-IS + BWT, 1 thread) on a bounded
+           prefix of the same text.
+
+--impl reference times the reference's CPU implementation of the step on the
+host cores (the compiled reference where available, else the oracle port).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+WORKLOADS = {
+    # name: (generator, n, description)
+    "genome_like_2^28": ("genome_like", 1 << 28, "repetitive genome-like uint8 text, n=2^28"),
+    "dna_iid_2^24": ("iid", 1 << 24, "i.i.d. uniform ACGT uint8 text, n=2^24"),
+    "all_A_2^26": ("constant", 1 << 26, "all-'A' uint8 text, n=2^26"),
+    "period7_2^26": ("periodic", 1 << 26, "period-7 'ACGTACG' uint8 text, n=2^26"),
+}
+METRIC = "SA+BWT input MB/s"
+UNIT = "MB/s"
+REF_SAMPLE = 1 << 24
+
+
+def make_text(name: str, n: int) -> np.ndarray:
+    from libsais_gb300 import textgen
+    gen = WORKLOADS[name][0]
+    if gen == "genome_like":
+        return textgen.genome_like(n, seed=2)
+    if gen == "iid":
+        return textgen.iid(n, seed=1)
+    if gen == "constant":
+        return textgen.constant(n)
+    return textgen.periodic(n)
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return world, rank, local, dist
+
+
+def reduce_max(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def cpu_step(T: np.ndarray):
+    """SA + BWT on the host with the best CPU implementation available here."""
+    from oracle.oracle import REF_SO, Oracle
+    if os.path.exists(REF_SO):
+        try:
+            from oracle.oracle import Reference
+            R = Reference()
+            threads = os.cpu_count() or 1
+            t0 = time.perf_counter()
+            rc, SA, _ = R.libsais(T, threads=threads)
+            i0 = int(np.flatnonzero(SA == 0)[0])
+            U = np.empty_like(T)
+            U[0] = T[-1]
+            rows = np.concatenate([SA[:i0], SA[i0 + 1:]])
+            U[1:] = T[rows - 1]
+            dt = time.perf_counter() - t0
+            return dt, "reference", threads
+        except OSError:
+            pass
+    O = Oracle()
+    t0 = time.perf_counter()
+    rc, SA = O.sa(T)
+    O.bwt_from_sa(T, SA)
+    return time.perf_counter() - t0, "port", 1
+
+
+def run_reference(args, rank, dist):
+    if rank != 0:
+        return
+    name = args.workload
+    n = args.n or WORKLOADS[name][1]
+    sample = min(n, args.ref_sample)
+    T = make_text(name, n)[:sample].copy()
+    for _ in range(args.warmup):
+        cpu_step(T)
+    times = []
+    kind, cores = "port", 1
+    for _ in range(args.steps):
+        dt, kind, cores = cpu_step(T)
+        times.append(dt)
+    mean = sum(times) / len(times)
+    value = sample / 1e6 / mean
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(mean * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+        "config": {"workload": name, "n": n, "sample_n": sample, "parallelism": "host CPU"},
+        "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": cores, "kind": kind,
+                         "sample": f"first {sample} symbols of the {WORKLOADS[name][2]}"},
+        "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="genome_like_2^28", choices=sorted(WORKLOADS))
+    ap.add_argument("--n", type=int, default=0, help="override the workload length")
+    ap.add_argument("--ref-sample", type=int, default=REF_SAMPLE)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--seed-key-bits", type=int, default=0)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    world, rank, local, dist = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, rank, dist)
+        return
+
+    import torch
+
+    import libsais_gb300 as G
+
+    torch.cuda.set_device(local)
+    name = args.workload
+    n = args.n or WORKLOADS[name][1]
+    T = make_text(name, n)
+    if args.seed_key_bits:
+        G.set_seed_key_bits(args.seed_key_bits)
+    dT = torch.from_numpy(T).cuda()
+    dSA = torch.empty(n, dtype=torch.int32, device="cuda")
+    dU = torch.empty(n, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    prim = None
+    for _ in range(args.warmup):
+        prim = G.sa_bwt_device(dT, dSA, dU, stream=stream)
+        if prim < 0:
+            raise SystemExit(f"gsais_sa_bwt_device failed: {prim}")
+    stats = G.last_stats()
+
+    # ---- device-resident timed region
+    sampler = ClockSampler(local)
+    sampler.start()
+    barrier(dist)
+    torch.cuda.synchronize()
+    G.profile_reset()
+    G.profile_enable(True)
+    launches0 = G.launch_count()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        p = G.sa_bwt_device(dT, dSA, dU, stream=stream)
+        if p != prim:
+            raise SystemExit(f"primary index changed between steps: {p} vs {prim}")
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier(dist)
+    launches = G.launch_count() - launches0
+    G.profile_enable(False)
+    prof = G.profile_read()
+    clocks = sampler.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    ms = reduce_max(dist, ms)
+    value = world * n / 1e6 / (ms / 1e3)
+
+    # ---- dominant kernel roofline (onesweep pass), from the same timed region
+    peak, peak_kind = peaks()
+    ks = prof.get("onesweep", {"launches": 0, "total_ms": 0.0, "bytes": 0})
+    roof = None
+    if ks["launches"]:
+        per_launch_ms = ks["total_ms"] / ks["launches"]
+        per_launch_bytes = ks["bytes"] / ks["launches"]
+        achieved = per_launch_bytes / (per_launch_ms / 1e3) / 1e9
+        traffic = None
+        tfile = os.path.join(ROOT, "profiles", "onesweep_traffic.json")
+        if os.path.exists(tfile):
+            with open(tfile) as f:
+                tr = json.load(f)
+            traffic = round(tr["dram_bytes_per_pair"] * per_launch_bytes / 24.0, 0)
+        roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
+                "kernel": "k_onesweep", "launches_per_step": ks["launches"] / args.steps,
+                "algorithmic_bytes_per_launch": int(per_launch_bytes), "ms_per_launch": round(per_launch_ms, 4)}
+    kernels = {k: {"launches_per_step": v["launches"] / args.steps,
+                   "ms_per_step": round(v["total_ms"] / args.steps, 3)} for k, v in prof.items() if v["launches"]}
+
+    # ---- end to end through the host C-ABI from pinned buffers
+    e2e = None
+    if not args.no_e2e:
+        hT = torch.from_numpy(T).pin_memory()
+        hSA = torch.empty(n, dtype=torch.int32).pin_memory()
+        hU = torch.empty(n, dtype=torch.uint8).pin_memory()
+        lib = G.load()
+        call = lambda: lib.gsais_sa_bwt(None, hT.data_ptr(), 1, n, hSA.data_ptr(), 4, hU.data_ptr(), None, 4)
+        if call() != prim:
+            raise SystemExit("host-path primary index differs from the device path")
+        if not (torch.equal(hSA, dSA.cpu()) and torch.equal(hU, dU.cpu())):
+            raise SystemExit("host-path SA/BWT differ from the device path")
+        barrier(dist)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            call()
+        e2e_s = (time.perf_counter() - t0) / args.steps
+        e2e_s = reduce_max(dist, e2e_s)
+        e2e = {"value": round(world * n / 1e6 / e2e_s, 3), "unit": UNIT, "h2d_bytes_per_step": n,
+               "d2h_bytes_per_step": n * 4 + n, "ms_per_step": round(e2e_s * 1e3, 3)}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        sample = min(n, args.ref_sample)
+        Ts = T[:sample].copy()
+        dt, kind, cores = cpu_step(Ts)
+        cpu = {"value": round(sample / 1e6 / dt, 3), "unit": UNIT, "cores": cores, "kind": kind,
+               "sample": f"first {sample} symbols of the {WORKLOADS[name][2]}, SA-IS + BWT"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+            "config": {"workload": name, "n": n, "description": WORKLOADS[name][2], "sa": "int32",
+                       "outputs": "SA + BWT + primary index", "l2": "inputs larger than L2 (text and SA > 129 MB)",
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "rounds": stats["rounds"], "seed_symbols": stats["seed_symbols"],
+                       "radix_passes": stats["radix_passes"]},
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+            "kernels": kernels, "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

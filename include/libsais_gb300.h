@@ -1,0 +1,111 @@
+/*--
+
+libsais_gb300 -- GB300 (sm_103a) suffix-array construction behind the libsais
+API.  This header declares the entry points that have NO counterpart in the
+reference libsais 2.10.4: device-resident variants for callers whose text
+already lives in GPU memory, a combined SA + BWT call, and run statistics.
+The reference-compatible entry points are declared in libsais.h,
+libsais64.h and libsais16.h.
+
+Conventions shared with libsais: return 0 (or the BWT primary index) on
+success, -1 for invalid arguments, -2 for allocation or device failures.
+
+--*/
+
+#ifndef LIBSAIS_GB300_H
+#define LIBSAIS_GB300_H 1
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+    /**
+    * Suffix array of a text that already resides in device memory.
+    * @param ctx A context from libsais_create_ctx (or NULL for the process-wide one).
+    * @param T [0..n-1] Device pointer to the text (1- or 2-byte symbols).
+    * @param symbytes 1 for uint8_t text, 2 for uint16_t text.
+    * @param n The text length (must be < 2^32).
+    * @param gsa Non-zero to build the generalized suffix array (0 separators, T[n-1] == 0).
+    * @param SA [0..n-1] Device pointer receiving the suffix array (int32 or int64).
+    * @param sa_bytes 4 for int32 SA, 8 for int64 SA.
+    * @param stream cudaStream_t to run on (NULL: the context's stream).
+    * @return 0 on success, -1 or -2 otherwise.
+    */
+    int64_t gsais_sa_device(void * ctx, const void * T, int32_t symbytes, int64_t n, int32_t gsa, void * SA, int32_t sa_bytes, void * stream);
+
+    /**
+    * Suffix array and BWT (libsais_bwt layout) of a device-resident text in one sort.
+    * @param SA [0..n-1] Device pointer receiving the suffix array (may be NULL).
+    * @param U [0..n-1] Device pointer receiving the BWT (must not alias T).
+    * @return The primary index (as libsais_bwt returns it), or -1 / -2.
+    */
+    int64_t gsais_sa_bwt_device(void * ctx, const void * T, int32_t symbytes, int64_t n, void * SA, int32_t sa_bytes, void * U, void * stream);
+
+    /**
+    * PLCP of a device-resident text and suffix array.
+    * @param idx_bytes Width of SA and PLCP entries (4 or 8).
+    * @return 0 on success, -1 or -2 otherwise.
+    */
+    int64_t gsais_plcp_device(void * ctx, const void * T, int32_t symbytes, const void * SA, void * PLCP, int32_t idx_bytes, int64_t n, int32_t gsa, void * stream);
+
+    /**
+    * LCP[i] = PLCP[SA[i]] on device-resident arrays (idx_bytes 4 or 8; LCP must not alias PLCP).
+    */
+    int64_t gsais_lcp_device(void * ctx, const void * PLCP, const void * SA, void * LCP, int32_t idx_bytes, int64_t n, void * stream);
+
+    /**
+    * Suffix array and BWT of a host text with one sort (one H2D of T, D2H of SA and U).
+    * @param SA [0..n-1] Output suffix array (int32 or int64 per sa_bytes).
+    * @param U [0..n-1] Output BWT in libsais_bwt's layout (may be T).
+    * @param freq Optional symbol frequencies (256 or 65536 entries, freq_bytes wide).
+    * @return The primary index, or -1 / -2.
+    */
+    int64_t gsais_sa_bwt(void * ctx, const void * T, int32_t symbytes, int64_t n, void * SA, int32_t sa_bytes, void * U, void * freq, int32_t freq_bytes);
+
+    /** Statistics of the last suffix sort run on a context. */
+    typedef struct gsais_stats
+    {
+        int32_t rounds;          /* prefix-doubling rounds after the seed sort */
+        int32_t seed_symbols;    /* symbols packed into each seed key */
+        int32_t seed_bits;       /* bits per dense symbol code */
+        int32_t radix_passes;    /* digit passes actually run (all sorts) */
+        int64_t active_total;    /* sum over rounds of still-unsorted suffixes */
+        int64_t workspace_bytes; /* device workspace held by the context */
+    } gsais_stats;
+
+    int32_t gsais_last_stats(void * ctx, gsais_stats * out);
+
+    /** Seed key width in bits (32 or 64) used by later sorts on ctx; returns the previous width. */
+    int32_t gsais_set_seed_key_bits(void * ctx, int32_t bits);
+
+    /** Per-kernel timing record (CUDA events on the launching stream). */
+    typedef struct gsais_kernel_profile
+    {
+        const char * name;       /* kernel family */
+        int64_t launches;        /* timed launches */
+        double total_ms;         /* summed device time */
+        int64_t bytes;           /* summed algorithmic bytes (reads + writes) */
+    } gsais_kernel_profile;
+
+    /** Turns per-kernel timing on ctx on or off; returns the previous state. */
+    int32_t gsais_profile_enable(void * ctx, int32_t on);
+
+    /** Copies up to max_kinds records; returns how many were written. */
+    int32_t gsais_profile_read(void * ctx, gsais_kernel_profile * out, int32_t max_kinds);
+
+    /** Clears the accumulated timing records of ctx. */
+    void gsais_profile_reset(void * ctx);
+
+    /** Kernels launched by this library since the process started (all contexts). */
+    int64_t gsais_launch_count(void);
+
+    /** Releases the device workspace cached by ctx (NULL: the process-wide context). */
+    void gsais_release_workspace(void * ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,576 @@
+// engine.cu -- device contexts, workspace arena and the C-ABI entry points
+// that the libsais-compatible shim (api.c) and direct device users call.
+//
+// A context maps libsais's LIBSAIS_CONTEXT (src/libsais.c:63-99, 176-266:
+// buckets + per-thread state reused across calls) onto GPU resources: one
+// CUDA stream, one device workspace arena that grows to the high-water mark
+// of the calls made on it, pinned host scratch for small read-backs, and a
+// device error word for bounded spin-waits.  The context-less libsais calls
+// share one process-wide context behind its mutex.
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+
+#include "device_util.cuh"
+#include "engine.h"
+#include "gsais.h"
+#include "libsais_gb300.h"
+#include "outputs.cuh"
+#include "suffix_sort.cuh"
+
+using namespace gsais;
+
+struct gsais_ctx {
+    std::mutex mu;
+    bool ready = false;
+    int device = -1;
+    cudaStream_t stream = nullptr;
+    void *arena = nullptr;
+    size_t arena_bytes = 0;
+    uint32_t *d_misc = nullptr;   // [0] error word, [1] validity flag
+    uint32_t *h_small = nullptr;  // pinned: 16 + 65536 hist words + 65536 u16 codes
+    uint32_t *h_hist = nullptr;   // pinned: radix histograms
+    SortOptions opt;
+    SortStats stats;
+    KernelProfiler prof;
+};
+
+namespace {
+
+constexpr size_t kAlign = 256;
+constexpr size_t kSmallWords = 16 + 65536 + 32768;
+constexpr uint64_t kMaxN = 0xFFFFFFFFull;   // 32-bit internal indices
+
+inline size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev)
+    {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (dev >= 0 && dev != prev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard()
+    {
+        int cur = -1;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+bool ctx_init(gsais_ctx *c)
+{
+    if (c->ready) return true;
+    if (cudaGetDevice(&c->device) != cudaSuccess) return false;
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return false;
+    if (cudaMalloc(&c->d_misc, 64) != cudaSuccess) return false;
+    if (cudaMemset(c->d_misc, 0, 64) != cudaSuccess) return false;
+    if (cudaMallocHost(&c->h_small, kSmallWords * sizeof(uint32_t)) != cudaSuccess) return false;
+    if (cudaMallocHost(&c->h_hist, 8 * 256 * sizeof(uint32_t)) != cudaSuccess) return false;
+    c->ready = true;
+    return true;
+}
+
+bool ensure_arena(gsais_ctx *c, size_t bytes)
+{
+    if (c->arena_bytes >= bytes) return true;
+    if (c->arena) {
+        cudaFree(c->arena);
+        c->arena = nullptr;
+        c->arena_bytes = 0;
+    }
+    const size_t want = (bytes + ((size_t)2 << 20) - 1) / ((size_t)2 << 20) * ((size_t)2 << 20);
+    if (cudaMalloc(&c->arena, want) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    c->arena_bytes = want;
+    return true;
+}
+
+struct Carver {
+    char *p;
+    explicit Carver(void *base) : p(static_cast<char *>(base)) {}
+    template <typename T>
+    T *take(size_t count)
+    {
+        T *r = reinterpret_cast<T *>(p);
+        p += align_up(count * sizeof(T));
+        return r;
+    }
+};
+
+// Clears the device error word; returns false on CUDA failure.
+bool clear_err(gsais_ctx *c, cudaStream_t st) { return cudaMemsetAsync(c->d_misc, 0, 8, st) == cudaSuccess; }
+
+// Synchronises the stream and turns a raised device error word into an error.
+cudaError_t sync_checked(gsais_ctx *c, cudaStream_t st)
+{
+    cudaError_t e = cudaMemcpyAsync(c->h_small + 8, c->d_misc, 4, cudaMemcpyDeviceToHost, st);
+    if (e != cudaSuccess) return e;
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+    return c->h_small[8] ? cudaErrorUnknown : cudaSuccess;
+}
+
+void emit_freq(const uint32_t *h_hist, int symbytes, void *freq, int freq_bytes)
+{
+    if (!freq) return;
+    const int k = symbytes == 1 ? 256 : 65536;
+    if (freq_bytes == 8) {
+        int64_t *f = static_cast<int64_t *>(freq);
+        for (int c = 0; c < k; ++c) f[c] = h_hist[c];
+    } else {
+        int32_t *f = static_cast<int32_t *>(freq);
+        for (int c = 0; c < k; ++c) f[c] = (int32_t)h_hist[c];
+    }
+}
+
+gsais_ctx *resolve(void *ctx) { return ctx ? static_cast<gsais_ctx *>(ctx) : gsais_default_ctx(); }
+
+int64_t fail(cudaError_t)
+{
+    cudaGetLastError();   // clear a non-sticky error so the context stays usable
+    return -2;
+}
+
+#define GS_TRY(expr)                                         \
+    do {                                                     \
+        cudaError_t _e = (expr);                             \
+        if (_e != cudaSuccess) return fail(_e);              \
+    } while (0)
+
+// Workspace for one suffix sort carved after `extra` bytes of call buffers.
+struct SortPlan {
+    size_t sort_bytes;
+    size_t total;
+};
+
+SortPlan plan_sort(uint64_t n, int symbytes, size_t extra)
+{
+    SortPlan p;
+    p.sort_bytes = sort_workspace_bytes(n, symbytes);
+    p.total = extra + p.sort_bytes;
+    return p;
+}
+
+// Sort a device text already placed in the arena.  `sa_override` (nullable)
+// receives SA directly when the caller wants uint32 output in its own buffer.
+int64_t run_sort(gsais_ctx *c, const void *d_T, int symbytes, uint64_t n, bool gsa, SortWorkspace &ws,
+                 cudaStream_t st)
+{
+    if (gsa) {
+        bool valid = true;
+        GS_TRY(gsa_validate(d_T, symbytes, n, c->d_misc + 1, c->h_small, st, &valid));
+        if (!valid) return -1;
+    }
+    ws.radix.prof = &c->prof;
+    GS_TRY(suffix_sort(d_T, symbytes, n, gsa, ws, c->opt, c->d_misc, st, &c->stats));
+    return 0;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ C ABI
+extern "C" {
+
+gsais_ctx *gsais_ctx_create(void)
+{
+    gsais_ctx *c = new (std::nothrow) gsais_ctx();
+    return c;
+}
+
+void gsais_ctx_destroy(gsais_ctx *c)
+{
+    if (!c) return;
+    if (c->ready) {
+        DeviceGuard g(c->device);
+        if (c->stream) cudaStreamSynchronize(c->stream);
+        if (c->arena) cudaFree(c->arena);
+        if (c->d_misc) cudaFree(c->d_misc);
+        if (c->h_small) cudaFreeHost(c->h_small);
+        if (c->h_hist) cudaFreeHost(c->h_hist);
+        if (c->stream) cudaStreamDestroy(c->stream);
+    }
+    delete c;
+}
+
+gsais_ctx *gsais_default_ctx(void)
+{
+    static gsais_ctx *g = new gsais_ctx();
+    return g;
+}
+
+int64_t gsais_run_sa(gsais_ctx *c, const void *T, int symbytes, int64_t n_, int gsa, void *SA, int sa_bytes,
+                     void *freq, int freq_bytes)
+{
+    if (!c) return -2;
+    std::lock_guard<std::mutex> lock(c->mu);
+    const uint64_t n = (uint64_t)n_;
+    if (n > kMaxN) return -2;
+    if (!ctx_init(c)) return fail(cudaErrorUnknown);
+    DeviceGuard g(c->device);
+    cudaStream_t st = c->stream;
+    const size_t tb = align_up(n * symbytes);
+    const size_t wide = sa_bytes == 8 ? align_up(n * 8) : 0;
+    const SortPlan plan = plan_sort(n, symbytes, tb + wide);
+    if (!ensure_arena(c, plan.total)) return -2;
+    Carver cv(c->arena);
+    uint8_t *d_T = cv.take<uint8_t>(n * symbytes);
+    int64_t *d_wide = sa_bytes == 8 ? cv.take<int64_t>(n) : nullptr;
+    SortWorkspace ws;
+    sort_workspace_carve(ws, cv.p, n, symbytes, c->h_small, c->h_hist);
+    if (!clear_err(c, st)) return fail(cudaErrorUnknown);
+    GS_TRY(cudaMemcpyAsync(d_T, T, n * symbytes, cudaMemcpyHostToDevice, st));
+    const int64_t rc = run_sort(c, d_T, symbytes, n, gsa != 0, ws, st);
+    if (rc == -1) {
+        // libsais fills freq before rejecting a malformed GSA text (src/libsais.c:6883-6889)
+        GS_TRY(symbol_histogram(d_T, symbytes, n, ws.hist, c->h_small + 16, st));
+        emit_freq(c->h_small + 16, symbytes, freq, freq_bytes);
+        return -1;
+    }
+    if (rc != 0) return rc;
+    if (sa_bytes == 8) {
+        GS_TRY(widen_u32_to_i64(ws.sa, d_wide, n, st));
+        GS_TRY(cudaMemcpyAsync(SA, d_wide, n * 8, cudaMemcpyDeviceToHost, st));
+    } else {
+        GS_TRY(cudaMemcpyAsync(SA, ws.sa, n * 4, cudaMemcpyDeviceToHost, st));
+    }
+    GS_TRY(sync_checked(c, st));
+    emit_freq(c->h_small + 16, symbytes, freq, freq_bytes);
+    return 0;
+}
+
+int64_t gsais_run_bwt(gsais_ctx *c, const void *T, int symbytes, int64_t n_, void *U, void *freq, int freq_bytes,
+                      int64_t r, void *I, int idx_bytes, void *SA, int sa_bytes)
+{
+    if (!c) return -2;
+    std::lock_guard<std::mutex> lock(c->mu);
+    const uint64_t n = (uint64_t)n_;
+    if (n > kMaxN) return -2;
+    if (!ctx_init(c)) return fail(cudaErrorUnknown);
+    DeviceGuard g(c->device);
+    cudaStream_t st = c->stream;
+    const uint64_t icount = r > 0 ? (n - 1) / (uint64_t)r + 1 : 0;
+    const size_t extra = align_up(n * symbytes) * 2 + (r > 0 ? align_up(icount * idx_bytes) : 0) +
+                         (SA && sa_bytes == 8 ? align_up(n * 8) : 0);
+    const SortPlan plan = plan_sort(n, symbytes, extra);
+    if (!ensure_arena(c, plan.total)) return -2;
+    Carver cv(c->arena);
+    uint8_t *d_T = cv.take<uint8_t>(n * symbytes);
+    uint8_t *d_U = cv.take<uint8_t>(n * symbytes);
+    void *d_I = r > 0 ? (void *)cv.take<uint8_t>(icount * idx_bytes) : nullptr;
+    int64_t *d_wide = (SA && sa_bytes == 8) ? cv.take<int64_t>(n) : nullptr;
+    SortWorkspace ws;
+    sort_workspace_carve(ws, cv.p, n, symbytes, c->h_small, c->h_hist);
+    if (!clear_err(c, st)) return fail(cudaErrorUnknown);
+    GS_TRY(cudaMemcpyAsync(d_T, T, n * symbytes, cudaMemcpyHostToDevice, st));
+    const int64_t rc = run_sort(c, d_T, symbytes, n, false, ws, st);
+    if (rc != 0) return rc;
+    GS_TRY(bwt_gather(d_T, symbytes, ws.sa, ws.rank, n, d_U, c->d_misc, st));
+    if (r > 0) GS_TRY(aux_sample(ws.rank, n, (uint64_t)r, d_I, idx_bytes, st));
+    GS_TRY(cudaMemcpyAsync(c->h_small, ws.rank, 4, cudaMemcpyDeviceToHost, st));
+    GS_TRY(cudaMemcpyAsync(U, d_U, n * symbytes, cudaMemcpyDeviceToHost, st));
+    if (r > 0) GS_TRY(cudaMemcpyAsync(I, d_I, icount * idx_bytes, cudaMemcpyDeviceToHost, st));
+    if (SA) {
+        if (sa_bytes == 8) {
+            GS_TRY(widen_u32_to_i64(ws.sa, d_wide, n, st));
+            GS_TRY(cudaMemcpyAsync(SA, d_wide, n * 8, cudaMemcpyDeviceToHost, st));
+        } else {
+            GS_TRY(cudaMemcpyAsync(SA, ws.sa, n * 4, cudaMemcpyDeviceToHost, st));
+        }
+    }
+    GS_TRY(sync_checked(c, st));
+    const int64_t prim = (int64_t)c->h_small[0];   // ISA[0] + 1
+    emit_freq(c->h_small + 16, symbytes, freq, freq_bytes);
+    return r > 0 ? 0 : prim;
+}
+
+int64_t gsais_run_plcp(gsais_ctx *c, const void *T, int symbytes, const void *SA, void *PLCP, int idx_bytes,
+                       int64_t n_, int gsa)
+{
+    if (!c) return -2;
+    std::lock_guard<std::mutex> lock(c->mu);
+    const uint64_t n = (uint64_t)n_;
+    if (n > kMaxN) return -2;
+    if (!ctx_init(c)) return fail(cudaErrorUnknown);
+    DeviceGuard g(c->device);
+    cudaStream_t st = c->stream;
+    const size_t total = align_up(n * symbytes) + 2 * align_up(n * 4) + (idx_bytes == 8 ? align_up(n * 8) : 0) +
+                         align_up(plcp_sparse_words(n) * 4);
+    if (!ensure_arena(c, total)) return -2;
+    Carver cv(c->arena);
+    uint8_t *d_T = cv.take<uint8_t>(n * symbytes);
+    uint32_t *d_SA = cv.take<uint32_t>(n);
+    uint32_t *d_P = cv.take<uint32_t>(n);
+    int64_t *d_wide = idx_bytes == 8 ? cv.take<int64_t>(n) : nullptr;
+    uint32_t *d_sparse = cv.take<uint32_t>(plcp_sparse_words(n));
+    if (!clear_err(c, st)) return fail(cudaErrorUnknown);
+    GS_TRY(cudaMemcpyAsync(d_T, T, n * symbytes, cudaMemcpyHostToDevice, st));
+    if (idx_bytes == 8) {
+        GS_TRY(cudaMemcpyAsync(d_wide, SA, n * 8, cudaMemcpyHostToDevice, st));
+        GS_TRY(narrow_i64_to_u32(d_wide, d_SA, n, c->d_misc, st));
+    } else {
+        GS_TRY(cudaMemcpyAsync(d_SA, SA, n * 4, cudaMemcpyHostToDevice, st));
+    }
+    GS_TRY(plcp_build(d_T, symbytes, d_SA, n, gsa != 0, d_P, d_sparse, c->d_misc, st));
+    if (idx_bytes == 8) {
+        GS_TRY(widen_u32_to_i64(d_P, d_wide, n, st));
+        GS_TRY(cudaMemcpyAsync(PLCP, d_wide, n * 8, cudaMemcpyDeviceToHost, st));
+    } else {
+        GS_TRY(cudaMemcpyAsync(PLCP, d_P, n * 4, cudaMemcpyDeviceToHost, st));
+    }
+    GS_TRY(sync_checked(c, st));
+    return 0;
+}
+
+int64_t gsais_run_lcp(gsais_ctx *c, const void *PLCP, const void *SA, void *LCP, int idx_bytes, int64_t n_)
+{
+    if (!c) return -2;
+    std::lock_guard<std::mutex> lock(c->mu);
+    const uint64_t n = (uint64_t)n_;
+    if (n > kMaxN) return -2;
+    if (!ctx_init(c)) return fail(cudaErrorUnknown);
+    DeviceGuard g(c->device);
+    cudaStream_t st = c->stream;
+    const size_t total = 3 * align_up(n * 4) + (idx_bytes == 8 ? align_up(n * 8) : 0);
+    if (!ensure_arena(c, total)) return -2;
+    Carver cv(c->arena);
+    uint32_t *d_P = cv.take<uint32_t>(n);
+    uint32_t *d_SA = cv.take<uint32_t>(n);
+    uint32_t *d_L = cv.take<uint32_t>(n);
+    int64_t *d_wide = idx_bytes == 8 ? cv.take<int64_t>(n) : nullptr;
+    if (!clear_err(c, st)) return fail(cudaErrorUnknown);
+    if (idx_bytes == 8) {
+        GS_TRY(cudaMemcpyAsync(d_wide, PLCP, n * 8, cudaMemcpyHostToDevice, st));
+        GS_TRY(narrow_i64_to_u32(d_wide, d_P, n, c->d_misc, st));
+        GS_TRY(cudaMemcpyAsync(d_wide, SA, n * 8, cudaMemcpyHostToDevice, st));
+        GS_TRY(narrow_i64_to_u32(d_wide, d_SA, n, c->d_misc, st));
+    } else {
+        GS_TRY(cudaMemcpyAsync(d_P, PLCP, n * 4, cudaMemcpyHostToDevice, st));
+        GS_TRY(cudaMemcpyAsync(d_SA, SA, n * 4, cudaMemcpyHostToDevice, st));
+    }
+    GS_TRY(lcp_gather(d_P, d_SA, d_L, n, c->d_misc, st));
+    if (idx_bytes == 8) {
+        GS_TRY(widen_u32_to_i64(d_L, d_wide, n, st));
+        GS_TRY(cudaMemcpyAsync(LCP, d_wide, n * 8, cudaMemcpyDeviceToHost, st));
+    } else {
+        GS_TRY(cudaMemcpyAsync(LCP, d_L, n * 4, cudaMemcpyDeviceToHost, st));
+    }
+    GS_TRY(sync_checked(c, st));
+    return 0;
+}
+
+// ------------------------------------------------ public extension entry points
+
+int64_t gsais_sa_device(void *ctx, const void *T, int32_t symbytes, int64_t n_, int32_t gsa, void *SA,
+                        int32_t sa_bytes, void *stream)
+{
+    gsais_ctx *c = resolve(ctx);
+    if (!c || !T || !SA || n_ < 0 || (symbytes != 1 && symbytes != 2) || (sa_bytes != 4 && sa_bytes != 8)) return -1;
+    std::lock_guard<std::mutex> lock(c->mu);
+    const uint64_t n = (uint64_t)n_;
+    if (n > kMaxN) return -2;
+    if (n == 0) return 0;
+    if (!ctx_init(c)) return fail(cudaErrorUnknown);
+    DeviceGuard g(c->device);
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : c->stream;
+    const SortPlan plan = plan_sort(n, symbytes, 0);
+    if (!ensure_arena(c, plan.total)) return -2;
+    SortWorkspace ws;
+    sort_workspace_carve(ws, c->arena, n, symbytes, c->h_small, c->h_hist);
+    if (sa_bytes == 4) ws.sa = static_cast<uint32_t *>(SA);
+    if (!clear_err(c, st)) return fail(cudaErrorUnknown);
+    const int64_t rc = run_sort(c, T, symbytes, n, gsa != 0, ws, st);
+    if (rc != 0) return rc;
+    if (sa_bytes == 8) GS_TRY(widen_u32_to_i64(ws.sa, static_cast<int64_t *>(SA), n, st));
+    GS_TRY(sync_checked(c, st));
+    return 0;
+}
+
+int64_t gsais_sa_bwt_device(void *ctx, const void *T, int32_t symbytes, int64_t n_, void *SA, int32_t sa_bytes,
+                            void *U, void *stream)
+{
+    gsais_ctx *c = resolve(ctx);
+    if (!c || !T || !U || n_ < 0 || (symbytes != 1 && symbytes != 2) || (SA && sa_bytes != 4 && sa_bytes != 8))
+        return -1;
+    std::lock_guard<std::mutex> lock(c->mu);
+    const uint64_t n = (uint64_t)n_;
+    if (n > kMaxN) return -2;
+    if (n == 0) return 0;
+    if (!ctx_init(c)) return fail(cudaErrorUnknown);
+    DeviceGuard g(c->device);
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : c->stream;
+    const SortPlan plan = plan_sort(n, symbytes, 0);
+    if (!ensure_arena(c, plan.total)) return -2;
+    SortWorkspace ws;
+    sort_workspace_carve(ws, c->arena, n, symbytes, c->h_small, c->h_hist);
+    if (SA && sa_bytes == 4) ws.sa = static_cast<uint32_t *>(SA);
+    if (!clear_err(c, st)) return fail(cudaErrorUnknown);
+    const int64_t rc = run_sort(c, T, symbytes, n, false, ws, st);
+    if (rc != 0) return rc;
+    GS_TRY(bwt_gather(T, symbytes, ws.sa, ws.rank, n, U, c->d_misc, st));
+    if (SA && sa_bytes == 8) GS_TRY(widen_u32_to_i64(ws.sa, static_cast<int64_t *>(SA), n, st));
+    GS_TRY(cudaMemcpyAsync(c->h_small, ws.rank, 4, cudaMemcpyDeviceToHost, st));
+    GS_TRY(sync_checked(c, st));
+    return (int64_t)c->h_small[0];
+}
+
+int64_t gsais_plcp_device(void *ctx, const void *T, int32_t symbytes, const void *SA, void *PLCP, int32_t idx_bytes,
+                          int64_t n_, int32_t gsa, void *stream)
+{
+    gsais_ctx *c = resolve(ctx);
+    if (!c || !T || !SA || !PLCP || n_ < 0 || (symbytes != 1 && symbytes != 2) || (idx_bytes != 4 && idx_bytes != 8))
+        return -1;
+    std::lock_guard<std::mutex> lock(c->mu);
+    const uint64_t n = (uint64_t)n_;
+    if (n > kMaxN) return -2;
+    if (n == 0) return 0;
+    if (!ctx_init(c)) return fail(cudaErrorUnknown);
+    DeviceGuard g(c->device);
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : c->stream;
+    const size_t total = (idx_bytes == 8 ? 2 * align_up(n * 4) : 0) + align_up(plcp_sparse_words(n) * 4);
+    if (!ensure_arena(c, total)) return -2;
+    if (!clear_err(c, st)) return fail(cudaErrorUnknown);
+    Carver cv(c->arena);
+    const uint32_t *d_SA = static_cast<const uint32_t *>(SA);
+    uint32_t *d_P = static_cast<uint32_t *>(PLCP);
+    if (idx_bytes == 8) {
+        uint32_t *sa32 = cv.take<uint32_t>(n);
+        d_P = cv.take<uint32_t>(n);
+        GS_TRY(narrow_i64_to_u32(static_cast<const int64_t *>(SA), sa32, n, c->d_misc, st));
+        d_SA = sa32;
+    }
+    uint32_t *d_sparse = cv.take<uint32_t>(plcp_sparse_words(n));
+    GS_TRY(plcp_build(T, symbytes, d_SA, n, gsa != 0, d_P, d_sparse, c->d_misc, st));
+    if (idx_bytes == 8) GS_TRY(widen_u32_to_i64(d_P, static_cast<int64_t *>(PLCP), n, st));
+    GS_TRY(sync_checked(c, st));
+    return 0;
+}
+
+int64_t gsais_lcp_device(void *ctx, const void *PLCP, const void *SA, void *LCP, int32_t idx_bytes, int64_t n_,
+                         void *stream)
+{
+    gsais_ctx *c = resolve(ctx);
+    if (!c || !PLCP || !SA || !LCP || n_ < 0 || (idx_bytes != 4 && idx_bytes != 8)) return -1;
+    std::lock_guard<std::mutex> lock(c->mu);
+    const uint64_t n = (uint64_t)n_;
+    if (n > kMaxN) return -2;
+    if (n == 0) return 0;
+    if (!ctx_init(c)) return fail(cudaErrorUnknown);
+    DeviceGuard g(c->device);
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : c->stream;
+    if (!clear_err(c, st)) return fail(cudaErrorUnknown);
+    if (idx_bytes == 4) {
+        GS_TRY(lcp_gather(static_cast<const uint32_t *>(PLCP), static_cast<const uint32_t *>(SA),
+                          static_cast<uint32_t *>(LCP), n, c->d_misc, st));
+    } else {
+        if (!ensure_arena(c, 3 * align_up(n * 4))) return -2;
+        Carver cv(c->arena);
+        uint32_t *p = cv.take<uint32_t>(n), *s = cv.take<uint32_t>(n), *l = cv.take<uint32_t>(n);
+        GS_TRY(narrow_i64_to_u32(static_cast<const int64_t *>(PLCP), p, n, c->d_misc, st));
+        GS_TRY(narrow_i64_to_u32(static_cast<const int64_t *>(SA), s, n, c->d_misc, st));
+        GS_TRY(lcp_gather(p, s, l, n, c->d_misc, st));
+        GS_TRY(widen_u32_to_i64(l, static_cast<int64_t *>(LCP), n, st));
+    }
+    GS_TRY(sync_checked(c, st));
+    return 0;
+}
+
+int64_t gsais_sa_bwt(void *ctx, const void *T, int32_t symbytes, int64_t n, void *SA, int32_t sa_bytes, void *U,
+                     void *freq, int32_t freq_bytes)
+{
+    gsais_ctx *c = resolve(ctx);
+    if (!c || !T || !SA || !U || n < 0 || (symbytes != 1 && symbytes != 2) || (sa_bytes != 4 && sa_bytes != 8))
+        return -1;
+    if (n <= 1) {
+        if (freq) std::memset(freq, 0, (size_t)(symbytes == 1 ? 256 : 65536) * freq_bytes);
+        if (n == 1) {
+            if (sa_bytes == 8) static_cast<int64_t *>(SA)[0] = 0;
+            else static_cast<int32_t *>(SA)[0] = 0;
+            const uint32_t sym = symbytes == 1 ? static_cast<const uint8_t *>(T)[0] : static_cast<const uint16_t *>(T)[0];
+            if (symbytes == 1) static_cast<uint8_t *>(U)[0] = (uint8_t)sym;
+            else static_cast<uint16_t *>(U)[0] = (uint16_t)sym;
+            if (freq) {
+                if (freq_bytes == 8) static_cast<int64_t *>(freq)[sym] = 1;
+                else static_cast<int32_t *>(freq)[sym] = 1;
+            }
+        }
+        return n;
+    }
+    return gsais_run_bwt(c, T, symbytes, n, U, freq, freq_bytes, 0, nullptr, 4, SA, sa_bytes);
+}
+
+int32_t gsais_last_stats(void *ctx, gsais_stats *out)
+{
+    gsais_ctx *c = resolve(ctx);
+    if (!c || !out) return -1;
+    std::lock_guard<std::mutex> lock(c->mu);
+    out->rounds = c->stats.rounds;
+    out->seed_symbols = c->stats.seed_symbols;
+    out->seed_bits = c->stats.seed_bits;
+    out->radix_passes = c->stats.radix_passes;
+    out->active_total = (int64_t)c->stats.active_total;
+    out->workspace_bytes = (int64_t)c->arena_bytes;
+    return 0;
+}
+
+int32_t gsais_set_seed_key_bits(void *ctx, int32_t bits)
+{
+    gsais_ctx *c = resolve(ctx);
+    if (!c || (bits != 32 && bits != 64)) return -1;
+    std::lock_guard<std::mutex> lock(c->mu);
+    const int32_t prev = c->opt.seed_key_bits;
+    c->opt.seed_key_bits = bits;
+    return prev;
+}
+
+int32_t gsais_profile_enable(void *ctx, int32_t on)
+{
+    gsais_ctx *c = resolve(ctx);
+    if (!c) return -1;
+    std::lock_guard<std::mutex> lock(c->mu);
+    const int32_t prev = c->prof.enabled ? 1 : 0;
+    c->prof.enabled = on != 0;
+    return prev;
+}
+
+int32_t gsais_profile_read(void *ctx, gsais_kernel_profile *out, int32_t max_kinds)
+{
+    gsais_ctx *c = resolve(ctx);
+    if (!c || !out) return -1;
+    std::lock_guard<std::mutex> lock(c->mu);
+    static const char *names[KK_COUNT] = {"onesweep", "upsweep", "seed", "round_keys", "tile_summary", "assign"};
+    int k = 0;
+    for (; k < KK_COUNT && k < max_kinds; ++k) {
+        out[k].name = names[k];
+        out[k].launches = (int64_t)c->prof.launches[k];
+        out[k].total_ms = c->prof.ms[k];
+        out[k].bytes = (int64_t)c->prof.bytes[k];
+    }
+    return k;
+}
+
+void gsais_profile_reset(void *ctx)
+{
+    gsais_ctx *c = resolve(ctx);
+    if (!c) return;
+    std::lock_guard<std::mutex> lock(c->mu);
+    c->prof.reset();
+}
+
+int64_t gsais_launch_count(void) { return (int64_t)g_launches.load(); }
+
+void gsais_release_workspace(void *ctx)
+{
+    gsais_ctx *c = resolve(ctx);
+    if (!c) return;
+    std::lock_guard<std::mutex> lock(c->mu);
+    if (c->ready && c->arena) {
+        DeviceGuard g(c->device);
+        cudaStreamSynchronize(c->stream);
+        cudaFree(c->arena);
+        c->arena = nullptr;
+        c->arena_bytes = 0;
+    }
+}
+
+}  // extern "C"

@@ -1,0 +1,75 @@
+// engine.h -- internal C++ interface between the CUDA translation units.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <vector>
+
+namespace gsais {
+
+// Number of kernels this library has launched (all contexts).
+extern std::atomic<uint64_t> g_launches;
+#define GSAIS_COUNTED(launch) do { launch; ::gsais::g_launches.fetch_add(1, std::memory_order_relaxed); } while (0)
+
+// Optional per-kernel timing: CUDA events recorded on the launching stream
+// around each launch of the instrumented kernels, resolved after the stream
+// synchronises.  `bytes` is the algorithmic traffic of the launch.
+enum KernelKind { KK_ONESWEEP = 0, KK_UPSWEEP, KK_SEED, KK_ROUND_KEYS, KK_SUMMARY, KK_ASSIGN, KK_COUNT };
+
+struct KernelProfiler {
+    bool enabled = false;
+    struct Rec { int kind; cudaEvent_t a, b; uint64_t bytes; };
+    std::vector<Rec> pending;
+    std::vector<cudaEvent_t> pool;
+    double ms[KK_COUNT] = {0};
+    uint64_t launches[KK_COUNT] = {0};
+    uint64_t bytes[KK_COUNT] = {0};
+
+    cudaEvent_t get();
+    // returns the start event to pair with end(); nullptr when disabled
+    cudaEvent_t begin(cudaStream_t st);
+    void end(int kind, cudaEvent_t a, cudaStream_t st, uint64_t bytes);
+    void flush();   // call after the stream has synchronised
+    void reset();
+    ~KernelProfiler();
+};
+
+// ---------------------------------------------------------------- radix sort
+// Onesweep LSD radix sort of (key, value) pairs: 8-bit digits, one upsweep
+// histogram pass for all digits, then one scatter pass per digit with a
+// decoupled look-back.  Digits on which every key agrees are skipped.
+struct RadixScratch {
+    uint32_t *hist = nullptr;      // [8][256] digit histograms
+    uint32_t *bases = nullptr;     // [8][256] exclusive bucket starts
+    uint64_t *status = nullptr;    // look-back words, 256 per tile
+    uint32_t *counters = nullptr;  // [8] tile tickets, one per pass
+    size_t status_words = 0;
+    uint32_t *h_hist = nullptr;    // pinned host copy of hist
+    KernelProfiler *prof = nullptr;
+};
+
+constexpr int kRadixThreads = 256;
+constexpr int kRadixItems = 16;
+constexpr int kRadixTile = kRadixThreads * kRadixItems;
+
+size_t radix_status_words(uint64_t n);
+
+// Sorts keys[0]/vals[0] by key bits [0, end_bit).  keys[1]/vals[1] are the
+// alternate buffers.  On success returns 0 and sets *which to the buffer
+// index holding the result; returns a CUDA error code otherwise.
+cudaError_t radix_sort_pairs(uint64_t *keys[2], uint32_t *vals[2], uint64_t n, int end_bit,
+                             RadixScratch &rs, uint32_t *d_err, cudaStream_t st, int *which,
+                             int *passes_run);
+
+// --------------------------------------------------------------- statistics
+struct SortStats {
+    int rounds = 0;                // doubling rounds after the seed sort
+    int seed_symbols = 0;          // symbols packed per seed key
+    int seed_bits = 0;             // bits per symbol code
+    uint64_t active_total = 0;     // sum of active suffixes over rounds
+    int radix_passes = 0;          // non-trivial digit passes over all sorts
+};
+
+}  // namespace gsais

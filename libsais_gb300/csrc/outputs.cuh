@@ -1,0 +1,32 @@
+// outputs.cuh -- kernels that derive BWT / auxiliary indexes / PLCP / LCP
+// from a finished suffix array (internal).  `err` is the context's device
+// error word: out-of-range indexes raise GSAIS_ERR_BOUNDS there.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace gsais {
+
+// U[0] = T[n-1]; U[k] = T[SA[row]-1] with the primary row skipped
+// (libsais src/libsais.c:7111-7118).  isa1 = rank array (ISA + 1).
+cudaError_t bwt_gather(const void *d_T, int symbytes, const uint32_t *d_SA, const uint32_t *d_isa1, uint64_t n,
+                       void *d_U, uint32_t *err, cudaStream_t st);
+
+// I[t] = ISA[t*r] + 1 for t = 0..(n-1)/r, as int32 (idx_bytes 4) or int64 (8).
+cudaError_t aux_sample(const uint32_t *d_isa1, uint64_t n, uint64_t r, void *d_I, int idx_bytes, cudaStream_t st);
+
+// int64 <-> uint32 index conversion (narrowing checks 0 <= v < n).
+cudaError_t widen_u32_to_i64(const uint32_t *src, int64_t *dst, uint64_t n, cudaStream_t st);
+cudaError_t narrow_i64_to_u32(const int64_t *src, uint32_t *dst, uint64_t n, uint32_t *err, cudaStream_t st);
+
+// PLCP of (T, SA) into d_PLCP (uint32), using d_sparse (plcp_sparse_words(n)
+// words) as scratch.  gsa stops at separators (src/libsais.c:8215-8238).
+size_t plcp_sparse_words(uint64_t n);
+cudaError_t plcp_build(const void *d_T, int symbytes, const uint32_t *d_SA, uint64_t n, bool gsa, uint32_t *d_PLCP,
+                       uint32_t *d_sparse, uint32_t *err, cudaStream_t st);
+
+// LCP[i] = PLCP[SA[i]].
+cudaError_t lcp_gather(const uint32_t *d_PLCP, const uint32_t *d_SA, uint32_t *d_LCP, uint64_t n, uint32_t *err,
+                       cudaStream_t st);
+
+}  // namespace gsais

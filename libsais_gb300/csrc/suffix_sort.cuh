@@ -1,0 +1,57 @@
+// suffix_sort.cuh -- prefix-doubling suffix sorter (device side, internal).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "engine.h"
+
+namespace gsais {
+
+// Device buffers used by one suffix sort of a text of n symbols.
+struct SortWorkspace {
+    uint32_t *rank = nullptr;      // n + 1: 1 + SA position of the suffix's group start; rank[n] = 0
+    uint32_t *sa = nullptr;        // n: the suffix array (output)
+    uint64_t *keys[2] = {nullptr, nullptr};
+    uint32_t *vals[2] = {nullptr, nullptr};
+    uint32_t *pos[2] = {nullptr, nullptr};   // SA slot of each active entry
+    uint32_t *gid[2] = {nullptr, nullptr};   // dense id of each active entry's group
+    uint32_t *tile_info = nullptr;           // 3 words per assign tile
+    uint32_t *tile_carry = nullptr;          // 3 words per assign tile
+    uint32_t *totals = nullptr;              // [4] kept entries, kept groups, ...
+    uint32_t *hist = nullptr;                // symbol histogram (256 or 65536)
+    uint16_t *codes = nullptr;               // dense symbol codes (256 or 65536)
+    RadixScratch radix;
+    uint32_t *h_small = nullptr;             // pinned host scratch (>= 65536 + 16 words)
+};
+
+// Bytes of device memory SortWorkspace needs for n symbols of `symbytes`
+// bytes (the text itself is not included).
+size_t sort_workspace_bytes(uint64_t n, int symbytes);
+
+// Carves a SortWorkspace out of `base` (which holds sort_workspace_bytes).
+void sort_workspace_carve(SortWorkspace &ws, void *base, uint64_t n, int symbytes, uint32_t *h_small,
+                          uint32_t *h_hist);
+
+struct SortOptions {
+    int seed_key_bits = 64;   // width of the packed seed prefix (32 or 64)
+};
+
+// Suffix array of the device text d_T (n symbols of `symbytes` bytes).  gsa
+// sorts as a generalized suffix array with 0 separators (the caller has
+// validated the text).  On return ws.sa holds SA, ws.rank holds ISA + 1,
+// ws.hist the symbol histogram and ws.h_small[16..] a host copy of it.  Returns a CUDA error (or cudaErrorUnknown
+// when the device error word was raised).
+cudaError_t suffix_sort(const void *d_T, int symbytes, uint64_t n, bool gsa, SortWorkspace &ws,
+                        const SortOptions &opt, uint32_t *d_err, cudaStream_t st, SortStats *stats);
+
+// Symbol histogram of a device text into d_hist and the pinned h_hist
+// (256 or 65536 counts); synchronises the stream.
+cudaError_t symbol_histogram(const void *d_T, int symbytes, uint64_t n, uint32_t *d_hist, uint32_t *h_hist,
+                             cudaStream_t st);
+
+// GSA validity of a device text: T[0] != 0, no two adjacent zeros,
+// T[n-1] == 0.  Result through a pinned host word.
+cudaError_t gsa_validate(const void *d_T, int symbytes, uint64_t n, uint32_t *d_flag, uint32_t *h_flag,
+                         cudaStream_t st, bool *valid);
+
+}  // namespace gsais

@@ -1,0 +1,246 @@
+"""GPU parity: every construction entry point, called through the C-ABI, must
+be bit-exact against the CPU oracle (itself pinned to the reference's golden
+vectors) on the same inputs.  Integer outputs, so the tolerance is zero."""
+import itertools
+import os
+
+import numpy as np
+import pytest
+
+import libsais_gb300 as G
+from libsais_gb300 import textgen
+from conftest import golden_cases, load_golden
+
+pytestmark = pytest.mark.gpu
+
+
+def check_all(oracle, T, gsa=False, plcp=True, r=8):
+    """SA, freq, BWT/primary, aux I, PLCP, LCP against the oracle."""
+    T = np.ascontiguousarray(T)
+    sixteen = T.dtype == np.uint16
+    ors, oSA, ofreq = oracle.libsais(T, gsa=gsa)
+    if gsa:
+        rc, SA, F = (G.libsais16_gsa if sixteen else G.libsais_gsa)(T)
+    else:
+        rc, SA, F = (G.libsais16 if sixteen else G.libsais)(T)
+    assert rc == ors == 0
+    assert np.array_equal(SA.astype(np.int64), oSA), "SA mismatch"
+    assert np.array_equal(F.astype(np.int64), ofreq), "freq mismatch"
+    if not gsa:
+        p, oU, oI, _ = oracle.libsais_bwt(T)
+        prim, U, _ = (G.libsais16_bwt if sixteen else G.libsais_bwt)(T)
+        assert prim == p, "primary index mismatch"
+        assert np.array_equal(U, oU), "BWT mismatch"
+        if r:
+            _, _, oI, _ = oracle.libsais_bwt(T, r=r)
+            rc, Ua, I, _ = (G.libsais16_bwt_aux if sixteen else G.libsais_bwt_aux)(T, r)
+            assert rc == 0 and np.array_equal(Ua, oU) and np.array_equal(I.astype(np.int64), oI)
+    if plcp:
+        oP = oracle.plcp(T, oSA, gsa=gsa)
+        if sixteen:
+            rc, P = (G.libsais16_plcp_gsa if gsa else G.libsais16_plcp)(T, SA)
+        else:
+            rc, P = (G.libsais_plcp_gsa if gsa else G.libsais_plcp)(T, SA)
+        assert rc == 0 and np.array_equal(P.astype(np.int64), oP), "PLCP mismatch"
+        rc, L = G.libsais_lcp(P, SA)
+        assert rc == 0 and np.array_equal(L.astype(np.int64), oracle.lcp(oP, oSA)), "LCP mismatch"
+    return SA
+
+
+@pytest.mark.parametrize("path", golden_cases(), ids=lambda p: os.path.basename(p)[:-4])
+def test_golden_vectors(path):
+    g = load_golden(path)
+    T, gsa = g["T"], bool(g["gsa"])
+    sixteen = T.dtype == np.uint16
+    f = (G.libsais16_gsa if gsa else G.libsais16) if sixteen else (G.libsais_gsa if gsa else G.libsais)
+    rc, SA, F = f(T)
+    assert rc == 0
+    assert np.array_equal(SA, g["SA"]) and np.array_equal(F, g["freq"])
+    if "U" in g:
+        prim, U, _ = (G.libsais16_bwt if sixteen else G.libsais_bwt)(T)
+        assert prim == int(g["primary"]) and np.array_equal(U, g["U"])
+    if "I8" in g:
+        rc, _, I, _ = G.libsais_bwt_aux(T, 8)
+        assert rc == 0 and np.array_equal(I, g["I8"])
+        rc, SA64, _ = G.libsais64(T)
+        assert rc == 0 and np.array_equal(SA64, g["SA"].astype(np.int64))
+    pf = (G.libsais16_plcp_gsa if gsa else G.libsais16_plcp) if sixteen else (G.libsais_plcp_gsa if gsa else G.libsais_plcp)
+    rc, P = pf(T, SA)
+    assert rc == 0 and np.array_equal(P, g["PLCP"])
+    rc, L = G.libsais_lcp(P, SA)
+    assert rc == 0 and np.array_equal(L, g["LCP"])
+
+
+def test_exhaustive_binary_strings(oracle):
+    """All strings over {A, C} of length 2..10 (SA and BWT)."""
+    for n in range(2, 11):
+        for bits in itertools.product(b"AC", repeat=n):
+            T = np.frombuffer(bytes(bits), dtype=np.uint8)
+            _, oSA = oracle.sa(T)
+            rc, SA, _ = G.libsais(T)
+            assert rc == 0 and np.array_equal(SA.astype(np.int64), oSA), bytes(bits)
+
+
+def test_random_small(oracle):
+    rng = np.random.default_rng(11)
+    for trial in range(300):
+        n = int(rng.integers(2, 300))
+        k = int(rng.integers(1, 6))
+        base = 0 if trial % 3 == 0 else 65
+        T = (rng.integers(0, k, n) + base).astype(np.uint8)
+        check_all(oracle, T, plcp=trial % 2 == 0, r=2 ** int(rng.integers(1, 5)))
+
+
+def test_random_small_u16(oracle):
+    rng = np.random.default_rng(12)
+    for trial in range(120):
+        n = int(rng.integers(2, 400))
+        T = (rng.integers(0, int(rng.integers(1, 7)), n) * 9973).astype(np.uint16)
+        check_all(oracle, T, plcp=True, r=4)
+
+
+def random_gsa(rng, count, maxlen, k):
+    parts = []
+    for _ in range(count):
+        parts.append(rng.integers(1, k + 1, int(rng.integers(1, maxlen + 1))).astype(np.uint8))
+        parts.append(np.zeros(1, np.uint8))
+    return np.concatenate(parts)
+
+
+def test_random_gsa(oracle):
+    rng = np.random.default_rng(13)
+    for trial in range(150):
+        T = random_gsa(rng, int(rng.integers(1, 30)), int(rng.integers(1, 40)), int(rng.integers(1, 4)))
+        check_all(oracle, T, gsa=True)
+
+
+def test_gsa_invalid_inputs_fill_freq(oracle):
+    for bad in ([0, 1, 2, 0], [1, 0, 0, 2, 0], [3, 1, 0, 0]):
+        T = np.array(bad, np.uint8)
+        rc, _, F = G.libsais_gsa(T)
+        assert rc == -1
+        if T[-1] == 0:   # past the host-side T[n-1] check, freq is filled as the reference does
+            assert np.array_equal(F.astype(np.int64), oracle.freq(T))
+
+
+@pytest.mark.parametrize("name,make", [
+    ("dna_iid_1M", lambda: textgen.iid(1 << 20, seed=1)),
+    ("genome_like_4M", lambda: textgen.genome_like(1 << 22, seed=2)),
+    ("all_A_1M", lambda: textgen.constant(1 << 20)),
+    ("period7_1M", lambda: textgen.periodic(1 << 20)),
+    ("bytes_1M", lambda: np.random.default_rng(3).integers(0, 256, 1 << 20).astype(np.uint8)),
+    ("zeros_256K", lambda: np.zeros(1 << 18, np.uint8)),
+    ("binary_1M", lambda: np.random.default_rng(4).integers(0, 2, 1 << 20).astype(np.uint8)),
+    ("dna_n_1M", lambda: textgen.dna_with_n(1 << 20, 0.01, seed=5)),
+])
+def test_medium_texts(oracle, name, make):
+    check_all(oracle, make())
+
+
+def test_medium_u16_zipf(oracle):
+    check_all(oracle, textgen.zipf_u16(1 << 20, seed=6))
+
+
+def test_medium_gsa_reads(oracle):
+    check_all(oracle, textgen.reads_gsa(1 << 14, ref_len=200_000, seed=4), gsa=True)
+
+
+def test_c1_workload(oracle):
+    """The plain single-string workload at full size: n = 2^24 i.i.d. ACGT."""
+    check_all(oracle, textgen.iid(1 << 24, seed=1), r=0)
+
+
+def test_64bit_api(oracle):
+    T = textgen.genome_like(1 << 20, seed=9)
+    _, oSA = oracle.sa(T)
+    rc, SA, F = G.libsais64(T)
+    assert rc == 0 and SA.dtype == np.int64 and np.array_equal(SA, oSA)
+    assert np.array_equal(F, oracle.freq(T))
+    p, oU, _, _ = oracle.libsais_bwt(T)
+    prim, U, _ = G.libsais64_bwt(T)
+    assert prim == p and np.array_equal(U, oU)
+    _, _, oI, _ = oracle.libsais_bwt(T, r=16)
+    rc, _, I, _ = G.libsais64_bwt_aux(T, 16)
+    assert rc == 0 and np.array_equal(I, oI)
+    rc, P = G.libsais64_plcp(T, SA)
+    oP = oracle.plcp(T, oSA)
+    assert rc == 0 and np.array_equal(P, oP)
+    rc, L = G.libsais64_lcp(P, SA)
+    assert rc == 0 and np.array_equal(L, oracle.lcp(oP, oSA))
+    G64 = textgen.reads_gsa(3000, ref_len=50_000, seed=10)
+    rc, SAg, _ = G.libsais64_gsa(G64)
+    assert rc == 0 and np.array_equal(SAg, oracle.sa(G64, gsa=True)[1])
+    rc, Pg = G.libsais64_plcp_gsa(G64, SAg)
+    assert rc == 0 and np.array_equal(Pg, oracle.plcp(G64, SAg, gsa=True))
+
+
+def test_context_reuse_across_sizes(oracle):
+    ctx = G.Context()
+    try:
+        for n, seed in ((1 << 18, 1), (1000, 2), (1 << 19, 3), (17, 4)):
+            T = textgen.iid(n, seed=seed)
+            rc, SA, _ = G.libsais(T, ctx=ctx)
+            assert rc == 0 and np.array_equal(SA.astype(np.int64), oracle.sa(T)[1])
+            p, U, _ = G.libsais_bwt(T, ctx=ctx)
+            po, Uo, _, _ = oracle.libsais_bwt(T)
+            assert p == po and np.array_equal(U, Uo)
+    finally:
+        ctx.close()
+
+
+def test_bwt_in_place(oracle):
+    """U may be T (include/libsais.h: 'can be T')."""
+    T = textgen.iid(5000, seed=3)
+    po, Uo, _, _ = oracle.libsais_bwt(T)
+    buf = T.copy()
+    rc, U, _, _ = G._bwt_call("libsais_bwt", buf, 4, U=buf)
+    assert rc == po and np.array_equal(buf, Uo)
+
+
+def test_lcp_may_alias_sa(oracle):
+    T = textgen.iid(7000, seed=4)
+    rc, SA, _ = G.libsais(T)
+    rc, P = G.libsais_plcp(T, SA)
+    expect = oracle.lcp(P.astype(np.int64), SA.astype(np.int64))
+    buf = SA.copy()
+    rc, L = G.libsais_lcp(P, buf, out=buf)
+    assert rc == 0 and np.array_equal(buf.astype(np.int64), expect)
+
+
+def test_combined_sa_bwt(oracle):
+    T = textgen.genome_like(1 << 20, seed=12)
+    prim, SA, U, F = G.sa_bwt(T)
+    p, oU, _, _ = oracle.libsais_bwt(T)
+    assert prim == p and np.array_equal(U, oU)
+    assert np.array_equal(SA.astype(np.int64), oracle.sa(T)[1])
+
+
+def test_device_api(oracle):
+    torch = pytest.importorskip("torch")
+    T = textgen.genome_like(1 << 20, seed=13)
+    dT = torch.from_numpy(T).cuda()
+    dSA = torch.empty(T.size, dtype=torch.int32, device="cuda")
+    dU = torch.empty(T.size, dtype=torch.uint8, device="cuda")
+    prim = G.sa_bwt_device(dT, dSA, dU, stream=torch.cuda.current_stream())
+    p, oU, _, _ = oracle.libsais_bwt(T)
+    _, oSA = oracle.sa(T)
+    assert prim == p
+    assert np.array_equal(dU.cpu().numpy(), oU)
+    assert np.array_equal(dSA.cpu().numpy().astype(np.int64), oSA)
+    dSA64 = torch.empty(T.size, dtype=torch.int64, device="cuda")
+    assert G.sa_device(dT, dSA64) == 0
+    assert np.array_equal(dSA64.cpu().numpy(), oSA)
+    dP = torch.empty_like(dSA)
+    assert G.plcp_device(dT, dSA, dP) == 0
+    oP = oracle.plcp(T, oSA)
+    assert np.array_equal(dP.cpu().numpy().astype(np.int64), oP)
+    dL = torch.empty_like(dSA)
+    assert G.lcp_device(dP, dSA, dL) == 0
+    assert np.array_equal(dL.cpu().numpy().astype(np.int64), oracle.lcp(oP, oSA))
+
+
+def test_stats_reported():
+    T = textgen.periodic(1 << 16)
+    rc, _, _ = G.libsais(T)
+    s = G.last_stats()
+    assert rc == 0 and s["rounds"] >= 1 and s["seed_symbols"] >= 8 and s["workspace_bytes"] > 0
