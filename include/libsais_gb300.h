@@ -104,6 +104,24 @@ extern "C" {
     /** Releases the device workspace cached by ctx (NULL: the process-wide context). */
     void gsais_release_workspace(void * ctx);
 
+    /**
+    * Suffix array of a device-resident text, allocating nothing.  No counterpart in
+    * the reference libsais: it exists for callers that cannot call cudaMalloc (code
+    * running under CUDA graph capture, inside a framework whose allocator owns all
+    * device memory, or on paths where an allocation may block).  All scratch comes
+    * from one fixed 4 MiB __device__ array that every GPU loading this library
+    * reserves until the library is unloaded; calls share it, so calls that overlap
+    * on the GPU race.  The first call on each device looks up the array's address
+    * (cudaGetSymbolAddress); make it before any stream capture.
+    * @param T [0..n-1] Device pointer to the text (symbytes 1 or 2).
+    * @param n The text length, at most 65536 symbols (longer texts return -1).
+    * @param gsa Non-zero for the generalized suffix array (0 separators, T[n-1] == 0).
+    * @param SA [0..n-1] Device pointer receiving the int32 suffix array.
+    * @param stream cudaStream_t to run on (NULL: the legacy default stream).
+    * @return 0 on success, -1 for invalid arguments or n > 65536, -2 on device failure.
+    */
+    int64_t gsais_sa_device_noalloc(const void * T, int32_t symbytes, int64_t n, int32_t gsa, void * SA, void * stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -101,6 +101,7 @@ _SIGS = {
     "gsais_profile_read": (_i32, [_p, _p, _i32]),
     "gsais_profile_reset": (None, [_p]),
     "gsais_launch_count": (_i64, []),
+    "gsais_sa_device_noalloc": (_i64, [_p, _i32, _i64, _i32, _p, _p]),
 }
 
 EXPORTED_SYMBOLS = tuple(_SIGS)
