@@ -109,7 +109,7 @@ extern "C" {
     * the reference libsais: it exists for callers that cannot call cudaMalloc (code
     * running under CUDA graph capture, inside a framework whose allocator owns all
     * device memory, or on paths where an allocation may block).  All scratch comes
-    * from one fixed 4 MiB __device__ array that every GPU loading this library
+    * from one fixed 6 MiB __device__ array that every GPU loading this library
     * reserves until the library is unloaded; calls share it, so calls that overlap
     * on the GPU race.  The first call on each device looks up the array's address
     * (cudaGetSymbolAddress); make it before any stream capture.

@@ -127,6 +127,48 @@ __device__ __forceinline__ T warp_inclusive_max(T v)
     return v;
 }
 
+// "Last non-zero" scans: the operator keeps the right operand when it is
+// non-zero, else the left one (associative).  Used to carry the value of the
+// most recent group head along a list whose groups are in any order.
+__device__ __forceinline__ uint32_t lastnz(uint32_t a, uint32_t b) { return b ? b : a; }
+
+__device__ __forceinline__ uint32_t warp_inclusive_lastnz(uint32_t v)
+{
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t u = __shfl_up_sync(GSAIS_FULL_MASK, v, o);
+        if (lane >= o) v = lastnz(u, v);
+    }
+    return v;
+}
+
+// Exclusive block-wide lastnz scan (identity 0); `warp_buf` >= blockDim.x/32.
+template <int THREADS>
+__device__ __forceinline__ uint32_t block_exclusive_lastnz(uint32_t v, uint32_t *warp_buf, uint32_t &total)
+{
+    constexpr int WARPS = THREADS / 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t inc = warp_inclusive_lastnz(v);
+    uint32_t exc = __shfl_up_sync(GSAIS_FULL_MASK, inc, 1);
+    if (lane == 0) exc = 0;
+    if (lane == 31) warp_buf[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t w = lane < WARPS ? warp_buf[lane] : 0u;
+        const uint32_t wi = warp_inclusive_lastnz(w);
+        uint32_t we = __shfl_up_sync(GSAIS_FULL_MASK, wi, 1);
+        if (lane == 0) we = 0;
+        if (lane < WARPS) warp_buf[lane] = we;
+        if (lane == WARPS - 1) warp_buf[WARPS] = wi;
+    }
+    __syncthreads();
+    const uint32_t r = lastnz(warp_buf[warp], exc);
+    total = warp_buf[WARPS];
+    __syncthreads();
+    return r;
+}
+
 // Exclusive block-wide sum; `warp_buf` holds at least blockDim.x/32 entries.
 // Returns the exclusive prefix for the calling thread and the block total.
 template <typename T, int THREADS>

@@ -138,6 +138,15 @@ int64_t fail(cudaError_t)
         if (_e != cudaSuccess) return fail(_e);              \
     } while (0)
 
+PackedText packed_of(const SortWorkspace &ws)
+{
+    PackedText pk;
+    pk.packed = ws.packed;
+    pk.pack_bits = ws.pack_bits;
+    for (int c = 0; c < 16; ++c) pk.decode[c] = ws.decode[c];
+    return pk;
+}
+
 // Workspace for one suffix sort carved after `extra` bytes of call buffers.
 struct SortPlan {
     size_t sort_bytes;
@@ -265,7 +274,7 @@ int64_t gsais_run_bwt(gsais_ctx *c, const void *T, int symbytes, int64_t n_, voi
     GS_TRY(cudaMemcpyAsync(d_T, T, n * symbytes, cudaMemcpyHostToDevice, st));
     const int64_t rc = run_sort(c, d_T, symbytes, n, false, ws, st);
     if (rc != 0) return rc;
-    GS_TRY(bwt_gather(d_T, symbytes, ws.sa, ws.rank, n, d_U, c->d_misc, st));
+    GS_TRY(bwt_gather(d_T, symbytes, ws.sa, ws.rank, n, d_U, packed_of(ws), c->d_misc, st));
     if (r > 0) GS_TRY(aux_sample(ws.rank, n, (uint64_t)r, d_I, idx_bytes, st));
     GS_TRY(cudaMemcpyAsync(c->h_small, ws.rank, 4, cudaMemcpyDeviceToHost, st));
     GS_TRY(cudaMemcpyAsync(U, d_U, n * symbytes, cudaMemcpyDeviceToHost, st));
@@ -407,7 +416,7 @@ int64_t gsais_sa_bwt_device(void *ctx, const void *T, int32_t symbytes, int64_t 
     if (!clear_err(c, st)) return fail(cudaErrorUnknown);
     const int64_t rc = run_sort(c, T, symbytes, n, false, ws, st);
     if (rc != 0) return rc;
-    GS_TRY(bwt_gather(T, symbytes, ws.sa, ws.rank, n, U, c->d_misc, st));
+    GS_TRY(bwt_gather(T, symbytes, ws.sa, ws.rank, n, U, packed_of(ws), c->d_misc, st));
     if (SA && sa_bytes == 8) GS_TRY(widen_u32_to_i64(ws.sa, static_cast<int64_t *>(SA), n, st));
     GS_TRY(cudaMemcpyAsync(c->h_small, ws.rank, 4, cudaMemcpyDeviceToHost, st));
     GS_TRY(sync_checked(c, st));
@@ -538,7 +547,8 @@ int32_t gsais_profile_read(void *ctx, gsais_kernel_profile *out, int32_t max_kin
     gsais_ctx *c = resolve(ctx);
     if (!c || !out) return -1;
     std::lock_guard<std::mutex> lock(c->mu);
-    static const char *names[KK_COUNT] = {"onesweep", "upsweep", "seed", "round_keys", "tile_summary", "assign"};
+    static const char *names[KK_COUNT] = {"onesweep", "upsweep", "seed", "round_keys", "tile_summary", "assign",
+                                          "small_groups"};
     int k = 0;
     for (; k < KK_COUNT && k < max_kinds; ++k) {
         out[k].name = names[k];

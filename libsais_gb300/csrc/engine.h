@@ -16,7 +16,7 @@ extern std::atomic<uint64_t> g_launches;
 // Optional per-kernel timing: CUDA events recorded on the launching stream
 // around each launch of the instrumented kernels, resolved after the stream
 // synchronises.  `bytes` is the algorithmic traffic of the launch.
-enum KernelKind { KK_ONESWEEP = 0, KK_UPSWEEP, KK_SEED, KK_ROUND_KEYS, KK_SUMMARY, KK_ASSIGN, KK_COUNT };
+enum KernelKind { KK_ONESWEEP = 0, KK_UPSWEEP, KK_SEED, KK_ROUND_KEYS, KK_SUMMARY, KK_ASSIGN, KK_SMALL, KK_COUNT };
 
 struct KernelProfiler {
     bool enabled = false;
@@ -50,18 +50,19 @@ struct RadixScratch {
     KernelProfiler *prof = nullptr;
 };
 
-constexpr int kRadixThreads = 256;
-constexpr int kRadixItems = 16;
-constexpr int kRadixTile = kRadixThreads * kRadixItems;
-
 size_t radix_status_words(uint64_t n);
 
 // Sorts keys[0]/vals[0] by key bits [0, end_bit).  keys[1]/vals[1] are the
 // alternate buffers.  On success returns 0 and sets *which to the buffer
 // index holding the result; returns a CUDA error code otherwise.
+// hist_ready: rs.hist already holds the digit histograms of keys[0] (the
+// producer accumulated them), so the upsweep read is skipped.
 cudaError_t radix_sort_pairs(uint64_t *keys[2], uint32_t *vals[2], uint64_t n, int end_bit,
                              RadixScratch &rs, uint32_t *d_err, cudaStream_t st, int *which,
-                             int *passes_run);
+                             int *passes_run, bool hist_ready = false);
+cudaError_t radix_sort_pairs32(uint32_t *keys[2], uint32_t *vals[2], uint64_t n, int end_bit,
+                               RadixScratch &rs, uint32_t *d_err, cudaStream_t st, int *which,
+                               int *passes_run, bool hist_ready = false);
 
 // --------------------------------------------------------------- statistics
 struct SortStats {
@@ -69,6 +70,7 @@ struct SortStats {
     int seed_symbols = 0;          // symbols packed per seed key
     int seed_bits = 0;             // bits per symbol code
     uint64_t active_total = 0;     // sum of active suffixes over rounds
+    uint64_t large_total = 0;      // sum over rounds of suffixes in groups sorted by the radix path
     int radix_passes = 0;          // non-trivial digit passes over all sorts
 };
 

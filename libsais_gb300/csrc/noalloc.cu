@@ -11,7 +11,7 @@
 //
 // Limits and sharing rules:
 //   * texts of at most kNoAllocMaxN = 65,536 symbols; longer texts get -1;
-//   * the scratch array (kNoAllocScratchBytes = 4 MiB) is reserved on every
+//   * the scratch array (kNoAllocScratchBytes = 6 MiB) is reserved on every
 //     GPU that loads this library, for as long as the library stays loaded;
 //   * every call uses the same array and the array keeps the previous call's
 //     contents; the sort clears everything that must start at zero;
@@ -33,15 +33,15 @@ using namespace gsais;
 namespace {
 
 constexpr uint64_t kNoAllocMaxN = 65536;
-constexpr size_t kNoAllocScratchBytes = (size_t)4 << 20;
+constexpr size_t kNoAllocScratchBytes = (size_t)6 << 20;
 constexpr int kMaxDevices = 64;
 
 // The only device memory the entry point uses.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
 // Host-side read-back buffers (ordinary static storage, no allocation).
-static uint32_t g_host_small[16 + 65536 + 32768];
-static uint32_t g_host_hist[8 * 256];
+alignas(16) static uint32_t g_host_small[16 + 65536 + 32768];
+alignas(16) static uint32_t g_host_hist[8 * 256];
 static uint32_t g_host_flag[4];
 
 std::mutex g_noalloc_mu;

@@ -32,9 +32,12 @@ int grid_for(uint64_t items, int threads)
 // (libsais src/libsais.c:4777/:5396 write T[p-1] during the final induction).
 template <typename Sym>
 __global__ void __launch_bounds__(256) k_bwt(const Sym *__restrict__ T, const uint32_t *__restrict__ SA, uint64_t n,
-                                             const uint32_t *__restrict__ isa1, Sym *__restrict__ U,
+                                             const uint32_t *__restrict__ isa1, Sym *__restrict__ U, PackedText pk,
                                              uint32_t *__restrict__ err)
 {
+    __shared__ Sym dec[16];
+    if (threadIdx.x < 16) dec[threadIdx.x] = (Sym)pk.decode[threadIdx.x];
+    __syncthreads();
     const uint64_t i0 = (uint64_t)isa1[0] - 1;   // SA row of suffix 0
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
@@ -47,7 +50,15 @@ __global__ void __launch_bounds__(256) k_bwt(const Sym *__restrict__ T, const ui
                 atomicOr(err, GSAIS_ERR_BOUNDS);
                 continue;
             }
-            U[k] = T[p - 1];
+            if (pk.pack_bits == 2) {
+                const uint32_t w = reinterpret_cast<const uint16_t *>(pk.packed)[(p - 1) >> 3];
+                U[k] = dec[(w >> (2 * ((p - 1) & 7))) & 3u];
+            } else if (pk.pack_bits == 4) {
+                const uint32_t w = reinterpret_cast<const uint32_t *>(pk.packed)[(p - 1) >> 3];
+                U[k] = dec[(w >> (4 * ((p - 1) & 7))) & 15u];
+            } else {
+                U[k] = T[p - 1];
+            }
         }
     }
 }
@@ -227,15 +238,15 @@ cudaError_t plcp_run(const Sym *T, const uint32_t *SA, uint64_t n, uint32_t *plc
 }  // namespace
 
 cudaError_t bwt_gather(const void *d_T, int symbytes, const uint32_t *d_SA, const uint32_t *d_isa1, uint64_t n,
-                       void *d_U, uint32_t *err, cudaStream_t st)
+                       void *d_U, const PackedText &pk, uint32_t *err, cudaStream_t st)
 {
     if (n == 0) return cudaSuccess;
     if (symbytes == 1)
         GSAIS_COUNTED((k_bwt<uint8_t><<<grid_for(n, 256), 256, 0, st>>>(
-            static_cast<const uint8_t *>(d_T), d_SA, n, d_isa1, static_cast<uint8_t *>(d_U), err)));
+            static_cast<const uint8_t *>(d_T), d_SA, n, d_isa1, static_cast<uint8_t *>(d_U), pk, err)));
     else
         GSAIS_COUNTED((k_bwt<uint16_t><<<grid_for(n, 256), 256, 0, st>>>(
-            static_cast<const uint16_t *>(d_T), d_SA, n, d_isa1, static_cast<uint16_t *>(d_U), err)));
+            static_cast<const uint16_t *>(d_T), d_SA, n, d_isa1, static_cast<uint16_t *>(d_U), pk, err)));
     return cudaGetLastError();
 }
 

@@ -9,8 +9,16 @@ namespace gsais {
 
 // U[0] = T[n-1]; U[k] = T[SA[row]-1] with the primary row skipped
 // (libsais src/libsais.c:7111-7118).  isa1 = rank array (ISA + 1).
+// With pack_bits 2 or 4 the symbols are read from the packed code text
+// (positions p at bits [(p % per)*pack_bits, ...) of word p / per) and mapped
+// back through decode[], which keeps the gather inside L2 for DNA-like texts.
+struct PackedText {
+    const uint8_t *packed = nullptr;
+    int pack_bits = 0;
+    uint16_t decode[16] = {0};
+};
 cudaError_t bwt_gather(const void *d_T, int symbytes, const uint32_t *d_SA, const uint32_t *d_isa1, uint64_t n,
-                       void *d_U, uint32_t *err, cudaStream_t st);
+                       void *d_U, const PackedText &pk, uint32_t *err, cudaStream_t st);
 
 // I[t] = ISA[t*r] + 1 for t = 0..(n-1)/r, as int32 (idx_bytes 4) or int64 (8).
 cudaError_t aux_sample(const uint32_t *d_isa1, uint64_t n, uint64_t r, void *d_I, int idx_bytes, cudaStream_t st);

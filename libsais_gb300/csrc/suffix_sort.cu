@@ -30,6 +30,7 @@
 
 #include "device_util.cuh"
 #include "engine.h"
+#include "radix_hist.cuh"
 #include "suffix_sort.cuh"
 
 namespace gsais {
@@ -91,51 +92,82 @@ __global__ void __launch_bounds__(256) k_hist_u16(const uint16_t *__restrict__ T
 }
 
 // ------------------------------------------------------------------ seed
-// Bytes per suffix: T 1-2 (staged), key 8 + value 4 written.
-template <typename Sym>
+// Packed K-symbol prefix of every suffix.  Each thread builds the keys of 8
+// consecutive positions: the highest one from its K codes, the others by
+// sliding the window one symbol left (key(i) = code(T[i]) on top of
+// key(i+1) >> bits; a separator zeroes the rest for the GSA).  Keys are
+// staged in shared memory and written out coalesced, in reverse text order
+// for plain texts (see the tail rule above).
+// The same pass accumulates the digit histograms of the keys for the radix
+// sort and, for small alphabets (codes of <= 4 bits), writes the text as
+// packed codes (pack_bits 2 or 4) for the BWT gather.
+// Bytes per suffix: T s read (staged), key sizeof(KeyT) + value 4 written
+// (+ pack_bits/8 for the packed text).
+template <typename Sym, typename KeyT>
 __global__ void __launch_bounds__(256) k_seed(const Sym *__restrict__ T, uint64_t n, const uint16_t *__restrict__ codes,
-                                              int bits, int K, int gsa, uint64_t *__restrict__ keys,
-                                              uint32_t *__restrict__ vals)
+                                              int bits, int K, int gsa, KeyT *__restrict__ keys,
+                                              uint32_t *__restrict__ vals, int passes, int end_bit,
+                                              uint32_t *__restrict__ hist, int pack_bits,
+                                              uint8_t *__restrict__ packed)
 {
+    constexpr int PER = kSeedTile / 256;
     __shared__ uint16_t sc[kSeedTile + 64];
-    const uint64_t base = (uint64_t)blockIdx.x * kSeedTile;
-    for (int q = threadIdx.x; q < kSeedTile + K - 1; q += blockDim.x) {
-        const uint64_t p = base + q;
-        sc[q] = p < n ? codes[T[p]] : (uint16_t)0;
+    __shared__ KeyT sk[kSeedTile];
+    __shared__ uint32_t sh[kMaxRadixPasses][256];
+    radix_hist_zero(sh, passes);
+    const uint64_t tiles = (n + kSeedTile - 1) / kSeedTile;
+    const int r0 = threadIdx.x * PER;
+    const int top = (K - 1) * bits;
+    for (uint64_t t = blockIdx.x; t < tiles; t += gridDim.x) {
+        const uint64_t base = t * kSeedTile;
+        __syncthreads();   // previous tile's sk/sc reads are done
+        for (int q = threadIdx.x; q < kSeedTile + K - 1; q += blockDim.x) {
+            const uint64_t p = base + q;
+            sc[q] = p < n ? codes[T[p]] : (uint16_t)0;
+        }
+        __syncthreads();
+        KeyT key = 0;
+        {
+            bool term = false;
+            for (int q = 0; q < K; ++q) {
+                const KeyT c = term ? KeyT(0) : (KeyT)sc[r0 + PER - 1 + q];
+                key = (KeyT)((key << bits) | c);
+                if (gsa && c == 0) term = true;
+            }
+        }
+        sk[r0 + PER - 1] = key;
+#pragma unroll
+        for (int r = PER - 2; r >= 0; --r) {
+            const KeyT c = (KeyT)sc[r0 + r];
+            key = (gsa && c == 0) ? KeyT(0) : (KeyT)((c << top) | (key >> bits));
+            sk[r0 + r] = key;
+        }
+        if (pack_bits == 2) {
+            uint32_t w = 0;
+#pragma unroll
+            for (int r = 0; r < PER; ++r) w |= (uint32_t)(sc[r0 + r] & 3u) << (2 * r);
+            reinterpret_cast<uint16_t *>(packed)[(base + r0) / PER] = (uint16_t)w;
+        } else if (pack_bits == 4) {
+            uint32_t w = 0;
+#pragma unroll
+            for (int r = 0; r < PER; ++r) w |= (uint32_t)(sc[r0 + r] & 15u) << (4 * r);
+            reinterpret_cast<uint32_t *>(packed)[(base + r0) / PER] = w;
+        }
+        __syncthreads();
+        for (int r = threadIdx.x; r < kSeedTile; r += blockDim.x) {
+            const uint64_t i = base + r;
+            const bool ok = i < n;
+            const KeyT k = sk[r];
+            if (ok) {
+                const uint64_t j = gsa ? i : n - 1 - i;
+                keys[j] = k;
+                vals[j] = (uint32_t)i;
+            }
+            radix_hist_add(sh, (uint64_t)k, ok, passes, end_bit);
+        }
     }
     __syncthreads();
-    for (int r = threadIdx.x; r < kSeedTile; r += blockDim.x) {
-        const uint64_t i = base + r;
-        if (i >= n) break;
-        uint64_t key = 0;
-        bool term = false;
-        for (int q = 0; q < K; ++q) {
-            const uint32_t c = term ? 0u : (uint32_t)sc[r + q];
-            key = (key << bits) | c;
-            if (gsa && c == 0) term = true;
-        }
-        const uint64_t j = gsa ? i : n - 1 - i;
-        keys[j] = key;
-        vals[j] = (uint32_t)i;
-    }
-}
-
-// ------------------------------------------------------------ round keys
-// Bytes per active suffix: index 4 + group 4 read, rank gather 4, key 8 written.
-__global__ void __launch_bounds__(256) k_round_keys(const uint32_t *__restrict__ act_i,
-                                                    const uint32_t *__restrict__ act_gid,
-                                                    const uint32_t *__restrict__ rank, uint64_t h, uint64_t N,
-                                                    uint64_t n, int b2, uint64_t *__restrict__ keys,
-                                                    uint32_t *__restrict__ err)
-{
-    const uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= N) return;
-    const uint64_t i = act_i[j];
-    // an active suffix has length >= h, so i + h <= n (rank[n] is the sentinel)
-    uint32_t r2 = 0;
-    if (i + h <= n) r2 = rank[i + h];
-    else atomicOr(err, GSAIS_ERR_BOUNDS);
-    keys[j] = ((uint64_t)act_gid[j] << b2) | (uint64_t)r2;
+    radix_hist_flush(sh, passes, hist);
 }
 
 // --------------------------------------------------- head / assign tiles
@@ -143,6 +175,7 @@ enum { MODE_INIT_PLAIN = 0, MODE_INIT_GSA = 1, MODE_ROUND = 2 };
 
 struct TileArgs {
     const uint64_t *keys;
+    const uint32_t *keys32;  // non-null: 32-bit keys (the seed round with short seeds)
     const uint32_t *vals;
     const uint32_t *pos;     // nullptr: identity (the seed round)
     uint64_t N;              // entries in this round
@@ -165,7 +198,7 @@ __device__ __forceinline__ uint32_t stage_tile(const TileArgs &a, uint64_t base,
     for (int x = threadIdx.x; x < (int)valid + 2; x += blockDim.x) {
         const int64_t j = (int64_t)base + x - 1;
         const bool in = j >= 0 && (uint64_t)j < a.N;
-        s_keys[x] = in ? a.keys[j] : 0ull;
+        s_keys[x] = in ? (a.keys32 ? (uint64_t)a.keys32[j] : a.keys[j]) : 0ull;
         if (need_vals) s_vals[x] = in ? a.vals[j] : 0u;
     }
     __syncthreads();
@@ -221,30 +254,43 @@ __global__ void __launch_bounds__(kAssignThreads) k_tile_summary(TileArgs a, uin
     __shared__ uint64_t s_keys[kAssignTile + 2];
     __shared__ uint32_t s_vals[kAssignTile + 2];
     __shared__ uint32_t s_red[3][kAssignWarps];
+    __shared__ int s_redx[kAssignWarps];
     const uint64_t base = (uint64_t)blockIdx.x * kAssignTile;
     const uint32_t valid = stage_tile(a, base, s_keys, s_vals, MODE == MODE_INIT_PLAIN);
-    uint32_t mx = 0, kept = 0, kh = 0;
+    uint32_t mx = 0, kept = 0, kh = 0;   // mx: value of the last head (highest index) of the tile
+    int mxx = -1;
     for (int x = threadIdx.x; x < (int)valid; x += blockDim.x) {
         const uint64_t j = base + x;
         const uint32_t pos = a.pos ? a.pos[j] : (uint32_t)j;
         const ElemFlags f = elem_flags<MODE>(a, base, x, s_keys, s_vals, pos);
-        mx = f.hv > mx ? f.hv : mx;
+        if (f.hv) {
+            mx = f.hv;
+            mxx = x;
+        }
         kept += f.kept;
         kh += f.kh;
     }
     for (int o = 16; o > 0; o >>= 1) {
         const uint32_t m2 = __shfl_down_sync(GSAIS_FULL_MASK, mx, o);
-        mx = m2 > mx ? m2 : mx;
+        const int x2 = __shfl_down_sync(GSAIS_FULL_MASK, mxx, o);
+        if (x2 > mxx) {
+            mxx = x2;
+            mx = m2;
+        }
         kept += __shfl_down_sync(GSAIS_FULL_MASK, kept, o);
         kh += __shfl_down_sync(GSAIS_FULL_MASK, kh, o);
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) { s_red[0][warp] = mx; s_red[1][warp] = kept; s_red[2][warp] = kh; }
+    if (lane == 0) { s_red[0][warp] = mx; s_red[1][warp] = kept; s_red[2][warp] = kh; s_redx[warp] = mxx; }
     __syncthreads();
     if (threadIdx.x == 0) {
         uint32_t M = 0, A = 0, B = 0;
+        int MX = -1;
         for (int w = 0; w < kAssignWarps; ++w) {
-            M = s_red[0][w] > M ? s_red[0][w] : M;
+            if (s_redx[w] > MX) {
+                MX = s_redx[w];
+                M = s_red[0][w];
+            }
             A += s_red[1][w];
             B += s_red[2][w];
         }
@@ -256,31 +302,31 @@ __global__ void __launch_bounds__(kAssignThreads) k_tile_summary(TileArgs a, uin
 
 // Exclusive scan of the tile summaries (single CTA): carry[t] = (max, sum, sum)
 // over tiles < t; totals[0] = kept entries, totals[1] = kept groups.
+// `base` (nullable) = (groups << 32 | entries) already emitted by the
+// small-group path of the same round; survivors and groups follow them.
 __global__ void __launch_bounds__(1024) k_tile_scan(const uint32_t *__restrict__ info, uint32_t *__restrict__ carry,
-                                                    uint64_t tiles, uint32_t *__restrict__ totals)
+                                                    uint64_t tiles, uint32_t *__restrict__ totals,
+                                                    const unsigned long long *__restrict__ base)
 {
     __shared__ uint32_t wb[3][33];
-    uint32_t cm = 0, ck = 0, ch = 0;
+    const unsigned long long b0 = base ? *base : 0ull;
+    uint32_t cm = 0, ck = (uint32_t)b0, ch = (uint32_t)(b0 >> 32);
     for (uint64_t c0 = 0; c0 < tiles; c0 += 1024) {
         const uint64_t t = c0 + threadIdx.x;
         const bool ok = t < tiles;
         const uint32_t m = ok ? info[3 * t + 0] : 0u;
         const uint32_t k = ok ? info[3 * t + 1] : 0u;
         const uint32_t h = ok ? info[3 * t + 2] : 0u;
-        uint32_t tk, th;
-        const uint32_t em = block_exclusive_max<uint32_t, 1024>(m, wb[0]);
+        uint32_t tk, th, tm;
+        const uint32_t em = block_exclusive_lastnz<1024>(m, wb[0], tm);
         const uint32_t ek = block_exclusive_sum<uint32_t, 1024>(k, wb[1], tk);
         const uint32_t eh = block_exclusive_sum<uint32_t, 1024>(h, wb[2], th);
         if (ok) {
-            carry[3 * t + 0] = em > cm ? em : cm;
+            carry[3 * t + 0] = lastnz(cm, em);
             carry[3 * t + 1] = ck + ek;
             carry[3 * t + 2] = ch + eh;
         }
-        // block max of this chunk: the last thread's inclusive value
-        __shared__ uint32_t s_lastmax;
-        if (threadIdx.x == 1023) s_lastmax = em > m ? em : m;
-        __syncthreads();
-        cm = s_lastmax > cm ? s_lastmax : cm;
+        cm = lastnz(cm, tm);
         ck += tk;
         ch += th;
         __syncthreads();
@@ -294,7 +340,8 @@ __global__ void __launch_bounds__(1024) k_tile_scan(const uint32_t *__restrict__
 template <int MODE>
 __global__ void __launch_bounds__(kAssignThreads)
     k_assign(TileArgs a, const uint32_t *__restrict__ carry, uint32_t *__restrict__ rank, uint32_t *__restrict__ sa,
-             uint32_t *__restrict__ out_i, uint32_t *__restrict__ out_pos, uint32_t *__restrict__ out_gid)
+             uint32_t *__restrict__ out_i, uint32_t *__restrict__ out_pos, uint32_t *__restrict__ out_gid,
+             uint32_t *__restrict__ gstart_out)
 {
     __shared__ uint64_t s_keys[kAssignTile + 2];
     __shared__ uint32_t s_vals[kAssignTile + 2];
@@ -304,7 +351,7 @@ __global__ void __launch_bounds__(kAssignThreads)
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
     uint32_t hv_inc[kAssignPerLane], k_exc[kAssignPerLane], h_inc[kAssignPerLane], posv[kAssignPerLane];
-    bool single[kAssignPerLane];
+    bool single[kAssignPerLane], khead[kAssignPerLane];
     uint32_t run_m = 0, run_k = 0, run_h = 0;
 #pragma unroll
     for (int q = 0; q < kAssignPerLane; ++q) {
@@ -319,8 +366,9 @@ __global__ void __launch_bounds__(kAssignThreads)
         }
         posv[q] = pos;
         single[q] = f.single;
-        uint32_t m = warp_inclusive_max(f.hv);
-        m = m > run_m ? m : run_m;
+        khead[q] = f.kh != 0;
+        uint32_t m = warp_inclusive_lastnz(f.hv);
+        m = lastnz(run_m, m);
         const uint32_t ki = warp_inclusive_sum(f.kept);
         const uint32_t hi = warp_inclusive_sum(f.kh);
         hv_inc[q] = m;
@@ -334,7 +382,7 @@ __global__ void __launch_bounds__(kAssignThreads)
     __syncthreads();
     uint32_t wm = carry[3 * blockIdx.x + 0], wk = carry[3 * blockIdx.x + 1], wh = carry[3 * blockIdx.x + 2];
     for (int w = 0; w < warp; ++w) {
-        wm = s_w[0][w] > wm ? s_w[0][w] : wm;
+        wm = lastnz(wm, s_w[0][w]);
         wk += s_w[1][w];
         wh += s_w[2][w];
     }
@@ -343,7 +391,7 @@ __global__ void __launch_bounds__(kAssignThreads)
         const int x = warp * 256 + q * 32 + lane;
         if (x >= (int)valid) continue;
         const uint32_t v = s_vals[x + 1];
-        const uint32_t r = hv_inc[q] > wm ? hv_inc[q] : wm;
+        const uint32_t r = lastnz(wm, hv_inc[q]);
         rank[v] = r;
         if (single[q]) {
             sa[posv[q]] = v;
@@ -351,8 +399,261 @@ __global__ void __launch_bounds__(kAssignThreads)
             const uint32_t c = wk + k_exc[q];
             out_i[c] = v;
             out_pos[c] = posv[q];
-            out_gid[c] = wh + h_inc[q] - 1;
+            const uint32_t g = wh + h_inc[q] - 1;
+            out_gid[c] = g;
+            if (khead[q]) gstart_out[g] = c;
         }
+    }
+}
+
+// ------------------------------------------------- rounds: small / large
+// Groups of at most kSmallMax suffixes are split inside one warp (no global
+// sort); larger groups go through the onesweep radix sort keyed by
+// (dense large-group id, rank[i + h]).
+constexpr uint32_t kSmallMax = 32;
+constexpr uint32_t kNoLarge = 0xFFFFFFFFu;
+
+// Per group: size from the group table; large groups get an id and a slot
+// range in the large list from one combined counter, so ids and ranges are
+// in the same order.  Bytes per group: 8 read, 4-8 written.
+__global__ void __launch_bounds__(256) k_classify(const uint32_t *__restrict__ gstart, uint64_t G, uint64_t N,
+                                                  uint32_t *__restrict__ lid, uint32_t *__restrict__ loff,
+                                                  unsigned long long *__restrict__ lcount)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < G; g += stride) {
+        const uint64_t s = gstart[g];
+        const uint64_t e = g + 1 < G ? gstart[g + 1] : N;
+        const uint64_t size = e - s;
+        if (size > kSmallMax) {
+            const unsigned long long old = atomicAdd(lcount, (1ull << 32) | size);
+            lid[g] = (uint32_t)(old >> 32);
+            loff[g] = (uint32_t)old;
+        } else {
+            lid[g] = kNoLarge;
+        }
+    }
+}
+
+// Gathers rank[i + h] of every active suffix (before any rank of this round
+// changes).  Entries of small groups keep it in r2[]; entries of large groups
+// are copied to the large list with key (large id << b2 | rank), and the
+// key's digit histograms are accumulated for the radix sort.
+// Bytes per active suffix: index 4 + slot 4 + group 4 read, rank gather 4,
+// group table 8 read; 4 (r2) or 16 (large list) written.
+__global__ void __launch_bounds__(256) k_round_r2(const uint32_t *__restrict__ act_i,
+                                                  const uint32_t *__restrict__ act_pos,
+                                                  const uint32_t *__restrict__ act_gid,
+                                                  const uint32_t *__restrict__ gstart, const uint32_t *__restrict__ lid,
+                                                  const uint32_t *__restrict__ loff, const uint32_t *__restrict__ rank,
+                                                  uint64_t h, uint64_t N, uint64_t n, int b2, uint32_t *__restrict__ r2o,
+                                                  uint64_t *__restrict__ lkeys, uint32_t *__restrict__ lvals,
+                                                  uint32_t *__restrict__ lpos, uint32_t *__restrict__ err, int passes,
+                                                  int end_bit, uint32_t *__restrict__ hist)
+{
+    __shared__ uint32_t sh[kMaxRadixPasses][256];
+    radix_hist_zero(sh, passes);
+    __syncthreads();
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t N_round = (N + 31) & ~31ull;   // whole warps iterate together
+    for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < N_round; j += stride) {
+        bool large = false;
+        uint64_t key = 0;
+        if (j < N) {
+            const uint64_t i = act_i[j];
+            // an active suffix has length >= h, so i + h <= n (rank[n] is the sentinel)
+            uint32_t r2 = 0;
+            if (i + h <= n) r2 = rank[i + h];
+            else atomicOr(err, GSAIS_ERR_BOUNDS);
+            const uint32_t g = act_gid[j];
+            const uint32_t L = lid[g];
+            if (L == kNoLarge) {
+                r2o[j] = r2;
+            } else {
+                large = true;
+                const uint64_t d = (uint64_t)loff[g] + (j - gstart[g]);
+                key = ((uint64_t)L << b2) | r2;
+                lkeys[d] = key;
+                lvals[d] = (uint32_t)i;
+                lpos[d] = act_pos[j];
+            }
+        }
+        radix_hist_add(sh, key, large, passes, end_bit);
+    }
+    __syncthreads();
+    radix_hist_flush(sh, passes, hist);
+}
+
+// Splits the small groups.  A warp takes a window of 32 list positions and
+// owns the groups that start in it (with their members: at most 63
+// entries, two per lane).  For each owned suffix, counting over its group's
+// members gives lt (members with smaller rank[i+h]), eq and its new slot;
+// rank = 1 + first slot of its new subgroup; a subgroup of one is final
+// (SA[slot] = i); survivors are written in slot order behind one atomic
+// reservation per CTA of (groups, entries), which keeps group ids increasing
+// with list position.  Bytes per suffix: 16 read, rank scatter 4, SA 4 or
+// survivors 12-16 written.
+__global__ void __launch_bounds__(256) k_small_groups(const uint32_t *__restrict__ act_i,
+                                                      const uint32_t *__restrict__ act_pos,
+                                                      const uint32_t *__restrict__ act_gid,
+                                                      const uint32_t *__restrict__ r2, uint64_t N,
+                                                      uint32_t *__restrict__ rank, uint32_t *__restrict__ sa,
+                                                      uint32_t *__restrict__ out_i, uint32_t *__restrict__ out_pos,
+                                                      uint32_t *__restrict__ out_gid,
+                                                      uint32_t *__restrict__ gstart_out,
+                                                      unsigned long long *__restrict__ counter)
+{
+    constexpr int WARPS = 8;
+    __shared__ uint32_t s_we[WARPS], s_wg[WARPS];
+    __shared__ unsigned long long s_base;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint64_t wb = ((uint64_t)blockIdx.x * WARPS + warp) * 32;
+    const uint64_t j0 = wb + lane, j1 = wb + 32 + lane;
+    const bool v0 = j0 < N, v1 = j1 < N;
+    const uint32_t g0 = v0 ? act_gid[j0] : 0xFFFFFFFFu;
+    const uint32_t g1 = v1 ? act_gid[j1] : 0xFFFFFFFEu;
+    uint32_t pg0 = __shfl_up_sync(GSAIS_FULL_MASK, g0, 1);
+    uint32_t pg1 = __shfl_up_sync(GSAIS_FULL_MASK, g1, 1);
+    const uint32_t g0_last = __shfl_sync(GSAIS_FULL_MASK, g0, 31);
+    if (lane == 0) {
+        pg0 = (wb > 0 && wb - 1 < N) ? act_gid[wb - 1] : ~g0;
+        pg1 = g0_last;
+    }
+    const bool head0 = v0 && (j0 == 0 || g0 != pg0);
+    const bool head1 = v1 && g1 != pg1;
+    const uint64_t H = (uint64_t)__ballot_sync(GSAIS_FULL_MASK, head0) |
+                       ((uint64_t)__ballot_sync(GSAIS_FULL_MASK, head1) << 32);
+
+    // group [gs, ge) (window offsets) of offset o; gs = -1 if it started before the window
+    auto group_of = [&](int o, int &gs, int &ge) {
+        const uint64_t upto = o == 63 ? ~0ull : ((2ull << o) - 1);
+        const uint64_t m = H & upto;
+        gs = m ? 63 - __clzll((long long)m) : -1;
+        const uint64_t above = H & ~upto;
+        ge = above ? __ffsll((long long)above) - 1 : 64;
+    };
+    int gs[2], ge[2];
+    group_of(lane, gs[0], ge[0]);
+    group_of(32 + lane, gs[1], ge[1]);
+    bool own[2];
+    for (int e = 0; e < 2; ++e) {
+        const uint64_t j = e ? j1 : j0;
+        bool ok = (e ? v1 : v0) && gs[e] >= 0 && gs[e] < 32;
+        if (ok) {
+            const uint64_t start = wb + gs[e];
+            const uint64_t end = (ge[e] == 64 || wb + ge[e] > N) ? N : wb + ge[e];
+            // a group reaching the window end may continue: it is large then
+            const bool open = ge[e] == 64 && wb + 64 < N;
+            ok = !open && end - start <= kSmallMax;
+        }
+        (void)j;
+        own[e] = ok;
+    }
+    const uint32_t rr0 = own[0] ? r2[j0] : 0u, rr1 = own[1] ? r2[j1] : 0u;
+    const uint32_t p0 = own[0] ? act_pos[j0] : 0u, p1 = own[1] ? act_pos[j1] : 0u;
+    const uint32_t i0 = own[0] ? act_i[j0] : 0u, i1 = own[1] ? act_i[j1] : 0u;
+
+    // group end inside the window (the list may end before offset 64);
+    // the widest owned group of the warp bounds the member loops
+    int gend[2];
+    int sz_me = 0;
+    for (int e = 0; e < 2; ++e) {
+        gend[e] = (ge[e] == 64 || wb + ge[e] > N) ? (int)(N - wb < 64 ? N - wb : 64) : ge[e];
+        if (own[e]) {
+            const int sz = gend[e] - gs[e];
+            sz_me = sz > sz_me ? sz : sz_me;
+        }
+    }
+    const int maxsz = (int)__reduce_max_sync(GSAIS_FULL_MASK, (uint32_t)sz_me);
+
+    uint32_t lt[2] = {0, 0}, eq[2] = {0, 0}, before[2] = {0, 0};
+    const uint32_t myr[2] = {rr0, rr1};
+    for (int t = 0; t < maxsz; ++t) {
+        for (int e = 0; e < 2; ++e) {
+            const int src = (gs[e] < 0 ? 0 : gs[e]) + t;
+            const uint32_t a = __shfl_sync(GSAIS_FULL_MASK, rr0, src & 31);
+            const uint32_t b = __shfl_sync(GSAIS_FULL_MASK, rr1, src & 31);
+            const uint32_t rt = src >= 32 ? b : a;
+            const int o = e ? 32 + lane : lane;
+            if (own[e] && src < gend[e]) {
+                lt[e] += rt < myr[e];
+                eq[e] += rt == myr[e];
+                before[e] += (rt < myr[e]) || (rt == myr[e] && src < o);
+            }
+        }
+    }
+    // the group's first slot is the slot of its first member (offset gs < 32)
+    uint32_t P[2];
+    for (int e = 0; e < 2; ++e) P[e] = __shfl_sync(GSAIS_FULL_MASK, p0, (gs[e] < 0 ? 0 : gs[e]) & 31);
+
+    bool surv[2], hsub[2];
+    for (int e = 0; e < 2; ++e) {
+        surv[e] = false;
+        hsub[e] = false;
+        if (!own[e]) continue;
+        const uint32_t idx = e ? i1 : i0;
+        const uint32_t sub = P[e] + lt[e];
+        rank[idx] = 1 + sub;
+        if (eq[e] == 1) {
+            sa[sub] = idx;
+        } else {
+            surv[e] = true;
+            hsub[e] = before[e] == lt[e];
+        }
+    }
+    const uint64_t S = (uint64_t)__ballot_sync(GSAIS_FULL_MASK, surv[0]) |
+                       ((uint64_t)__ballot_sync(GSAIS_FULL_MASK, surv[1]) << 32);
+    const uint64_t HS = (uint64_t)__ballot_sync(GSAIS_FULL_MASK, hsub[0]) |
+                        ((uint64_t)__ballot_sync(GSAIS_FULL_MASK, hsub[1]) << 32);
+
+    // survivors / subgroup heads of my group ordered before me
+    uint32_t sb[2] = {0, 0}, hb[2] = {0, 0};
+    const uint32_t bf0 = before[0], bf1 = before[1];
+    for (int t = 0; t < maxsz; ++t) {
+        for (int e = 0; e < 2; ++e) {
+            const int src = (gs[e] < 0 ? 0 : gs[e]) + t;
+            const uint32_t ra = __shfl_sync(GSAIS_FULL_MASK, rr0, src & 31);
+            const uint32_t rb = __shfl_sync(GSAIS_FULL_MASK, rr1, src & 31);
+            const uint32_t ba = __shfl_sync(GSAIS_FULL_MASK, bf0, src & 31);
+            const uint32_t bb = __shfl_sync(GSAIS_FULL_MASK, bf1, src & 31);
+            const uint32_t rt = src >= 32 ? rb : ra;
+            const uint32_t bt = src >= 32 ? bb : ba;
+            if (surv[e] && src < gend[e]) {
+                const bool st = (S >> src) & 1ull, ht = (HS >> src) & 1ull;
+                sb[e] += st && bt < before[e];
+                hb[e] += ht && rt < myr[e];
+            }
+        }
+    }
+    // per-warp totals -> one reservation per CTA
+    if (lane == 0) {
+        s_we[warp] = (uint32_t)__popcll((long long)S);
+        s_wg[warp] = (uint32_t)__popcll((long long)HS);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t te = 0, tg = 0;
+        for (int w = 0; w < WARPS; ++w) {
+            const uint32_t a = s_we[w], b = s_wg[w];
+            s_we[w] = te;
+            s_wg[w] = tg;
+            te += a;
+            tg += b;
+        }
+        s_base = (te | tg) ? atomicAdd(counter, ((unsigned long long)tg << 32) | te) : 0ull;
+    }
+    __syncthreads();
+    const uint32_t base_e = (uint32_t)s_base + s_we[warp];
+    const uint32_t base_g = (uint32_t)(s_base >> 32) + s_wg[warp];
+    for (int e = 0; e < 2; ++e) {
+        if (!surv[e]) continue;
+        const uint64_t below = (1ull << gs[e]) - 1;   // offsets of earlier groups in the window
+        const uint32_t c = base_e + (uint32_t)__popcll((long long)(S & below)) + sb[e];
+        const uint32_t g = base_g + (uint32_t)__popcll((long long)(HS & below)) + hb[e];
+        out_i[c] = e ? i1 : i0;
+        out_pos[c] = P[e] + before[e];
+        out_gid[c] = g;
+        if (hsub[e]) gstart_out[g] = c;
     }
 }
 
@@ -382,10 +683,14 @@ size_t sort_workspace_bytes(uint64_t n, int symbytes)
     s += 2 * align_up(n * 4, A);                   // vals
     s += 2 * align_up(n * 4, A);                   // pos
     s += 2 * align_up(n * 4, A);                   // gid
+    s += 4 * align_up((n / 2 + 2) * 4, A);         // gstart x2, lid, loff (at most n/2 groups are active)
+    s += 3 * align_up(n * 4, A);                   // large list: values x2, slots
+    s += align_up(4 * 8, A);                       // round counters
     s += 2 * align_up(tiles * 12, A);              // tile info + carry
     s += align_up(16 * 4, A);                      // totals
     s += align_up(65536 * 4, A);                   // hist
     s += align_up(65536 * 2, A);                   // codes
+    s += align_up((n + kSeedTile - 1) / kSeedTile * (kSeedTile / 2) + 16, A);   // packed codes (<= 4 bits each)
     s += 2 * align_up(8 * 256 * 4, A);             // radix hist + bases
     s += align_up(8 * 4, A);                       // radix counters
     s += align_up(radix_status_words(n) * 8, A);   // look-back words
@@ -406,11 +711,19 @@ void sort_workspace_carve(SortWorkspace &ws, void *base, uint64_t n, int symbyte
     for (int i = 0; i < 2; ++i) ws.vals[i] = reinterpret_cast<uint32_t *>(take(n * 4));
     for (int i = 0; i < 2; ++i) ws.pos[i] = reinterpret_cast<uint32_t *>(take(n * 4));
     for (int i = 0; i < 2; ++i) ws.gid[i] = reinterpret_cast<uint32_t *>(take(n * 4));
+    for (int i = 0; i < 2; ++i) ws.gstart[i] = reinterpret_cast<uint32_t *>(take((n / 2 + 2) * 4));
+    ws.lid = reinterpret_cast<uint32_t *>(take((n / 2 + 2) * 4));
+    ws.loff = reinterpret_cast<uint32_t *>(take((n / 2 + 2) * 4));
+    for (int i = 0; i < 2; ++i) ws.lvals[i] = reinterpret_cast<uint32_t *>(take(n * 4));
+    ws.lpos = reinterpret_cast<uint32_t *>(take(n * 4));
+    ws.counters = reinterpret_cast<unsigned long long *>(take(4 * 8));
     ws.tile_info = reinterpret_cast<uint32_t *>(take(tiles * 12));
     ws.tile_carry = reinterpret_cast<uint32_t *>(take(tiles * 12));
     ws.totals = reinterpret_cast<uint32_t *>(take(16 * 4));
     ws.hist = reinterpret_cast<uint32_t *>(take(65536 * 4));
     ws.codes = reinterpret_cast<uint16_t *>(take(65536 * 2));
+    ws.packed = reinterpret_cast<uint8_t *>(take((n + kSeedTile - 1) / kSeedTile * (kSeedTile / 2) + 16));
+    ws.pack_bits = 0;
     ws.radix.hist = reinterpret_cast<uint32_t *>(take(8 * 256 * 4));
     ws.radix.bases = reinterpret_cast<uint32_t *>(take(8 * 256 * 4));
     ws.radix.counters = reinterpret_cast<uint32_t *>(take(8 * 4));
@@ -438,17 +751,18 @@ static int stream_grid(uint64_t items, int threads)
 
 template <int MODE>
 static cudaError_t run_assign(const TileArgs &a, SortWorkspace &ws, uint32_t *out_i, uint32_t *out_pos,
-                              uint32_t *out_gid, cudaStream_t st, uint32_t *kept, uint32_t *groups)
+                              uint32_t *out_gid, uint32_t *gstart_out, const unsigned long long *base,
+                              cudaStream_t st, uint32_t *kept, uint32_t *groups)
 {
     const uint64_t tiles = (a.N + kAssignTile - 1) / kAssignTile;
     KernelProfiler *prof = ws.radix.prof;
     cudaEvent_t ev = prof ? prof->begin(st) : nullptr;
     GSAIS_COUNTED((k_tile_summary<MODE><<<(unsigned)tiles, kAssignThreads, 0, st>>>(a, ws.tile_info)));
     if (ev) prof->end(KK_SUMMARY, ev, st, a.N * (MODE == MODE_ROUND ? 12 : 16));
-    GSAIS_COUNTED((k_tile_scan<<<1, 1024, 0, st>>>(ws.tile_info, ws.tile_carry, tiles, ws.totals)));
+    GSAIS_COUNTED((k_tile_scan<<<1, 1024, 0, st>>>(ws.tile_info, ws.tile_carry, tiles, ws.totals, base)));
     ev = prof ? prof->begin(st) : nullptr;
     GSAIS_COUNTED((k_assign<MODE><<<(unsigned)tiles, kAssignThreads, 0, st>>>(a, ws.tile_carry, ws.rank, ws.sa, out_i,
-                                                                                out_pos, out_gid)));
+                                                                                out_pos, out_gid, gstart_out)));
     // algorithmic bytes: key 8 + value 4 + slot 4 read, rank 4 scattered, and
     // 4 (SA) or 12 (survivor lists) written -- counted as 28 per entry
     if (ev) prof->end(KK_ASSIGN, ev, st, a.N * 28);
@@ -480,7 +794,7 @@ cudaError_t suffix_sort(const void *d_T, int symbytes, uint64_t n, bool gsa, Sor
         if (h_hist[c]) ++sigma;
     }
     int bits = gsais_bits_for(sigma > 1 ? sigma - 1 : 1);
-    int K = opt.seed_key_bits / bits;
+    int K = (opt.seed_key_bits <= 32 ? 32 : 64) / bits;
     if (K < 1) K = 1;
     if (K > 64) K = 64;
     S.seed_symbols = K;
@@ -489,26 +803,56 @@ cudaError_t suffix_sort(const void *d_T, int symbytes, uint64_t n, bool gsa, Sor
         return e;
     if ((e = cudaMemsetAsync(ws.rank + n, 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
 
-    // ---- seed keys and the K-prefix sort
-    const unsigned seed_grid = (unsigned)grid_for(n, kSeedTile);
+    // ---- seed keys (+ digit histograms, + packed codes) and the K-prefix sort
+    const int seed_end = K * bits;
+    const int seed_passes = (seed_end + 7) / 8;
+    const bool narrow = seed_end <= 32;   // 32-bit seed keys: less sort traffic
+    ws.pack_bits = gsa ? 0 : (bits <= 2 ? 2 : (bits <= 4 ? 4 : 0));
+    for (int c = 0, code = 0; c < nsym && code < 16; ++c)
+        if (h_hist[c]) ws.decode[code++] = (uint16_t)c;
+    const unsigned seed_grid = (unsigned)stream_grid((n + kSeedTile - 1) / kSeedTile * 256, 256);
+    uint32_t *k32[2] = {reinterpret_cast<uint32_t *>(ws.keys[0]), reinterpret_cast<uint32_t *>(ws.keys[1])};
+    if ((e = cudaMemsetAsync(ws.radix.hist, 0, (size_t)seed_passes * 256 * 4, st)) != cudaSuccess) return e;
     cudaEvent_t ev_seed = ws.radix.prof ? ws.radix.prof->begin(st) : nullptr;
-    if (symbytes == 1)
-        GSAIS_COUNTED((k_seed<uint8_t><<<seed_grid, 256, 0, st>>>(static_cast<const uint8_t *>(d_T), n, ws.codes, bits, K, gsa ? 1 : 0,
-                                                   ws.keys[0], ws.vals[0])));
-    else
-        GSAIS_COUNTED((k_seed<uint16_t><<<seed_grid, 256, 0, st>>>(static_cast<const uint16_t *>(d_T), n, ws.codes, bits, K,
-                                                    gsa ? 1 : 0, ws.keys[0], ws.vals[0])));
-    if (ev_seed) ws.radix.prof->end(KK_SEED, ev_seed, st, n * (symbytes + 12));
+    if (symbytes == 1) {
+        const uint8_t *T8 = static_cast<const uint8_t *>(d_T);
+        if (narrow)
+            GSAIS_COUNTED((k_seed<uint8_t, uint32_t><<<seed_grid, 256, 0, st>>>(
+                T8, n, ws.codes, bits, K, gsa ? 1 : 0, k32[0], ws.vals[0], seed_passes, seed_end, ws.radix.hist,
+                ws.pack_bits, ws.packed)));
+        else
+            GSAIS_COUNTED((k_seed<uint8_t, uint64_t><<<seed_grid, 256, 0, st>>>(
+                T8, n, ws.codes, bits, K, gsa ? 1 : 0, ws.keys[0], ws.vals[0], seed_passes, seed_end, ws.radix.hist,
+                ws.pack_bits, ws.packed)));
+    } else {
+        const uint16_t *T16 = static_cast<const uint16_t *>(d_T);
+        if (narrow)
+            GSAIS_COUNTED((k_seed<uint16_t, uint32_t><<<seed_grid, 256, 0, st>>>(
+                T16, n, ws.codes, bits, K, gsa ? 1 : 0, k32[0], ws.vals[0], seed_passes, seed_end, ws.radix.hist,
+                ws.pack_bits, ws.packed)));
+        else
+            GSAIS_COUNTED((k_seed<uint16_t, uint64_t><<<seed_grid, 256, 0, st>>>(
+                T16, n, ws.codes, bits, K, gsa ? 1 : 0, ws.keys[0], ws.vals[0], seed_passes, seed_end, ws.radix.hist,
+                ws.pack_bits, ws.packed)));
+    }
+    if (ev_seed) ws.radix.prof->end(KK_SEED, ev_seed, st, n * (symbytes + (narrow ? 8 : 12)));
     int w = 0, ran = 0;
     {
-        uint64_t *kk[2] = {ws.keys[0], ws.keys[1]};
         uint32_t *vv[2] = {ws.vals[0], ws.vals[1]};
-        if ((e = radix_sort_pairs(kk, vv, n, K * bits, ws.radix, d_err, st, &w, &ran)) != cudaSuccess) return e;
+        if (narrow) {
+            if ((e = radix_sort_pairs32(k32, vv, n, seed_end, ws.radix, d_err, st, &w, &ran, true)) != cudaSuccess)
+                return e;
+        } else {
+            uint64_t *kk[2] = {ws.keys[0], ws.keys[1]};
+            if ((e = radix_sort_pairs(kk, vv, n, seed_end, ws.radix, d_err, st, &w, &ran, true)) != cudaSuccess)
+                return e;
+        }
         S.radix_passes += ran;
     }
 
     TileArgs a;
     a.keys = ws.keys[w];
+    a.keys32 = narrow ? k32[w] : nullptr;
     a.vals = ws.vals[w];
     a.pos = nullptr;
     a.N = n;
@@ -520,9 +864,11 @@ cudaError_t suffix_sort(const void *d_T, int symbytes, uint64_t n, bool gsa, Sor
     uint32_t kept = 0, groups = 0;
     int av = w ^ 1, pg = 0;
     if (gsa)
-        e = run_assign<MODE_INIT_GSA>(a, ws, ws.vals[av], ws.pos[pg], ws.gid[pg], st, &kept, &groups);
+        e = run_assign<MODE_INIT_GSA>(a, ws, ws.vals[av], ws.pos[pg], ws.gid[pg], ws.gstart[pg], nullptr, st, &kept,
+                                      &groups);
     else
-        e = run_assign<MODE_INIT_PLAIN>(a, ws, ws.vals[av], ws.pos[pg], ws.gid[pg], st, &kept, &groups);
+        e = run_assign<MODE_INIT_PLAIN>(a, ws, ws.vals[av], ws.pos[pg], ws.gid[pg], ws.gstart[pg], nullptr, st,
+                                        &kept, &groups);
     if (e != cudaSuccess) return e;
 
     // ---- doubling rounds over the active suffixes
@@ -536,29 +882,59 @@ cudaError_t suffix_sort(const void *d_T, int symbytes, uint64_t n, bool gsa, Sor
             return cudaErrorUnknown;
         }
         S.active_total += kept;
-        const uint64_t N = kept;
-        const int gb = gsais_bits_for(groups > 1 ? groups - 1 : 0);
+        const uint64_t N = kept, G = groups;
+        const int gb = gsais_bits_for(G > 1 ? G - 1 : 0);
+        const int end_bit = b2 + gb;   // large ids < G: unused top digits are skipped by the sort
+        const int passes = (end_bit + 7) / 8;
+        uint32_t *act_i = ws.vals[av], *act_pos = ws.pos[pg], *act_gid = ws.gid[pg];
+        uint32_t *out_i = ws.vals[av ^ 1], *out_pos = ws.pos[pg ^ 1], *out_gid = ws.gid[pg ^ 1];
+        uint32_t *r2 = reinterpret_cast<uint32_t *>(ws.keys[1]);   // consumed before the large sort reuses keys[1]
+        if ((e = cudaMemsetAsync(ws.counters, 0, 2 * sizeof(unsigned long long), st)) != cudaSuccess) return e;
+        if ((e = cudaMemsetAsync(ws.radix.hist, 0, (size_t)passes * 256 * 4, st)) != cudaSuccess) return e;
+        GSAIS_COUNTED((k_classify<<<stream_grid(G, 256), 256, 0, st>>>(ws.gstart[pg], G, N, ws.lid, ws.loff,
+                                                                      ws.counters + 1)));
         cudaEvent_t ev_rk = ws.radix.prof ? ws.radix.prof->begin(st) : nullptr;
-        GSAIS_COUNTED((k_round_keys<<<grid_for(N, 256), 256, 0, st>>>(ws.vals[av], ws.gid[pg], ws.rank, h, N, n, b2, ws.keys[0],
-                                                        d_err)));
-        if (ev_rk) ws.radix.prof->end(KK_ROUND_KEYS, ev_rk, st, N * 24);
-        uint64_t *kk[2] = {ws.keys[0], ws.keys[1]};
-        uint32_t *vv[2] = {ws.vals[av], ws.vals[av ^ 1]};
-        int which = 0;
-        if ((e = radix_sort_pairs(kk, vv, N, b2 + gb, ws.radix, d_err, st, &which, &ran)) != cudaSuccess) return e;
-        S.radix_passes += ran;
-        const int sv = which == 0 ? av : (av ^ 1);   // vals buffer holding the sorted values
-        TileArgs r;
-        r.keys = kk[which];
-        r.vals = ws.vals[sv];
-        r.pos = ws.pos[pg];
-        r.N = N;
-        r.n = n;
-        r.K = (uint32_t)K;
-        r.zlo = r.zhi = 0;
-        if ((e = run_assign<MODE_ROUND>(r, ws, ws.vals[sv ^ 1], ws.pos[pg ^ 1], ws.gid[pg ^ 1], st, &kept, &groups)) !=
-            cudaSuccess)
+        GSAIS_COUNTED((k_round_r2<<<stream_grid(N, 256), 256, 0, st>>>(
+            act_i, act_pos, act_gid, ws.gstart[pg], ws.lid, ws.loff, ws.rank, h, N, n, b2, r2, ws.keys[0],
+            ws.lvals[0], ws.lpos, d_err, passes, end_bit, ws.radix.hist)));
+        if (ev_rk) ws.radix.prof->end(KK_ROUND_KEYS, ev_rk, st, N * 28);
+        cudaEvent_t ev_sm = ws.radix.prof ? ws.radix.prof->begin(st) : nullptr;
+        GSAIS_COUNTED((k_small_groups<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(
+            act_i, act_pos, act_gid, r2, N, ws.rank, ws.sa, out_i, out_pos, out_gid, ws.gstart[pg ^ 1],
+            ws.counters)));
+        if (ev_sm) ws.radix.prof->end(KK_SMALL, ev_sm, st, N * 32);
+        if ((e = cudaMemcpyAsync(ws.h_small, ws.counters, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                 st)) != cudaSuccess)
             return e;
+        if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+        const unsigned long long small_tot = reinterpret_cast<unsigned long long *>(ws.h_small)[0];
+        const unsigned long long large_tot = reinterpret_cast<unsigned long long *>(ws.h_small)[1];
+        const uint64_t NL = (uint32_t)large_tot;
+        if (NL == 0) {
+            kept = (uint32_t)small_tot;
+            groups = (uint32_t)(small_tot >> 32);
+        } else {
+            uint64_t *kk[2] = {ws.keys[0], ws.keys[1]};
+            uint32_t *vv[2] = {ws.lvals[0], ws.lvals[1]};
+            int which = 0;
+            if ((e = radix_sort_pairs(kk, vv, NL, end_bit, ws.radix, d_err, st, &which, &ran, true)) != cudaSuccess)
+                return e;
+            S.radix_passes += ran;
+            S.large_total += NL;
+            TileArgs r;
+            r.keys = kk[which];
+            r.keys32 = nullptr;
+            r.vals = vv[which];
+            r.pos = ws.lpos;
+            r.N = NL;
+            r.n = n;
+            r.K = (uint32_t)K;
+            r.zlo = r.zhi = 0;
+            if ((e = run_assign<MODE_ROUND>(r, ws, out_i, out_pos, out_gid, ws.gstart[pg ^ 1], ws.counters, st, &kept,
+                                            &groups)) != cudaSuccess)
+                return e;
+        }
+        int sv = av;
         av = sv ^ 1;
         pg ^= 1;
         h *= 2;

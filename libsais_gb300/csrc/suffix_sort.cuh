@@ -15,11 +15,20 @@ struct SortWorkspace {
     uint32_t *vals[2] = {nullptr, nullptr};
     uint32_t *pos[2] = {nullptr, nullptr};   // SA slot of each active entry
     uint32_t *gid[2] = {nullptr, nullptr};   // dense id of each active entry's group
+    uint32_t *gstart[2] = {nullptr, nullptr};  // list index of each group's first entry
+    uint32_t *lid = nullptr;                 // per group: id among the large groups, or none
+    uint32_t *loff = nullptr;                // per group: first slot in the large list
+    uint32_t *lvals[2] = {nullptr, nullptr};   // large list: suffix indexes (sort ping-pong)
+    uint32_t *lpos = nullptr;                // large list: SA slot of each entry
+    unsigned long long *counters = nullptr;  // [0] small-path (groups<<32 | entries), [1] large groups (count<<32 | size)
     uint32_t *tile_info = nullptr;           // 3 words per assign tile
     uint32_t *tile_carry = nullptr;          // 3 words per assign tile
     uint32_t *totals = nullptr;              // [4] kept entries, kept groups, ...
     uint32_t *hist = nullptr;                // symbol histogram (256 or 65536)
     uint16_t *codes = nullptr;               // dense symbol codes (256 or 65536)
+    uint8_t *packed = nullptr;               // text as packed codes when they fit 2 or 4 bits
+    int pack_bits = 0;                       // 0 (not packed), 2 or 4
+    uint16_t decode[16] = {0};               // symbol of each code when packed
     RadixScratch radix;
     uint32_t *h_small = nullptr;             // pinned host scratch (>= 65536 + 16 words)
 };
@@ -33,7 +42,7 @@ void sort_workspace_carve(SortWorkspace &ws, void *base, uint64_t n, int symbyte
                           uint32_t *h_hist);
 
 struct SortOptions {
-    int seed_key_bits = 64;   // width of the packed seed prefix (32 or 64)
+    int seed_key_bits = 32;   // width of the packed seed prefix (32 or 64)
 };
 
 // Suffix array of the device text d_T (n symbols of `symbytes` bytes).  gsa

@@ -99,6 +99,28 @@ def test_random_small_u16(oracle):
         check_all(oracle, T, plcp=True, r=4)
 
 
+def test_runs_and_tandem_repeats(oracle):
+    """Runs of the smallest symbol at the end and inside the text, and tandem
+    repeats: groups of every size around the 32-suffix small/large cut-over,
+    including the last group of the active list ending mid-window."""
+    rng = np.random.default_rng(5)
+    for trial in range(200):
+        m = int(rng.integers(50, 5000))
+        s = (rng.integers(0, 4, m) + 65).astype(np.uint8)
+        s[-int(rng.integers(1, 30)):] = 65
+        s[int(rng.integers(0, m // 2)):][:40] = 65
+        rc, SA, _ = G.libsais(s)
+        assert rc == 0 and np.array_equal(SA.astype(np.int64), oracle.sa(s)[1]), trial
+    for trial in range(60):
+        n = int(rng.integers(2000, 20000))
+        t = (rng.integers(0, 4, n) + 65).astype(np.uint8)
+        a = int(rng.integers(0, n // 2))
+        L = int(rng.integers(50, n // 4))
+        p = int(rng.integers(2, 40))
+        t[a:a + L] = np.tile(t[a:a + p], L // p + 1)[:L]
+        check_all(oracle, t, plcp=trial % 4 == 0, r=0)
+
+
 def random_gsa(rng, count, maxlen, k):
     parts = []
     for _ in range(count):

@@ -2,7 +2,7 @@
 
 It serves callers that cannot call cudaMalloc (CUDA graph capture, a
 framework allocator that owns all device memory, latency-critical paths):
-the suffix sort takes all of its scratch from a fixed 4 MiB __device__
+the suffix sort takes all of its scratch from a fixed 6 MiB __device__
 array, for texts of at most 65,536 symbols.  This test calls it through the
 C-ABI twice in a row on each input and compares its output with the existing
 allocating entry point gsais_sa_device; suffix arrays are integers, so the
