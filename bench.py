@@ -208,6 +208,64 @@ def run_reference(args, rank, dist):
     print(json.dumps(line), flush=True)
 
 
+def run_batched(G, torch, count: int = 4096, steps: int = 3, warmup: int = 1, cpu_strings: int = 32):
+    """The batched workload: `count` uint8 strings, lengths log-uniform over
+    256 B - 4 MiB, i.i.d. ACGT with 1% 'N' (seeded).  Times the batched sort
+    (all strings in the same launches) against one GPU call per string on the
+    same device buffers, and checks that both give identical SA/BWT/primary."""
+    from libsais_gb300 import textgen
+    T, offs = textgen.batch_strings(count, seed=3)
+    n = int(offs[-1])
+    dT = torch.from_numpy(T).cuda()
+    dO = torch.from_numpy(offs).cuda()
+    dSA = torch.empty(n, dtype=torch.int32, device="cuda")
+    dU = torch.empty(n, dtype=torch.uint8, device="cuda")
+    dP = torch.empty(count, dtype=torch.int32, device="cuda")
+    stream = torch.cuda.current_stream()
+    for _ in range(warmup):
+        if G.batch_sa_bwt_device(dT, dO, dSA, dU, dP, stream=stream) != 0:
+            raise SystemExit("batched sort failed")
+    launches0 = G.launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        G.batch_sa_bwt_device(dT, dO, dSA, dU, dP, stream=stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    batched_ms = e0.elapsed_time(e1) / steps
+    batched_launches = (G.launch_count() - launches0) / steps
+    # one call per string, same buffers
+    pSA = torch.empty_like(dSA)
+    pU = torch.empty_like(dU)
+    prim = np.zeros(count, dtype=np.int32)
+    torch.cuda.synchronize()
+    launches0 = G.launch_count()
+    t0 = time.perf_counter()
+    for s in range(count):
+        a, b = int(offs[s]), int(offs[s + 1])
+        if b > a:
+            prim[s] = G.sa_bwt_device(dT[a:b], pSA[a:b], pU[a:b], stream=stream)
+    torch.cuda.synchronize()
+    per_string_s = time.perf_counter() - t0
+    per_string_launches = G.launch_count() - launches0
+    identical = bool(torch.equal(pSA, dSA) and torch.equal(pU, dU) and np.array_equal(prim, dP.cpu().numpy()))
+    from oracle.oracle import Oracle
+    O = Oracle()
+    cpu_n = int(offs[cpu_strings])
+    t0 = time.perf_counter()
+    for s in range(cpu_strings):
+        t = T[int(offs[s]):int(offs[s + 1])]
+        _, sa = O.sa(t)
+        O.bwt_from_sa(t, sa)
+    cpu_s = time.perf_counter() - t0
+    return {"strings": count, "total_symbols": n, "batched_mb_s": round(n / 1e6 / (batched_ms / 1e3), 1),
+            "batched_ms": round(batched_ms, 2), "batched_launches": batched_launches,
+            "per_string_mb_s": round(n / 1e6 / per_string_s, 1), "per_string_ms": round(per_string_s * 1e3, 1),
+            "per_string_launches": per_string_launches,
+            "speedup_vs_per_string": round(per_string_s * 1e3 / batched_ms, 2), "identical": identical,
+            "cpu_port_mb_s": round(cpu_n / 1e6 / cpu_s, 2), "cpu_sample": f"first {cpu_strings} strings, 1 thread"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -220,6 +278,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--seed-key-bits", type=int, default=0)
+    ap.add_argument("--no-extras", action="store_true", help="skip the batched and serving measurements")
+    ap.add_argument("--batch-strings", type=int, default=4096)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -326,6 +386,11 @@ def main():
         cpu = {"value": round(sample / 1e6 / dt, 3), "unit": UNIT, "cores": cores, "kind": kind,
                "sample": f"first {sample} symbols of the {WORKLOADS[name][2]}, SA-IS + BWT"}
 
+    extras = {}
+    if rank == 0 and world == 1 and not args.no_extras:
+        G.release_workspace()
+        extras["batched"] = run_batched(G, torch, count=args.batch_strings)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -339,6 +404,7 @@ def main():
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
             "kernels": kernels, "clocks": clocks,
         }
+        line.update(extras)
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()

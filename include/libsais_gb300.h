@@ -64,6 +64,21 @@ extern "C" {
     */
     int64_t gsais_sa_bwt(void * ctx, const void * T, int32_t symbytes, int64_t n, void * SA, int32_t sa_bytes, void * U, void * freq, int32_t freq_bytes);
 
+    /**
+    * Suffix arrays and BWTs of many independent uint8 strings in one batched sort
+    * (every doubling round is one set of launches for all strings; the string id
+    * is packed into the high bits of the seed keys).  String s is
+    * T[offsets[s] .. offsets[s+1]-1]; offsets has count + 1 entries, offsets[0] = 0.
+    * Outputs use the same concatenated layout: SA[offsets[s] + k] is the k-th suffix
+    * of string s (relative to its start), U[offsets[s] ..] its BWT in libsais_bwt's
+    * layout, primary[s] its primary index (as libsais_bwt returns it; 0 for empty strings).
+    * Host buffers.  Returns 0, -1 or -2.
+    */
+    int64_t gsais_batch_sa_bwt(void * ctx, const void * T, const int64_t * offsets, int32_t count, int32_t * SA, uint8_t * U, int32_t * primary);
+
+    /** gsais_batch_sa_bwt on device buffers (n = offsets[count], given by the caller). */
+    int64_t gsais_batch_sa_bwt_device(void * ctx, const void * T, int64_t n, const int64_t * offsets, int32_t count, int32_t * SA, uint8_t * U, int32_t * primary, void * stream);
+
     /** Statistics of the last suffix sort run on a context. */
     typedef struct gsais_stats
     {

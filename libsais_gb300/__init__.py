@@ -102,6 +102,8 @@ _SIGS = {
     "gsais_profile_reset": (None, [_p]),
     "gsais_launch_count": (_i64, []),
     "gsais_sa_device_noalloc": (_i64, [_p, _i32, _i64, _i32, _p, _p]),
+    "gsais_batch_sa_bwt": (_i64, [_p, _p, _p, _i32, _p, _p, _p]),
+    "gsais_batch_sa_bwt_device": (_i64, [_p, _p, _i64, _p, _i32, _p, _p, _p, _p]),
 }
 
 EXPORTED_SYMBOLS = tuple(_SIGS)
@@ -395,3 +397,34 @@ def profile_read(ctx=None) -> dict:
 
 def launch_count() -> int:
     return int(load().gsais_launch_count())
+
+
+def batch_sa_bwt(T, offsets, ctx=None):
+    """Batched SA + BWT of the strings T[offsets[s]:offsets[s+1]] (host arrays).
+
+    Returns (rc, SA, U, primary) in the concatenated layout."""
+    lib = load()
+    T = np.ascontiguousarray(T, dtype=np.uint8)
+    offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+    count = offsets.size - 1
+    n = int(offsets[-1])
+    SA = np.zeros(max(n, 1), dtype=np.int32)
+    U = np.zeros(max(n, 1), dtype=np.uint8)
+    P = np.zeros(max(count, 1), dtype=np.int32)
+    rc = lib.gsais_batch_sa_bwt(ctx.handle if ctx else None, _ptr(T), _ptr(offsets), count, _ptr(SA), _ptr(U),
+                                _ptr(P))
+    return int(rc), SA[:n], U[:n], P[:count]
+
+
+def batch_sa_bwt_device(T, offsets, SA, U, primary, ctx=None, stream=None):
+    """Device variant: torch tensors T (uint8), offsets (int64, count + 1), SA (int32), U (uint8), primary (int32)."""
+    lib = load()
+    count = offsets.numel() - 1
+    return int(lib.gsais_batch_sa_bwt_device(ctx.handle if ctx else None, T.data_ptr(), T.numel(),
+                                             offsets.data_ptr(), count, SA.data_ptr(), U.data_ptr(),
+                                             primary.data_ptr(), _stream_handle(stream)))
+
+
+def release_workspace(ctx=None) -> None:
+    """Free the device workspace cached by a context (the process-wide one by default)."""
+    load().gsais_release_workspace(ctx.handle if ctx else None)

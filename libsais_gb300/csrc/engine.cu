@@ -508,6 +508,71 @@ int64_t gsais_sa_bwt(void *ctx, const void *T, int32_t symbytes, int64_t n, void
     return gsais_run_bwt(c, T, symbytes, n, U, freq, freq_bytes, 0, nullptr, 4, SA, sa_bytes);
 }
 
+static int64_t batch_run(gsais_ctx *c, const uint8_t *d_T, int64_t n_, const uint64_t *d_offs, int32_t count,
+                         int32_t *d_SA, uint8_t *d_U, int32_t *d_primary, cudaStream_t st, size_t extra_front)
+{
+    const uint64_t n = (uint64_t)n_;
+    SortWorkspace ws;
+    Carver cv(static_cast<char *>(c->arena) + extra_front);
+    sort_workspace_carve(ws, cv.p, n + (uint64_t)count, 1, c->h_small, c->h_hist);
+    ws.radix.prof = &c->prof;
+    if (!clear_err(c, st)) return fail(cudaErrorUnknown);
+    GS_TRY(batch_suffix_sort(d_T, n, d_offs, (uint32_t)count, ws, c->d_misc, st, &c->stats));
+    GS_TRY(batch_outputs(ws, d_T, n, d_offs, (uint32_t)count, d_SA, d_U, d_primary, c->d_misc, st));
+    GS_TRY(sync_checked(c, st));
+    return 0;
+}
+
+int64_t gsais_batch_sa_bwt_device(void *ctx, const void *T, int64_t n, const int64_t *offsets, int32_t count,
+                                  int32_t *SA, uint8_t *U, int32_t *primary, void *stream)
+{
+    gsais_ctx *c = resolve(ctx);
+    if (!c || !T || !offsets || !SA || !U || !primary || n < 0 || count <= 0) return -1;
+    std::lock_guard<std::mutex> lock(c->mu);
+    if ((uint64_t)n + (uint64_t)count > kMaxN) return -2;
+    if (!ctx_init(c)) return fail(cudaErrorUnknown);
+    DeviceGuard g(c->device);
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : c->stream;
+    if (!ensure_arena(c, batch_workspace_bytes((uint64_t)n, (uint32_t)count))) return -2;
+    return batch_run(c, static_cast<const uint8_t *>(T), n, reinterpret_cast<const uint64_t *>(offsets), count, SA,
+                     U, primary, st, 0);
+}
+
+int64_t gsais_batch_sa_bwt(void *ctx, const void *T, const int64_t *offsets, int32_t count, int32_t *SA, uint8_t *U,
+                           int32_t *primary)
+{
+    gsais_ctx *c = resolve(ctx);
+    if (!c || !T || !offsets || !SA || !U || !primary || count <= 0) return -1;
+    const int64_t n_ = offsets[count];
+    if (n_ < 0 || offsets[0] != 0) return -1;
+    for (int32_t s = 0; s < count; ++s)
+        if (offsets[s + 1] < offsets[s]) return -1;
+    std::lock_guard<std::mutex> lock(c->mu);
+    const uint64_t n = (uint64_t)n_;
+    if (n + (uint64_t)count > kMaxN) return -2;
+    if (!ctx_init(c)) return fail(cudaErrorUnknown);
+    DeviceGuard g(c->device);
+    cudaStream_t st = c->stream;
+    const size_t front = align_up(n) + align_up((count + 1) * 8) + align_up(n * 4) + align_up(n) +
+                         align_up((size_t)count * 4);
+    if (!ensure_arena(c, front + batch_workspace_bytes(n, (uint32_t)count))) return -2;
+    Carver cv(c->arena);
+    uint8_t *d_T = cv.take<uint8_t>(n);
+    uint64_t *d_offs = cv.take<uint64_t>(count + 1);
+    int32_t *d_SA = cv.take<int32_t>(n);
+    uint8_t *d_U = cv.take<uint8_t>(n);
+    int32_t *d_P = cv.take<int32_t>(count);
+    GS_TRY(cudaMemcpyAsync(d_T, T, n, cudaMemcpyHostToDevice, st));
+    GS_TRY(cudaMemcpyAsync(d_offs, offsets, (size_t)(count + 1) * 8, cudaMemcpyHostToDevice, st));
+    const int64_t rc = batch_run(c, d_T, n_, d_offs, count, d_SA, d_U, d_P, st, front);
+    if (rc != 0) return rc;
+    GS_TRY(cudaMemcpyAsync(SA, d_SA, n * 4, cudaMemcpyDeviceToHost, st));
+    GS_TRY(cudaMemcpyAsync(U, d_U, n, cudaMemcpyDeviceToHost, st));
+    GS_TRY(cudaMemcpyAsync(primary, d_P, (size_t)count * 4, cudaMemcpyDeviceToHost, st));
+    GS_TRY(cudaStreamSynchronize(st));
+    return 0;
+}
+
 int32_t gsais_last_stats(void *ctx, gsais_stats *out)
 {
     gsais_ctx *c = resolve(ctx);

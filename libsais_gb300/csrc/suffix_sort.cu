@@ -657,6 +657,97 @@ __global__ void __launch_bounds__(256) k_small_groups(const uint32_t *__restrict
     }
 }
 
+// ------------------------------------------------------ batched strings
+// Many independent strings are sorted together: string s of the
+// concatenation occupies [offs[s], offs[s+1]) and, in rank coordinates, the
+// slots [offs[s] + s, offs[s+1] + s) followed by one gap slot whose rank is
+// 0 (its end-of-string sentinel).  Symbol codes are shifted by one so the
+// gap's code 0 ends a seed window: a suffix shorter than K packs zeros after
+// its last symbol and therefore sorts before every longer suffix with the
+// same symbols (libsais's implicit sentinel).  The string id sits in the
+// high bits of the seed key, so groups never span two strings and the
+// sorted rows come out grouped by string.
+
+// Largest s with offs[s] <= p (offs has count + 1 entries, offs[count] = n).
+__device__ __forceinline__ uint32_t string_of(const uint64_t *__restrict__ offs, uint32_t count, uint64_t p)
+{
+    uint32_t lo = 0, hi = count;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (offs[mid] <= p) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Bytes per suffix: T 1 read (windows overlap in L1), key 8 + value 4 written.
+__global__ void __launch_bounds__(256) k_seed_batch(const uint8_t *__restrict__ T, uint64_t n,
+                                                    const uint64_t *__restrict__ offs, uint32_t count,
+                                                    const uint16_t *__restrict__ codes, int bits, int K,
+                                                    uint64_t *__restrict__ keys, uint32_t *__restrict__ vals,
+                                                    int passes, int end_bit, uint32_t *__restrict__ hist)
+{
+    __shared__ uint32_t sh[kMaxRadixPasses][256];
+    radix_hist_zero(sh, passes);
+    __syncthreads();
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t n_round = (n + 31) & ~31ull;
+    for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n_round; p += stride) {
+        const bool ok = p < n;
+        uint64_t key = 0;
+        if (ok) {
+            const uint32_t s = string_of(offs, count, p);
+            const uint64_t e = offs[s + 1];
+            for (int q = 0; q < K; ++q) {
+                const uint64_t c = p + q < e ? (uint64_t)codes[T[p + q]] : 0ull;
+                key = (key << bits) | c;
+            }
+            key |= (uint64_t)s << (K * bits);
+            keys[p] = key;
+            vals[p] = (uint32_t)(p + s);
+        }
+        radix_hist_add(sh, key, ok, passes, end_bit);
+    }
+    __syncthreads();
+    radix_hist_flush(sh, passes, hist);
+}
+
+// Per-string outputs from the batched rows: SA relative to the string start,
+// BWT in libsais_bwt's layout and the primary index of every string.
+// Bytes per row: SA 4 read + 4 gathered, T 1 gathered; SA 4 + U 1 written.
+__global__ void __launch_bounds__(256) k_batch_outputs(const uint32_t *__restrict__ SA, const uint32_t *__restrict__ isa1,
+                                                       const uint8_t *__restrict__ T, uint64_t n,
+                                                       const uint64_t *__restrict__ offs, uint32_t count,
+                                                       int32_t *__restrict__ sa_out, uint8_t *__restrict__ U,
+                                                       int32_t *__restrict__ primary, uint32_t *__restrict__ err)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
+        const uint32_t s = string_of(offs, count, r);
+        const uint64_t base = offs[s], len = offs[s + 1] - base, gs = base + s;
+        const uint64_t k = r - base;
+        const uint64_t g = SA[r];
+        if (g < gs || g >= gs + len) {
+            atomicOr(err, GSAIS_ERR_BOUNDS);
+            continue;
+        }
+        sa_out[r] = (int32_t)(g - gs);
+        const uint64_t i0 = (uint64_t)isa1[gs] - 1 - base;   // row of the string's suffix 0
+        if (k == 0) {
+            U[r] = T[base + len - 1];
+            primary[s] = (int32_t)(i0 + 1);
+        } else {
+            const uint64_t row = k <= i0 ? k - 1 : k;
+            const uint64_t p = (uint64_t)SA[base + row] - gs;
+            if (p == 0 || p >= len) {
+                atomicOr(err, GSAIS_ERR_BOUNDS);
+                continue;
+            }
+            U[r] = T[base + p - 1];
+        }
+    }
+}
+
 // GSA validity: T[n-1] == 0, T[0] != 0, no two adjacent zeros.
 template <typename Sym>
 __global__ void k_gsa_check(const Sym *__restrict__ T, uint64_t n, uint32_t *__restrict__ flag)
@@ -774,6 +865,83 @@ static cudaError_t run_assign(const TileArgs &a, SortWorkspace &ws, uint32_t *ou
     return cudaGetLastError();
 }
 
+// Doubling rounds over the kept groups of the seed round until every suffix
+// is final.  nr = length of the rank domain (rank[nr] is the sentinel).
+static cudaError_t run_rounds(SortWorkspace &ws, uint64_t nr, int K, uint32_t kept, uint32_t groups, int av, int pg,
+                              uint32_t *d_err, cudaStream_t st, SortStats &S)
+{
+    cudaError_t e;
+    int ran = 0;
+    const int b2 = gsais_bits_for(nr);
+    uint64_t h = (uint64_t)K;
+    while (kept > 0) {
+        if (++S.rounds > 64) {
+            uint32_t flag = GSAIS_ERR_ROUNDS;
+            cudaMemcpyAsync(d_err, &flag, 4, cudaMemcpyHostToDevice, st);
+            cudaStreamSynchronize(st);
+            return cudaErrorUnknown;
+        }
+        S.active_total += kept;
+        const uint64_t N = kept, G = groups;
+        const int gb = gsais_bits_for(G > 1 ? G - 1 : 0);
+        const int end_bit = b2 + gb;   // large ids < G: unused top digits are skipped by the sort
+        const int passes = (end_bit + 7) / 8;
+        uint32_t *act_i = ws.vals[av], *act_pos = ws.pos[pg], *act_gid = ws.gid[pg];
+        uint32_t *out_i = ws.vals[av ^ 1], *out_pos = ws.pos[pg ^ 1], *out_gid = ws.gid[pg ^ 1];
+        uint32_t *r2 = reinterpret_cast<uint32_t *>(ws.keys[1]);   // consumed before the large sort reuses keys[1]
+        if ((e = cudaMemsetAsync(ws.counters, 0, 2 * sizeof(unsigned long long), st)) != cudaSuccess) return e;
+        if ((e = cudaMemsetAsync(ws.radix.hist, 0, (size_t)passes * 256 * 4, st)) != cudaSuccess) return e;
+        GSAIS_COUNTED((k_classify<<<stream_grid(G, 256), 256, 0, st>>>(ws.gstart[pg], G, N, ws.lid, ws.loff,
+                                                                      ws.counters + 1)));
+        cudaEvent_t ev_rk = ws.radix.prof ? ws.radix.prof->begin(st) : nullptr;
+        GSAIS_COUNTED((k_round_r2<<<stream_grid(N, 256), 256, 0, st>>>(
+            act_i, act_pos, act_gid, ws.gstart[pg], ws.lid, ws.loff, ws.rank, h, N, nr, b2, r2, ws.keys[0],
+            ws.lvals[0], ws.lpos, d_err, passes, end_bit, ws.radix.hist)));
+        if (ev_rk) ws.radix.prof->end(KK_ROUND_KEYS, ev_rk, st, N * 28);
+        cudaEvent_t ev_sm = ws.radix.prof ? ws.radix.prof->begin(st) : nullptr;
+        GSAIS_COUNTED((k_small_groups<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(
+            act_i, act_pos, act_gid, r2, N, ws.rank, ws.sa, out_i, out_pos, out_gid, ws.gstart[pg ^ 1],
+            ws.counters)));
+        if (ev_sm) ws.radix.prof->end(KK_SMALL, ev_sm, st, N * 32);
+        if ((e = cudaMemcpyAsync(ws.h_small, ws.counters, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                 st)) != cudaSuccess)
+            return e;
+        if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+        const unsigned long long small_tot = reinterpret_cast<unsigned long long *>(ws.h_small)[0];
+        const unsigned long long large_tot = reinterpret_cast<unsigned long long *>(ws.h_small)[1];
+        const uint64_t NL = (uint32_t)large_tot;
+        if (NL == 0) {
+            kept = (uint32_t)small_tot;
+            groups = (uint32_t)(small_tot >> 32);
+        } else {
+            uint64_t *kk[2] = {ws.keys[0], ws.keys[1]};
+            uint32_t *vv[2] = {ws.lvals[0], ws.lvals[1]};
+            int which = 0;
+            if ((e = radix_sort_pairs(kk, vv, NL, end_bit, ws.radix, d_err, st, &which, &ran, true)) != cudaSuccess)
+                return e;
+            S.radix_passes += ran;
+            S.large_total += NL;
+            TileArgs r;
+            r.keys = kk[which];
+            r.keys32 = nullptr;
+            r.vals = vv[which];
+            r.pos = ws.lpos;
+            r.N = NL;
+            r.n = nr;
+            r.K = (uint32_t)K;
+            r.zlo = r.zhi = 0;
+            if ((e = run_assign<MODE_ROUND>(r, ws, out_i, out_pos, out_gid, ws.gstart[pg ^ 1], ws.counters, st, &kept,
+                                            &groups)) != cudaSuccess)
+                return e;
+        }
+        int sv = av;
+        av = sv ^ 1;
+        pg ^= 1;
+        h *= 2;
+    }
+    return cudaSuccess;
+}
+
 cudaError_t suffix_sort(const void *d_T, int symbytes, uint64_t n, bool gsa, SortWorkspace &ws,
                         const SortOptions &opt, uint32_t *d_err, cudaStream_t st, SortStats *stats)
 {
@@ -872,73 +1040,7 @@ cudaError_t suffix_sort(const void *d_T, int symbytes, uint64_t n, bool gsa, Sor
     if (e != cudaSuccess) return e;
 
     // ---- doubling rounds over the active suffixes
-    const int b2 = gsais_bits_for(n);
-    uint64_t h = (uint64_t)K;
-    while (kept > 0) {
-        if (++S.rounds > 64) {
-            uint32_t flag = GSAIS_ERR_ROUNDS;
-            cudaMemcpyAsync(d_err, &flag, 4, cudaMemcpyHostToDevice, st);
-            cudaStreamSynchronize(st);
-            return cudaErrorUnknown;
-        }
-        S.active_total += kept;
-        const uint64_t N = kept, G = groups;
-        const int gb = gsais_bits_for(G > 1 ? G - 1 : 0);
-        const int end_bit = b2 + gb;   // large ids < G: unused top digits are skipped by the sort
-        const int passes = (end_bit + 7) / 8;
-        uint32_t *act_i = ws.vals[av], *act_pos = ws.pos[pg], *act_gid = ws.gid[pg];
-        uint32_t *out_i = ws.vals[av ^ 1], *out_pos = ws.pos[pg ^ 1], *out_gid = ws.gid[pg ^ 1];
-        uint32_t *r2 = reinterpret_cast<uint32_t *>(ws.keys[1]);   // consumed before the large sort reuses keys[1]
-        if ((e = cudaMemsetAsync(ws.counters, 0, 2 * sizeof(unsigned long long), st)) != cudaSuccess) return e;
-        if ((e = cudaMemsetAsync(ws.radix.hist, 0, (size_t)passes * 256 * 4, st)) != cudaSuccess) return e;
-        GSAIS_COUNTED((k_classify<<<stream_grid(G, 256), 256, 0, st>>>(ws.gstart[pg], G, N, ws.lid, ws.loff,
-                                                                      ws.counters + 1)));
-        cudaEvent_t ev_rk = ws.radix.prof ? ws.radix.prof->begin(st) : nullptr;
-        GSAIS_COUNTED((k_round_r2<<<stream_grid(N, 256), 256, 0, st>>>(
-            act_i, act_pos, act_gid, ws.gstart[pg], ws.lid, ws.loff, ws.rank, h, N, n, b2, r2, ws.keys[0],
-            ws.lvals[0], ws.lpos, d_err, passes, end_bit, ws.radix.hist)));
-        if (ev_rk) ws.radix.prof->end(KK_ROUND_KEYS, ev_rk, st, N * 28);
-        cudaEvent_t ev_sm = ws.radix.prof ? ws.radix.prof->begin(st) : nullptr;
-        GSAIS_COUNTED((k_small_groups<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(
-            act_i, act_pos, act_gid, r2, N, ws.rank, ws.sa, out_i, out_pos, out_gid, ws.gstart[pg ^ 1],
-            ws.counters)));
-        if (ev_sm) ws.radix.prof->end(KK_SMALL, ev_sm, st, N * 32);
-        if ((e = cudaMemcpyAsync(ws.h_small, ws.counters, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
-                                 st)) != cudaSuccess)
-            return e;
-        if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
-        const unsigned long long small_tot = reinterpret_cast<unsigned long long *>(ws.h_small)[0];
-        const unsigned long long large_tot = reinterpret_cast<unsigned long long *>(ws.h_small)[1];
-        const uint64_t NL = (uint32_t)large_tot;
-        if (NL == 0) {
-            kept = (uint32_t)small_tot;
-            groups = (uint32_t)(small_tot >> 32);
-        } else {
-            uint64_t *kk[2] = {ws.keys[0], ws.keys[1]};
-            uint32_t *vv[2] = {ws.lvals[0], ws.lvals[1]};
-            int which = 0;
-            if ((e = radix_sort_pairs(kk, vv, NL, end_bit, ws.radix, d_err, st, &which, &ran, true)) != cudaSuccess)
-                return e;
-            S.radix_passes += ran;
-            S.large_total += NL;
-            TileArgs r;
-            r.keys = kk[which];
-            r.keys32 = nullptr;
-            r.vals = vv[which];
-            r.pos = ws.lpos;
-            r.N = NL;
-            r.n = n;
-            r.K = (uint32_t)K;
-            r.zlo = r.zhi = 0;
-            if ((e = run_assign<MODE_ROUND>(r, ws, out_i, out_pos, out_gid, ws.gstart[pg ^ 1], ws.counters, st, &kept,
-                                            &groups)) != cudaSuccess)
-                return e;
-        }
-        int sv = av;
-        av = sv ^ 1;
-        pg ^= 1;
-        h *= 2;
-    }
+    if ((e = run_rounds(ws, n, K, kept, groups, av, pg, d_err, st, S)) != cudaSuccess) return e;
     uint32_t herr = 0;
     if ((e = cudaMemcpyAsync(ws.h_small, d_err, 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
@@ -976,6 +1078,89 @@ cudaError_t gsa_validate(const void *d_T, int symbytes, uint64_t n, uint32_t *d_
     if ((e = cudaMemcpyAsync(h_flag, d_flag, 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
     *valid = (*h_flag == 0);
+    return cudaGetLastError();
+}
+
+}  // namespace gsais
+
+namespace gsais {
+
+size_t batch_workspace_bytes(uint64_t n, uint32_t count) { return sort_workspace_bytes(n + count, 1); }
+
+cudaError_t batch_suffix_sort(const uint8_t *d_T, uint64_t n, const uint64_t *d_offs, uint32_t count,
+                              SortWorkspace &ws, uint32_t *d_err, cudaStream_t st, SortStats *stats)
+{
+    cudaError_t e;
+    SortStats local;
+    SortStats &S = stats ? *stats : local;
+    S = SortStats();
+    if (n == 0) return cudaSuccess;
+    const uint64_t nr = n + count;   // rank domain: every string followed by its gap slot
+
+    uint32_t *h_hist = ws.h_small + 16;
+    uint16_t *h_codes = reinterpret_cast<uint16_t *>(ws.h_small + 16 + 65536);
+    if ((e = symbol_histogram(d_T, 1, n, ws.hist, h_hist, st)) != cudaSuccess) return e;
+    uint32_t sigma = 0;
+    for (int c = 0; c < 256; ++c) {
+        if (h_hist[c]) ++sigma;
+        h_codes[c] = h_hist[c] ? (uint16_t)sigma : (uint16_t)0;   // codes 1..sigma; 0 = end of string
+    }
+    const int bits = gsais_bits_for(sigma);
+    const int sid_bits = gsais_bits_for(count > 1 ? count - 1 : 0);
+    int K = (64 - sid_bits) / bits;
+    if (K < 1) K = 1;
+    S.seed_symbols = K;
+    S.seed_bits = bits;
+    ws.pack_bits = 0;
+    if ((e = cudaMemcpyAsync(ws.codes, h_codes, 256 * 2, cudaMemcpyHostToDevice, st)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(ws.rank, 0, (nr + 1) * sizeof(uint32_t), st)) != cudaSuccess) return e;
+
+    const int seed_end = K * bits + sid_bits;
+    const int seed_passes = (seed_end + 7) / 8;
+    if ((e = cudaMemsetAsync(ws.radix.hist, 0, (size_t)seed_passes * 256 * 4, st)) != cudaSuccess) return e;
+    cudaEvent_t ev_seed = ws.radix.prof ? ws.radix.prof->begin(st) : nullptr;
+    GSAIS_COUNTED((k_seed_batch<<<stream_grid(n, 256), 256, 0, st>>>(d_T, n, d_offs, count, ws.codes, bits, K,
+                                                                     ws.keys[0], ws.vals[0], seed_passes, seed_end,
+                                                                     ws.radix.hist)));
+    if (ev_seed) ws.radix.prof->end(KK_SEED, ev_seed, st, n * 13);
+    int w = 0, ran = 0;
+    {
+        uint64_t *kk[2] = {ws.keys[0], ws.keys[1]};
+        uint32_t *vv[2] = {ws.vals[0], ws.vals[1]};
+        if ((e = radix_sort_pairs(kk, vv, n, seed_end, ws.radix, d_err, st, &w, &ran, true)) != cudaSuccess) return e;
+        S.radix_passes += ran;
+    }
+    // seed-round groups: equal (string, K-window); windows that reach the gap are unique
+    TileArgs a;
+    a.keys = ws.keys[w];
+    a.keys32 = nullptr;
+    a.vals = ws.vals[w];
+    a.pos = nullptr;
+    a.N = n;
+    a.n = nr;
+    a.K = (uint32_t)K;
+    a.zlo = a.zhi = 0;
+    uint32_t kept = 0, groups = 0;
+    const int av = w ^ 1, pg = 0;
+    if ((e = run_assign<MODE_ROUND>(a, ws, ws.vals[av], ws.pos[pg], ws.gid[pg], ws.gstart[pg], nullptr, st, &kept,
+                                    &groups)) != cudaSuccess)
+        return e;
+    if ((e = run_rounds(ws, nr, K, kept, groups, av, pg, d_err, st, S)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(ws.h_small, d_err, 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+    if (ws.radix.prof) ws.radix.prof->flush();
+    return ws.h_small[0] ? cudaErrorUnknown : cudaSuccess;
+}
+
+cudaError_t batch_outputs(const SortWorkspace &ws, const uint8_t *d_T, uint64_t n, const uint64_t *d_offs,
+                          uint32_t count, int32_t *d_sa, uint8_t *d_U, int32_t *d_primary, uint32_t *d_err,
+                          cudaStream_t st)
+{
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(d_primary, 0, (size_t)count * sizeof(int32_t), st)) != cudaSuccess) return e;
+    if (n == 0) return cudaSuccess;
+    GSAIS_COUNTED((k_batch_outputs<<<stream_grid(n, 256), 256, 0, st>>>(ws.sa, ws.rank, d_T, n, d_offs, count, d_sa,
+                                                                        d_U, d_primary, d_err)));
     return cudaGetLastError();
 }
 
