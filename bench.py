@@ -266,6 +266,91 @@ def run_batched(G, torch, count: int = 4096, steps: int = 3, warmup: int = 1, cp
             "cpu_port_mb_s": round(cpu_n / 1e6 / cpu_s, 2), "cpu_sample": f"first {cpu_strings} strings, 1 thread"}
 
 
+def _job_hash(res, SA, U) -> int:
+    """64-bit wrapping checksum of one job's outputs (compare two paths bit for bit)."""
+    m = np.uint64(0x9E3779B97F4A7C15)
+    with np.errstate(over="ignore"):
+        h = int((SA.astype(np.uint64) * m).sum(dtype=np.uint64))
+        h ^= int((U.astype(np.uint64) * np.uint64(1099511628211)).sum(dtype=np.uint64)) << 1
+    return (h ^ (int(res) & 0xFFFFFFFFFFFFFFFF)) & 0xFFFFFFFFFFFFFFFF
+
+
+def make_serving_jobs(count: int, seed: int = 6):
+    """The serving stream's jobs: lengths log-uniform over 4 KiB - 64 MiB; 70% order-2
+    Markov ACGT uint8, 20% uniform 0-255 uint8, 10% uint16 Zipf(1.1) over 1..65535.
+    Texts are seeded slices of three seeded pools (so generation stays fast)."""
+    from libsais_gb300 import textgen
+    u = textgen.uniform(3 * count, seed)
+    lens = textgen.loguniform_lengths(count, 4096, 64 << 20, seed + 1)
+    dna = textgen.markov2_dna(1 << 29, seed=seed + 2)
+    byt = np.frombuffer(np.random.default_rng(seed + 3).bytes(1 << 27), dtype=np.uint8)
+    zipf = textgen.zipf_u16(1 << 26, seed=seed + 4)
+    jobs = []
+    for k in range(count):
+        n = int(lens[k])
+        if u[3 * k] < 0.7:
+            pool = dna
+        elif u[3 * k] < 0.9:
+            pool = byt
+        else:
+            pool = zipf
+        n = min(n, pool.size)
+        a = int(u[3 * k + 1] * (pool.size - n))
+        jobs.append(pool[a:a + n])
+    return jobs
+
+
+def run_serving(G, rates=(100, 1000, 5000), max_jobs: int = 600, seconds: float = 4.0, seed: int = 6,
+                budget: int = 120 << 30, workers: int = 3):
+    """Continuous-batching server vs the plain one-job-at-a-time GPU path."""
+    jobs_all = make_serving_jobs(max_jobs, seed)
+    out = {"budget_bytes": budget, "workers": workers, "rates": []}
+    from libsais_gb300 import textgen
+    for rate in rates:
+        count = int(min(max_jobs, max(50, rate * seconds)))
+        jobs = jobs_all[:count]
+        arrivals = textgen.poisson_arrivals(count, float(rate), seed + 10 + rate)
+        srv = G.Server(hbm_budget_bytes=budget, workers=workers, small_job_symbols=1 << 20, max_batch=256)
+        ids, hashes, lat, queued = [], [], [], []
+        t0 = time.perf_counter()
+        for k, t in enumerate(jobs):
+            delay = arrivals[k] - (time.perf_counter() - t0)
+            if delay > 0:
+                time.sleep(delay)
+            ids.append(srv.submit(t))
+        for jid in ids:
+            res, SA, U, q, total, b = srv.wait(jid)
+            hashes.append(_job_hash(res, SA, U))
+            lat.append(total)
+            queued.append(q)
+        st = srv.stats()
+        srv.close()
+        sym = int(sum(t.size for t in jobs))
+        lat_ms = np.array(lat) * 1e3
+        # plain path: one job at a time through the host C-ABI, same outputs expected
+        lib = G.load()
+        same = True
+        t1 = time.perf_counter()
+        for k, t in enumerate(jobs):
+            SA = np.empty(t.size, dtype=np.int32)
+            U = np.empty_like(t)
+            res = lib.gsais_sa_bwt(None, t.ctypes.data, t.itemsize, t.size, SA.ctypes.data, 4, U.ctypes.data,
+                                   None, 4)
+            same &= _job_hash(res, SA, U) == hashes[k]
+        plain_s = time.perf_counter() - t1
+        out["rates"].append({
+            "rate_per_s": rate, "jobs": count, "input_mb": round(sym / 1e6, 1),
+            "p50_ms": round(float(np.percentile(lat_ms, 50)), 2), "p95_ms": round(float(np.percentile(lat_ms, 95)), 2),
+            "p99_ms": round(float(np.percentile(lat_ms, 99)), 2),
+            "served_mb_s": round(sym / 1e6 / st["busy_seconds"], 1),
+            "plain_one_job_at_a_time_mb_s": round(sym / 1e6 / plain_s, 1),
+            "coalesced_batches": st["batches"], "coalesced_jobs": st["batched_jobs"],
+            "hbm_high_water_gb": round(st["hbm_high_water_bytes"] / 1e9, 2), "rejected": st["rejected"],
+            "identical_to_single_job_path": bool(same)})
+    out["footprint_bytes_per_symbol"] = 80.0
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -390,6 +475,9 @@ def main():
     if rank == 0 and world == 1 and not args.no_extras:
         G.release_workspace()
         extras["batched"] = run_batched(G, torch, count=args.batch_strings)
+        G.release_workspace()
+        torch.cuda.empty_cache()
+        extras["serving"] = run_serving(G)
 
     if rank == 0:
         line = {

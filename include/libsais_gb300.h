@@ -79,6 +79,49 @@ extern "C" {
     /** gsais_batch_sa_bwt on device buffers (n = offsets[count], given by the caller). */
     int64_t gsais_batch_sa_bwt_device(void * ctx, const void * T, int64_t n, const int64_t * offsets, int32_t count, int32_t * SA, uint8_t * U, int32_t * primary, void * stream);
 
+    /**
+    * SA+BWT request loop with continuous batching.  `workers` host threads each own a
+    * CUDA stream and device workspace, so jobs taken by different workers overlap on
+    * the GPU; a free worker takes the oldest queued job and, if it is a small 8-bit job
+    * (n <= small_job_symbols), coalesces the small 8-bit jobs queued behind it (up to
+    * max_batch) into one batched sort.  Each worker may hold budget/workers bytes of
+    * device memory; a job needs about footprint_bytes_per_symbol * n bytes, and jobs
+    * that do not fit a worker's share complete with -2.
+    * @return an opaque server handle, or NULL.
+    */
+    void * gsais_server_create(int64_t hbm_budget_bytes, int32_t workers, int64_t small_job_symbols, int32_t max_batch);
+
+    /**
+    * Queues SA+BWT of T[0..n-1] (host memory, symbytes 1 or 2, n >= 2); SA (int32) and
+    * U receive the outputs.  The buffers must stay valid until the job is waited for.
+    * @return the job id (> 0), or -1 / -2.
+    */
+    int64_t gsais_server_submit(void * server, const void * T, int32_t symbytes, int64_t n, int32_t * SA, void * U);
+
+    /**
+    * Blocks until job `id` completes; stores its result (the BWT primary index, or -1 /
+    * -2), the seconds it waited in the queue, its total latency and the number of jobs in
+    * the batch it ran in.  Returns 0, or -1 for an unknown id.
+    */
+    int32_t gsais_server_wait(void * server, int64_t id, int64_t * result, double * queued_s, double * total_s, int32_t * batched);
+
+    typedef struct gsais_server_stats
+    {
+        int64_t submitted, completed, rejected;
+        int64_t batches;              /* coalesced launches of more than one job */
+        int64_t batched_jobs;         /* jobs that ran in such batches */
+        int64_t symbols_done;
+        int64_t hbm_high_water_bytes; /* peak admitted footprint */
+        int64_t hbm_budget_bytes;
+        double busy_seconds;          /* first submit to last completion */
+        double footprint_bytes_per_symbol;
+    } gsais_server_stats;
+
+    int32_t gsais_server_get_stats(void * server, gsais_server_stats * out);
+
+    /** Drains the queue, stops the workers and frees their contexts. */
+    void gsais_server_destroy(void * server);
+
     /** Statistics of the last suffix sort run on a context. */
     typedef struct gsais_stats
     {

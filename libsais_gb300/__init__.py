@@ -104,6 +104,11 @@ _SIGS = {
     "gsais_sa_device_noalloc": (_i64, [_p, _i32, _i64, _i32, _p, _p]),
     "gsais_batch_sa_bwt": (_i64, [_p, _p, _p, _i32, _p, _p, _p]),
     "gsais_batch_sa_bwt_device": (_i64, [_p, _p, _i64, _p, _i32, _p, _p, _p, _p]),
+    "gsais_server_create": (_p, [_i64, _i32, _i64, _i32]),
+    "gsais_server_submit": (_i64, [_p, _p, _i32, _i64, _p, _p]),
+    "gsais_server_wait": (_i32, [_p, _i64, _p, _p, _p, _p]),
+    "gsais_server_get_stats": (_i32, [_p, _p]),
+    "gsais_server_destroy": (None, [_p]),
 }
 
 EXPORTED_SYMBOLS = tuple(_SIGS)
@@ -428,3 +433,61 @@ def batch_sa_bwt_device(T, offsets, SA, U, primary, ctx=None, stream=None):
 def release_workspace(ctx=None) -> None:
     """Free the device workspace cached by a context (the process-wide one by default)."""
     load().gsais_release_workspace(ctx.handle if ctx else None)
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", _i64), ("completed", _i64), ("rejected", _i64), ("batches", _i64),
+                ("batched_jobs", _i64), ("symbols_done", _i64), ("hbm_high_water_bytes", _i64),
+                ("hbm_budget_bytes", _i64), ("busy_seconds", ctypes.c_double),
+                ("footprint_bytes_per_symbol", ctypes.c_double)]
+
+
+class Server:
+    """gsais_server_*: SA+BWT request loop with continuous batching."""
+
+    def __init__(self, hbm_budget_bytes: int, workers: int = 2, small_job_symbols: int = 1 << 20,
+                 max_batch: int = 256):
+        self.lib = load()
+        self.handle = self.lib.gsais_server_create(hbm_budget_bytes, workers, small_job_symbols, max_batch)
+        if not self.handle:
+            raise MemoryError("gsais_server_create failed")
+        self._keep = {}
+
+    def submit(self, T):
+        T = _text(T)
+        n = T.size
+        SA = np.empty(n, dtype=np.int32)
+        U = np.empty(n, dtype=T.dtype)
+        jid = int(self.lib.gsais_server_submit(self.handle, _ptr(T), T.itemsize, n, _ptr(SA), _ptr(U)))
+        if jid > 0:
+            self._keep[jid] = (T, SA, U)
+        return jid
+
+    def wait(self, jid: int):
+        """(result, SA, U, queued_s, total_s, batched)"""
+        res = ctypes.c_int64()
+        q = ctypes.c_double()
+        t = ctypes.c_double()
+        b = ctypes.c_int32()
+        rc = self.lib.gsais_server_wait(self.handle, jid, ctypes.byref(res), ctypes.byref(q), ctypes.byref(t),
+                                        ctypes.byref(b))
+        if rc != 0:
+            raise KeyError(jid)
+        T, SA, U = self._keep.pop(jid)
+        return int(res.value), SA, U, q.value, t.value, b.value
+
+    def stats(self) -> dict:
+        s = ServerStats()
+        self.lib.gsais_server_get_stats(self.handle, ctypes.byref(s))
+        return {k: getattr(s, k) for k, _ in ServerStats._fields_}
+
+    def close(self):
+        if self.handle:
+            self.lib.gsais_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
