@@ -351,6 +351,58 @@ def run_serving(G, rates=(100, 1000, 5000), max_jobs: int = 600, seconds: float 
     return out
 
 
+def _timed(torch, fn, steps: int = 3, warmup: int = 1):
+    for _ in range(warmup):
+        rc = fn()
+        if rc < 0:
+            raise SystemExit(f"call failed: {rc}")
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def run_plcp_lcp(G, torch, dT, dSA, n: int):
+    """PLCP (Phi + chunked Kasai) and LCP of the resident text and SA."""
+    dP = torch.empty_like(dSA)
+    dL = torch.empty_like(dSA)
+    stream = torch.cuda.current_stream()
+    plcp_ms = _timed(torch, lambda: G.plcp_device(dT, dSA, dP, stream=stream))
+    lcp_ms = _timed(torch, lambda: G.lcp_device(dP, dSA, dL, stream=stream))
+    return {"plcp_mb_s": round(n / 1e6 / (plcp_ms / 1e3), 1), "plcp_ms": round(plcp_ms, 3),
+            "lcp_mb_s": round(n / 1e6 / (lcp_ms / 1e3), 1), "lcp_ms": round(lcp_ms, 3)}
+
+
+def run_gsa(G, torch, reads: int = 1 << 20):
+    """Generalized SA + GSA-PLCP + LCP of the read set: 2^20 reads of length
+    N(150, 20) clipped to [50, 300] from a 4 Mbp reference with 1% substitutions,
+    each terminated by byte 0.  Checked against the oracle's linear-time SA
+    checker and its PLCP."""
+    from libsais_gb300 import textgen
+    from oracle.oracle import Oracle
+    T = textgen.reads_gsa(reads, ref_len=4_000_000, seed=4)
+    n = T.size
+    dT = torch.from_numpy(T).cuda()
+    dSA = torch.empty(n, dtype=torch.int32, device="cuda")
+    stream = torch.cuda.current_stream()
+    sa_ms = _timed(torch, lambda: G.sa_device(dT, dSA, gsa=True, stream=stream))
+    dP = torch.empty_like(dSA)
+    dL = torch.empty_like(dSA)
+    plcp_ms = _timed(torch, lambda: G.plcp_device(dT, dSA, dP, gsa=True, stream=stream))
+    lcp_ms = _timed(torch, lambda: G.lcp_device(dP, dSA, dL, stream=stream))
+    O = Oracle()
+    SA = dSA.cpu().numpy().astype(np.int64)
+    ok_sa = O.check_sa(T, SA, gsa=True)
+    ok_plcp = bool(np.array_equal(dP.cpu().numpy().astype(np.int64), O.plcp(T, SA, gsa=True)))
+    return {"reads": reads, "n": n, "gsa_mb_s": round(n / 1e6 / (sa_ms / 1e3), 1), "gsa_ms": round(sa_ms, 3),
+            "plcp_gsa_mb_s": round(n / 1e6 / (plcp_ms / 1e3), 1), "lcp_mb_s": round(n / 1e6 / (lcp_ms / 1e3), 1),
+            "sa_valid": bool(ok_sa), "plcp_matches_oracle": ok_plcp}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -473,6 +525,9 @@ def main():
 
     extras = {}
     if rank == 0 and world == 1 and not args.no_extras:
+        extras["plcp_lcp"] = run_plcp_lcp(G, torch, dT, dSA, n)
+        G.release_workspace()
+        extras["gsa"] = run_gsa(G, torch)
         G.release_workspace()
         extras["batched"] = run_batched(G, torch, count=args.batch_strings)
         G.release_workspace()

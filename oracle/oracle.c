@@ -279,12 +279,16 @@ void oracle_lcp(const idx_t *PLCP, const idx_t *SA, idx_t *LCP, idx_t n)
 int oracle_check_sa(const void *T, int symbytes, const idx_t *SA, idx_t n, int gsa)
 {
     if (n <= 0) return 1;
-    idx_t *isa = (idx_t *)malloc((size_t)(n + 1) * sizeof(idx_t));
+    /* inverse ranks stored as rank + 1 (0 = unset / the end of the text), in
+       32 bits when they fit so very long texts stay within host memory */
+    const int narrow = n < 0xFFFFFFFFll;
+    void *isa = calloc((size_t)(n + 1), narrow ? sizeof(uint32_t) : sizeof(idx_t));
     if (!isa) return -2;
-    for (idx_t i = 0; i <= n; i++) isa[i] = -1;
+    #define ISA_GET(p) (narrow ? (idx_t)((uint32_t *)isa)[p] : ((idx_t *)isa)[p])
+    #define ISA_SET(p, v) do { if (narrow) ((uint32_t *)isa)[p] = (uint32_t)(v); else ((idx_t *)isa)[p] = (v); } while (0)
     for (idx_t i = 0; i < n; i++) {
-        if (SA[i] < 0 || SA[i] >= n || isa[SA[i]] != -1) { free(isa); return 0; }
-        isa[SA[i]] = i;
+        if (SA[i] < 0 || SA[i] >= n || ISA_GET(SA[i]) != 0) { free(isa); return 0; }
+        ISA_SET(SA[i], i + 1);
     }
     #define SYM(p) (symbytes == 1 ? (int64_t)((const uint8_t *)T)[p] : (int64_t)((const uint16_t *)T)[p])
     int ok = 1;
@@ -295,9 +299,11 @@ int oracle_check_sa(const void *T, int symbytes, const idx_t *SA, idx_t n, int g
         if (ca > cb) { ok = 0; break; }
         if (gsa && ca == 0) { ok = a < b; continue; }
         /* equal symbol: compare the following suffixes by rank (end = smallest) */
-        if (isa[a + 1] >= isa[b + 1]) ok = 0;
+        if (ISA_GET(a + 1) >= ISA_GET(b + 1)) ok = 0;
     }
     #undef SYM
+    #undef ISA_GET
+    #undef ISA_SET
     free(isa);
     return ok;
 }
