@@ -63,6 +63,9 @@ cudaError_t radix_sort_pairs(uint64_t *keys[2], uint32_t *vals[2], uint64_t n, i
 cudaError_t radix_sort_pairs32(uint32_t *keys[2], uint32_t *vals[2], uint64_t n, int end_bit,
                                RadixScratch &rs, uint32_t *d_err, cudaStream_t st, int *which,
                                int *passes_run, bool hist_ready = false);
+// Stable partition of (uint32 key, value) pairs by key bits [begin_bit, end_bit).
+cudaError_t radix_partition32(uint32_t *keys[2], uint32_t *vals[2], uint64_t n, int begin_bit, int end_bit,
+                              RadixScratch &rs, uint32_t *d_err, cudaStream_t st, int *which);
 
 // --------------------------------------------------------------- statistics
 struct SortStats {

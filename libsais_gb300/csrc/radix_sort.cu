@@ -36,8 +36,8 @@ constexpr int kHistCopies = 4;
 // kHistCopies times (by warp) to spread shared-atomic traffic.
 // Bytes per key: sizeof(K) read.
 template <typename K>
-__global__ void __launch_bounds__(256) k_upsweep(const K *__restrict__ keys, uint64_t n, int passes, int end_bit,
-                                                 uint32_t *__restrict__ hist)
+__global__ void __launch_bounds__(256) k_upsweep(const K *__restrict__ keys, uint64_t n, int passes, int begin_bit,
+                                                 int end_bit, uint32_t *__restrict__ hist)
 {
     __shared__ uint32_t sh[kHistCopies][8][256];
     for (int c = 0; c < kHistCopies; ++c) radix_hist_zero(sh[c], 8);
@@ -47,7 +47,7 @@ __global__ void __launch_bounds__(256) k_upsweep(const K *__restrict__ keys, uin
     const uint64_t n_round = (n + 31) & ~31ull;   // whole warps iterate together
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_round; i += stride) {
         const bool ok = i < n;
-        radix_hist_add(sh[copy], ok ? (uint64_t)keys[i] : 0, ok, passes, end_bit);
+        radix_hist_add(sh[copy], ok ? ((uint64_t)keys[i] >> begin_bit) : 0, ok, passes, end_bit - begin_bit);
     }
     __syncthreads();
     for (int c = 1; c < kHistCopies; ++c)
@@ -257,13 +257,13 @@ cudaError_t onesweep_attr()
 }
 
 template <typename K>
-cudaError_t sort_impl(K *keys[2], uint32_t *vals[2], uint64_t n, int end_bit, RadixScratch &rs, uint32_t *d_err,
-                      cudaStream_t st, int *which, int *passes_run, bool hist_ready)
+cudaError_t sort_impl(K *keys[2], uint32_t *vals[2], uint64_t n, int begin_bit, int end_bit, RadixScratch &rs,
+                      uint32_t *d_err, cudaStream_t st, int *which, int *passes_run, bool hist_ready)
 {
     *which = 0;
     if (passes_run) *passes_run = 0;
-    if (n <= 1 || end_bit <= 0) return cudaSuccess;
-    const int passes = (end_bit + 7) / 8;
+    if (n <= 1 || end_bit <= begin_bit) return cudaSuccess;
+    const int passes = (end_bit - begin_bit + 7) / 8;
     cudaError_t e;
     if (!hist_ready) {
         if ((e = cudaMemsetAsync(rs.hist, 0, (size_t)passes * 256 * sizeof(uint32_t), st)) != cudaSuccess) return e;
@@ -271,7 +271,7 @@ cudaError_t sort_impl(K *keys[2], uint32_t *vals[2], uint64_t n, int end_bit, Ra
         const uint64_t cap = (uint64_t)sm_count() * 8;
         const int grid = (int)(want < 1 ? 1 : (want < cap ? want : cap));
         cudaEvent_t ev = rs.prof ? rs.prof->begin(st) : nullptr;
-        GSAIS_COUNTED((k_upsweep<K><<<grid, 256, 0, st>>>(keys[0], n, passes, end_bit, rs.hist)));
+        GSAIS_COUNTED((k_upsweep<K><<<grid, 256, 0, st>>>(keys[0], n, passes, begin_bit, end_bit, rs.hist)));
         if (ev) rs.prof->end(KK_UPSWEEP, ev, st, n * sizeof(K));
     }
     GSAIS_COUNTED((k_bucket_bases<<<passes, 256, 0, st>>>(rs.hist, rs.bases)));
@@ -291,11 +291,11 @@ cudaError_t sort_impl(K *keys[2], uint32_t *vals[2], uint64_t n, int end_bit, Ra
         if (trivial) continue;
         if ((e = cudaMemsetAsync(rs.status, 0, (size_t)tiles * 256 * sizeof(uint64_t), st)) != cudaSuccess) return e;
         if ((e = cudaMemsetAsync(rs.counters + p, 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
-        const int bits = end_bit - 8 * p < 8 ? end_bit - 8 * p : 8;
+        const int bits = end_bit - begin_bit - 8 * p < 8 ? end_bit - begin_bit - 8 * p : 8;
         const uint32_t mask = (1u << bits) - 1u;
         cudaEvent_t ev1 = rs.prof ? rs.prof->begin(st) : nullptr;
         GSAIS_COUNTED((k_onesweep<K><<<(unsigned)tiles, OnesweepShape<K>::kThreads, onesweep_smem<K>(), st>>>(
-            keys[cur], vals[cur], keys[cur ^ 1], vals[cur ^ 1], n, 8 * p, mask, rs.bases + p * 256, rs.status,
+            keys[cur], vals[cur], keys[cur ^ 1], vals[cur ^ 1], n, begin_bit + 8 * p, mask, rs.bases + p * 256, rs.status,
             rs.counters + p, d_err)));
         // algorithmic bytes: every (key, value) pair read once and written once
         if (ev1) rs.prof->end(KK_ONESWEEP, ev1, st, 2 * n * (sizeof(K) + sizeof(uint32_t)));
@@ -319,13 +319,19 @@ size_t radix_status_words(uint64_t n)
 cudaError_t radix_sort_pairs(uint64_t *keys[2], uint32_t *vals[2], uint64_t n, int end_bit, RadixScratch &rs,
                              uint32_t *d_err, cudaStream_t st, int *which, int *passes_run, bool hist_ready)
 {
-    return sort_impl<uint64_t>(keys, vals, n, end_bit, rs, d_err, st, which, passes_run, hist_ready);
+    return sort_impl<uint64_t>(keys, vals, n, 0, end_bit, rs, d_err, st, which, passes_run, hist_ready);
 }
 
 cudaError_t radix_sort_pairs32(uint32_t *keys[2], uint32_t *vals[2], uint64_t n, int end_bit, RadixScratch &rs,
                                uint32_t *d_err, cudaStream_t st, int *which, int *passes_run, bool hist_ready)
 {
-    return sort_impl<uint32_t>(keys, vals, n, end_bit, rs, d_err, st, which, passes_run, hist_ready);
+    return sort_impl<uint32_t>(keys, vals, n, 0, end_bit, rs, d_err, st, which, passes_run, hist_ready);
+}
+
+cudaError_t radix_partition32(uint32_t *keys[2], uint32_t *vals[2], uint64_t n, int begin_bit, int end_bit,
+                              RadixScratch &rs, uint32_t *d_err, cudaStream_t st, int *which)
+{
+    return sort_impl<uint32_t>(keys, vals, n, begin_bit, end_bit, rs, d_err, st, which, nullptr, false);
 }
 
 std::atomic<uint64_t> g_launches{0};

@@ -178,6 +178,7 @@ struct TileArgs {
     const uint32_t *keys32;  // non-null: 32-bit keys (the seed round with short seeds)
     const uint32_t *vals;
     const uint32_t *pos;     // nullptr: identity (the seed round)
+    uint32_t *rank_out;      // non-null: new ranks go here by list position (scattered later)
     uint64_t N;              // entries in this round
     uint64_t n;              // text length
     uint32_t K;              // seed symbols per key
@@ -392,7 +393,8 @@ __global__ void __launch_bounds__(kAssignThreads)
         if (x >= (int)valid) continue;
         const uint32_t v = s_vals[x + 1];
         const uint32_t r = lastnz(wm, hv_inc[q]);
-        rank[v] = r;
+        if (a.rank_out) a.rank_out[base + x] = r;
+        else rank[v] = r;
         if (single[q]) {
             sa[posv[q]] = v;
         } else {
@@ -410,28 +412,131 @@ __global__ void __launch_bounds__(kAssignThreads)
 // Groups of at most kSmallMax suffixes are split inside one warp (no global
 // sort); larger groups go through the onesweep radix sort keyed by
 // (dense large-group id, rank[i + h]).
-constexpr uint32_t kSmallMax = 32;
+constexpr uint32_t kSmallMax = 32;      // <= this: split inside one warp
+constexpr uint32_t kMediumMax = 4096;   // <= this: sorted and split inside one CTA
 constexpr uint32_t kNoLarge = 0xFFFFFFFFu;
+constexpr uint32_t kMedium = 0xFFFFFFFEu;
 
-// Per group: size from the group table; large groups get an id and a slot
-// range in the large list from one combined counter, so ids and ranges are
-// in the same order.  Bytes per group: 8 read, 4-8 written.
+// Per group: size from the group table.  Medium groups are listed for the
+// CTA path; large groups get an id and a slot range in the large list from
+// one combined counter, so ids and ranges are in the same order.
+// Bytes per group: 8 read, 4-8 written.
 __global__ void __launch_bounds__(256) k_classify(const uint32_t *__restrict__ gstart, uint64_t G, uint64_t N,
                                                   uint32_t *__restrict__ lid, uint32_t *__restrict__ loff,
-                                                  unsigned long long *__restrict__ lcount)
+                                                  unsigned long long *__restrict__ lcount,
+                                                  uint32_t *__restrict__ mlist, unsigned long long *__restrict__ mcount)
 {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < G; g += stride) {
         const uint64_t s = gstart[g];
         const uint64_t e = g + 1 < G ? gstart[g + 1] : N;
         const uint64_t size = e - s;
-        if (size > kSmallMax) {
+        if (size > kMediumMax) {
             const unsigned long long old = atomicAdd(lcount, (1ull << 32) | size);
             lid[g] = (uint32_t)(old >> 32);
             loff[g] = (uint32_t)old;
+        } else if (size > kSmallMax) {
+            lid[g] = kMedium;
+            mlist[atomicAdd(mcount, 1ull)] = (uint32_t)g;
         } else {
             lid[g] = kNoLarge;
         }
+    }
+}
+
+// Splits the medium groups (kSmallMax < size <= kMediumMax), one group per
+// CTA iteration: keys (rank[i+h] << 12 | member) are bitonic-sorted in
+// shared memory; a member's new slot is the group's first slot plus its
+// sorted position, its rank 1 + the first slot of its run of equal keys; a
+// run of one is final; survivors are appended behind the same atomic
+// (groups, entries) reservation as the warp path.
+// Bytes per suffix: r2 4 + index 4 read, rank scatter 4, SA 4 or survivors 12.
+__global__ void __launch_bounds__(256) k_medium_groups(const uint32_t *__restrict__ mlist,
+                                                       const unsigned long long *__restrict__ mcount,
+                                                       const uint32_t *__restrict__ gstart, uint64_t G, uint64_t N,
+                                                       const uint32_t *__restrict__ act_i,
+                                                       const uint32_t *__restrict__ act_pos,
+                                                       const uint32_t *__restrict__ r2, uint32_t *__restrict__ rank,
+                                                       uint32_t *__restrict__ sa, uint32_t *__restrict__ out_i,
+                                                       uint32_t *__restrict__ out_pos, uint32_t *__restrict__ out_gid,
+                                                       uint32_t *__restrict__ gstart_out,
+                                                       unsigned long long *__restrict__ counter)
+{
+    constexpr int THREADS = 256;
+    __shared__ uint64_t key[kMediumMax];
+    __shared__ uint32_t wb[3][THREADS / 32 + 1];
+    __shared__ unsigned long long s_base;
+    const uint32_t M = (uint32_t)*mcount;
+    const int tid = threadIdx.x;
+    for (uint32_t m = blockIdx.x; m < M; m += gridDim.x) {
+        const uint32_t g = mlist[m];
+        const uint64_t s = gstart[g];
+        const uint64_t e = (uint64_t)g + 1 < G ? gstart[g + 1] : N;
+        const uint32_t size = (uint32_t)(e - s);
+        const uint32_t P = act_pos[s];
+        uint32_t pw = 64;
+        while (pw < size) pw <<= 1;
+        for (uint32_t t = tid; t < pw; t += THREADS)
+            key[t] = t < size ? (((uint64_t)r2[s + t] << 12) | t) : ~0ull;
+        __syncthreads();
+        for (uint32_t k = 2; k <= pw; k <<= 1) {
+            for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+                for (uint32_t t = tid; t < pw; t += THREADS) {
+                    const uint32_t x = t ^ j;
+                    if (x > t) {
+                        const uint64_t a = key[t], b = key[x];
+                        if ((a > b) == ((t & k) == 0)) {
+                            key[t] = b;
+                            key[x] = a;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        // blocked ranges of sorted positions per thread
+        const uint32_t C = (size + THREADS - 1) / THREADS;
+        const uint32_t k0 = tid * C, k1 = k0 + C < size ? k0 + C : size;
+        uint32_t lastv = 0, surv = 0, sheads = 0;
+        for (uint32_t k = k0; k < k1; ++k) {
+            const uint64_t rk = key[k] >> 12;
+            const bool head = k == 0 || (key[k - 1] >> 12) != rk;
+            const bool last = k + 1 == size || (key[k + 1] >> 12) != rk;
+            if (head) lastv = k + 1;
+            if (!(head && last)) {
+                ++surv;
+                sheads += head;
+            }
+        }
+        uint32_t tot_s, tot_h, tot_l;
+        const uint32_t ex_last = block_exclusive_lastnz<THREADS>(lastv, wb[0], tot_l);
+        const uint32_t ex_surv = block_exclusive_sum<uint32_t, THREADS>(surv, wb[1], tot_s);
+        const uint32_t ex_head = block_exclusive_sum<uint32_t, THREADS>(sheads, wb[2], tot_h);
+        if (tid == 0) s_base = tot_s ? atomicAdd(counter, ((unsigned long long)tot_h << 32) | tot_s) : 0ull;
+        __syncthreads();
+        const uint32_t base_e = (uint32_t)s_base, base_g = (uint32_t)(s_base >> 32);
+        uint32_t run = ex_last, cs = ex_surv, ch = ex_head;
+        for (uint32_t k = k0; k < k1; ++k) {
+            const uint64_t kv = key[k];
+            const uint64_t rk = kv >> 12;
+            const bool head = k == 0 || (key[k - 1] >> 12) != rk;
+            const bool last = k + 1 == size || (key[k + 1] >> 12) != rk;
+            if (head) run = k + 1;
+            const uint32_t i = act_i[s + (kv & 4095u)];
+            rank[i] = 1 + P + (run - 1);
+            if (head && last) {
+                sa[P + k] = i;
+            } else {
+                ch += head;
+                const uint32_t gid = base_g + ch - 1;
+                const uint32_t c = base_e + cs++;
+                out_i[c] = i;
+                out_pos[c] = P + k;
+                out_gid[c] = gid;
+                if (head) gstart_out[gid] = c;
+            }
+        }
+        __syncthreads();   // key[] is reused by the next group
     }
 }
 
@@ -467,7 +572,7 @@ __global__ void __launch_bounds__(256) k_round_r2(const uint32_t *__restrict__ a
             else atomicOr(err, GSAIS_ERR_BOUNDS);
             const uint32_t g = act_gid[j];
             const uint32_t L = lid[g];
-            if (L == kNoLarge) {
+            if (L >= kMedium) {   // small or medium group: keep rank[i+h] by list position
                 r2o[j] = r2;
             } else {
                 large = true;
@@ -748,6 +853,24 @@ __global__ void __launch_bounds__(256) k_batch_outputs(const uint32_t *__restric
     }
 }
 
+// rank[pos[j]] = r[j] for a list partitioned by the high bits of pos, so
+// the writes of each stretch land in one L2-resident window of rank[] and
+// reach DRAM as whole sectors.  Bytes per entry: 8 read, 4 written.
+__global__ void __launch_bounds__(256) k_scatter_ranks(const uint32_t *__restrict__ pos,
+                                                       const uint32_t *__restrict__ r, uint64_t N, uint64_t nr,
+                                                       uint32_t *__restrict__ rank, uint32_t *__restrict__ err)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < N; j += stride) {
+        const uint32_t p = pos[j];
+        if (p >= nr) {
+            atomicOr(err, GSAIS_ERR_BOUNDS);
+            continue;
+        }
+        rank[p] = r[j];
+    }
+}
+
 // GSA validity: T[n-1] == 0, T[0] != 0, no two adjacent zeros.
 template <typename Sym>
 __global__ void k_gsa_check(const Sym *__restrict__ T, uint64_t n, uint32_t *__restrict__ flag)
@@ -865,6 +988,26 @@ static cudaError_t run_assign(const TileArgs &a, SortWorkspace &ws, uint32_t *ou
     return cudaGetLastError();
 }
 
+// Seed round: for a large rank domain the new ranks are written by list
+// position, partitioned by the top 8 bits of the suffix position and then
+// scattered inside L2-resident windows (instead of one random 4-byte write
+// per suffix into a rank array larger than L2).
+static bool use_two_level_ranks(uint64_t nr) { return nr >= (1ull << 23); }
+
+static cudaError_t scatter_seed_ranks(SortWorkspace &ws, uint32_t *sorted_pos, uint32_t *ranks, uint64_t N,
+                                      uint64_t nr, uint32_t *d_err, cudaStream_t st)
+{
+    const int b = gsais_bits_for(nr);
+    uint32_t *kk[2] = {sorted_pos, ws.lvals[0]};
+    uint32_t *vv[2] = {ranks, ws.lvals[1]};
+    int which = 0;
+    cudaError_t e = radix_partition32(kk, vv, N, b > 8 ? b - 8 : 0, b, ws.radix, d_err, st, &which);
+    if (e != cudaSuccess) return e;
+    GSAIS_COUNTED((k_scatter_ranks<<<stream_grid(N, 256), 256, 0, st>>>(kk[which], vv[which], N, nr, ws.rank,
+                                                                        d_err)));
+    return cudaGetLastError();
+}
+
 // Doubling rounds over the kept groups of the seed round until every suffix
 // is final.  nr = length of the rank domain (rank[nr] is the sentinel).
 static cudaError_t run_rounds(SortWorkspace &ws, uint64_t nr, int K, uint32_t kept, uint32_t groups, int av, int pg,
@@ -889,10 +1032,12 @@ static cudaError_t run_rounds(SortWorkspace &ws, uint64_t nr, int K, uint32_t ke
         uint32_t *act_i = ws.vals[av], *act_pos = ws.pos[pg], *act_gid = ws.gid[pg];
         uint32_t *out_i = ws.vals[av ^ 1], *out_pos = ws.pos[pg ^ 1], *out_gid = ws.gid[pg ^ 1];
         uint32_t *r2 = reinterpret_cast<uint32_t *>(ws.keys[1]);   // consumed before the large sort reuses keys[1]
-        if ((e = cudaMemsetAsync(ws.counters, 0, 2 * sizeof(unsigned long long), st)) != cudaSuccess) return e;
+        // counters: [0] small+medium output, [1] large list, [2] medium groups
+        if ((e = cudaMemsetAsync(ws.counters, 0, 3 * sizeof(unsigned long long), st)) != cudaSuccess) return e;
         if ((e = cudaMemsetAsync(ws.radix.hist, 0, (size_t)passes * 256 * 4, st)) != cudaSuccess) return e;
+        uint32_t *mlist = ws.lvals[1];   // free until the large sort's first pass
         GSAIS_COUNTED((k_classify<<<stream_grid(G, 256), 256, 0, st>>>(ws.gstart[pg], G, N, ws.lid, ws.loff,
-                                                                      ws.counters + 1)));
+                                                                      ws.counters + 1, mlist, ws.counters + 2)));
         cudaEvent_t ev_rk = ws.radix.prof ? ws.radix.prof->begin(st) : nullptr;
         GSAIS_COUNTED((k_round_r2<<<stream_grid(N, 256), 256, 0, st>>>(
             act_i, act_pos, act_gid, ws.gstart[pg], ws.lid, ws.loff, ws.rank, h, N, nr, b2, r2, ws.keys[0],
@@ -903,6 +1048,9 @@ static cudaError_t run_rounds(SortWorkspace &ws, uint64_t nr, int K, uint32_t ke
             act_i, act_pos, act_gid, r2, N, ws.rank, ws.sa, out_i, out_pos, out_gid, ws.gstart[pg ^ 1],
             ws.counters)));
         if (ev_sm) ws.radix.prof->end(KK_SMALL, ev_sm, st, N * 32);
+        GSAIS_COUNTED((k_medium_groups<<<stream_grid(G * 256, 256), 256, 0, st>>>(
+            mlist, ws.counters + 2, ws.gstart[pg], G, N, act_i, act_pos, r2, ws.rank, ws.sa, out_i, out_pos, out_gid,
+            ws.gstart[pg ^ 1], ws.counters)));
         if ((e = cudaMemcpyAsync(ws.h_small, ws.counters, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                                  st)) != cudaSuccess)
             return e;
@@ -926,6 +1074,7 @@ static cudaError_t run_rounds(SortWorkspace &ws, uint64_t nr, int K, uint32_t ke
             r.keys32 = nullptr;
             r.vals = vv[which];
             r.pos = ws.lpos;
+            r.rank_out = nullptr;
             r.N = NL;
             r.n = nr;
             r.K = (uint32_t)K;
@@ -1023,6 +1172,7 @@ cudaError_t suffix_sort(const void *d_T, int symbytes, uint64_t n, bool gsa, Sor
     a.keys32 = narrow ? k32[w] : nullptr;
     a.vals = ws.vals[w];
     a.pos = nullptr;
+    a.rank_out = nullptr;
     a.N = n;
     a.n = n;
     a.K = (uint32_t)K;
@@ -1031,6 +1181,7 @@ cudaError_t suffix_sort(const void *d_T, int symbytes, uint64_t n, bool gsa, Sor
     a.zhi = a.zlo << (bits - 1);
     uint32_t kept = 0, groups = 0;
     int av = w ^ 1, pg = 0;
+    if (use_two_level_ranks(n)) a.rank_out = reinterpret_cast<uint32_t *>(ws.keys[w ^ 1]);
     if (gsa)
         e = run_assign<MODE_INIT_GSA>(a, ws, ws.vals[av], ws.pos[pg], ws.gid[pg], ws.gstart[pg], nullptr, st, &kept,
                                       &groups);
@@ -1038,6 +1189,7 @@ cudaError_t suffix_sort(const void *d_T, int symbytes, uint64_t n, bool gsa, Sor
         e = run_assign<MODE_INIT_PLAIN>(a, ws, ws.vals[av], ws.pos[pg], ws.gid[pg], ws.gstart[pg], nullptr, st,
                                         &kept, &groups);
     if (e != cudaSuccess) return e;
+    if (a.rank_out && (e = scatter_seed_ranks(ws, ws.vals[w], a.rank_out, n, n, d_err, st)) != cudaSuccess) return e;
 
     // ---- doubling rounds over the active suffixes
     if ((e = run_rounds(ws, n, K, kept, groups, av, pg, d_err, st, S)) != cudaSuccess) return e;
@@ -1136,14 +1288,18 @@ cudaError_t batch_suffix_sort(const uint8_t *d_T, uint64_t n, const uint64_t *d_
     a.keys32 = nullptr;
     a.vals = ws.vals[w];
     a.pos = nullptr;
+    a.rank_out = nullptr;
     a.N = n;
     a.n = nr;
     a.K = (uint32_t)K;
     a.zlo = a.zhi = 0;
     uint32_t kept = 0, groups = 0;
     const int av = w ^ 1, pg = 0;
+    if (use_two_level_ranks(nr)) a.rank_out = reinterpret_cast<uint32_t *>(ws.keys[w ^ 1]);
     if ((e = run_assign<MODE_ROUND>(a, ws, ws.vals[av], ws.pos[pg], ws.gid[pg], ws.gstart[pg], nullptr, st, &kept,
                                     &groups)) != cudaSuccess)
+        return e;
+    if (a.rank_out && (e = scatter_seed_ranks(ws, ws.vals[w], a.rank_out, n, nr, d_err, st)) != cudaSuccess)
         return e;
     if ((e = run_rounds(ws, nr, K, kept, groups, av, pg, d_err, st, S)) != cudaSuccess) return e;
     if ((e = cudaMemcpyAsync(ws.h_small, d_err, 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
