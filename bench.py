@@ -12,10 +12,12 @@ synthetic data standing in for the genome corpora of libsais's benchmarks.
   e2e      the same step through the host C-ABI (gsais_sa_bwt) from pinned
            host buffers: H2D of the text and D2H of SA and BWT are inside the
            timed region.
-  roofline the onesweep radix-sort pass kernel (the dominant kernel): its
-           algorithmic bytes (every key/value pair read and written once)
-           over its CUDA-event time inside the timed region, against the
-           measured HBM copy bandwidth.
+  roofline the radix-sort digit pass kernel k_radix_pass (the dominant
+           kernel): its algorithmic bytes (every key/value pair read and
+           written once) over its CUDA-event time inside the timed region,
+           against the measured HBM copy bandwidth; traffic = the DRAM bytes
+           per algorithmic byte of an ncu capture of the same kernel
+           (profiles/radix_pass_traffic.json) times the launch's bytes.
   cpu_baseline  the CPU oracle port (SA-IS + BWT, 1 thread) on a bounded
            prefix of the same text.
 
@@ -473,23 +475,23 @@ def main():
     ms = reduce_max(dist, ms)
     value = world * n / 1e6 / (ms / 1e3)
 
-    # ---- dominant kernel roofline (onesweep pass), from the same timed region
+    # ---- dominant kernel roofline (radix digit pass), from the same timed region
     peak, peak_kind = peaks()
-    ks = prof.get("onesweep", {"launches": 0, "total_ms": 0.0, "bytes": 0})
+    ks = prof.get("radix_pass", {"launches": 0, "total_ms": 0.0, "bytes": 0})
     roof = None
     if ks["launches"]:
         per_launch_ms = ks["total_ms"] / ks["launches"]
         per_launch_bytes = ks["bytes"] / ks["launches"]
         achieved = per_launch_bytes / (per_launch_ms / 1e3) / 1e9
         traffic = None
-        tfile = os.path.join(ROOT, "profiles", "onesweep_traffic.json")
+        tfile = os.path.join(ROOT, "profiles", "radix_pass_traffic.json")
         if os.path.exists(tfile):
             with open(tfile) as f:
                 tr = json.load(f)
-            traffic = round(tr["dram_bytes_per_pair"] * per_launch_bytes / 24.0, 0)
+            traffic = round(tr["dram_bytes_per_algorithmic_byte"] * per_launch_bytes, 0)
         roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
-                "kernel": "k_onesweep", "launches_per_step": ks["launches"] / args.steps,
+                "kernel": "k_radix_pass", "launches_per_step": ks["launches"] / args.steps,
                 "algorithmic_bytes_per_launch": int(per_launch_bytes), "ms_per_launch": round(per_launch_ms, 4)}
     kernels = {k: {"launches_per_step": v["launches"] / args.steps,
                    "ms_per_step": round(v["total_ms"] / args.steps, 3)} for k, v in prof.items() if v["launches"]}

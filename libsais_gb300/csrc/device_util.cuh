@@ -1,5 +1,5 @@
 // device_util.cuh -- small sm_103a helpers shared by the kernels: scoped
-// relaxed loads/stores for the look-back flags, mbarrier + TMA bulk copies,
+// relaxed loads/stores, mbarrier + TMA bulk copies,
 // warp/block scans, and the bounded-spin error word.
 #pragma once
 #include <cstdint>

@@ -612,8 +612,8 @@ int32_t gsais_profile_read(void *ctx, gsais_kernel_profile *out, int32_t max_kin
     gsais_ctx *c = resolve(ctx);
     if (!c || !out) return -1;
     std::lock_guard<std::mutex> lock(c->mu);
-    static const char *names[KK_COUNT] = {"onesweep", "upsweep", "seed", "round_keys", "tile_summary", "assign",
-                                          "small_groups"};
+    static const char *names[KK_COUNT] = {"radix_pass", "tile_counts",  "upsweep", "seed",
+                                          "round_keys", "tile_summary", "assign",  "small_groups"};
     int k = 0;
     for (; k < KK_COUNT && k < max_kinds; ++k) {
         out[k].name = names[k];

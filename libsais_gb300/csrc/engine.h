@@ -16,7 +16,7 @@ extern std::atomic<uint64_t> g_launches;
 // Optional per-kernel timing: CUDA events recorded on the launching stream
 // around each launch of the instrumented kernels, resolved after the stream
 // synchronises.  `bytes` is the algorithmic traffic of the launch.
-enum KernelKind { KK_ONESWEEP = 0, KK_UPSWEEP, KK_SEED, KK_ROUND_KEYS, KK_SUMMARY, KK_ASSIGN, KK_SMALL, KK_COUNT };
+enum KernelKind { KK_RADIX_PASS = 0, KK_TILE_COUNTS, KK_UPSWEEP, KK_SEED, KK_ROUND_KEYS, KK_SUMMARY, KK_ASSIGN, KK_SMALL, KK_COUNT };
 
 struct KernelProfiler {
     bool enabled = false;
@@ -37,14 +37,15 @@ struct KernelProfiler {
 };
 
 // ---------------------------------------------------------------- radix sort
-// Onesweep LSD radix sort of (key, value) pairs: 8-bit digits, one upsweep
-// histogram pass for all digits, then one scatter pass per digit with a
-// decoupled look-back.  Digits on which every key agrees are skipped.
+// LSD radix sort of (key, value) pairs: 8-bit digits, one upsweep histogram
+// pass for all digits, then per digit a tile-count pass, a scan of the counts
+// over tiles and one scatter pass.  Digits on which every key agrees are
+// skipped.
 struct RadixScratch {
     uint32_t *hist = nullptr;      // [8][256] digit histograms
     uint32_t *bases = nullptr;     // [8][256] exclusive bucket starts
-    uint64_t *status = nullptr;    // look-back words, 256 per tile
-    uint32_t *counters = nullptr;  // [8] tile tickets, one per pass
+    uint64_t *status = nullptr;    // per (tile, digit): 32-bit count + 32-bit offset
+    uint32_t *counters = nullptr;  // [8] spare counters
     size_t status_words = 0;
     uint32_t *h_hist = nullptr;    // pinned host copy of hist
     KernelProfiler *prof = nullptr;

@@ -1,20 +1,20 @@
-// radix_sort.cu -- onesweep LSD radix sort of (key, uint32 value) pairs with
-// 32- or 64-bit keys, hand-written for sm_103a.
+// radix_sort.cu -- LSD radix sort of (key, uint32 value) pairs with 32- or
+// 64-bit keys, hand-written for sm_103a.
 //
-// Layout of one digit pass (8-bit digits, 256 buckets):
-//   * a CTA takes the next tile ticket (atomic counter, so tiles start in
-//     ticket order and the look-back below always makes progress);
-//   * full tiles are staged into shared memory with two TMA bulk copies
-//     (keys, values) completing on one mbarrier; the ragged last tile uses
-//     guarded loads;
-//   * each warp ranks its keys with __match_any_sync over the digit and a
-//     per-warp shared-memory digit histogram, in input order (stable);
-//   * per-digit tile counts are published to a decoupled look-back array and
-//     the exclusive prefix over earlier tiles is gathered with bounded spins;
-//   * keys (from registers) and values (shared -> shared) are re-ordered by
-//     digit inside the tile and written out, so each digit run of the tile
-//     lands contiguously in global memory.
-// The histograms of all digit passes come from one upsweep over the keys.
+// One digit pass (8-bit digits, 256 buckets) is reduce-then-scan over tiles:
+//   * k_tile_counts: digit counts of every tile (one read of the keys);
+//   * k_tile_offsets: per digit, an exclusive scan over the tiles plus the
+//     digit's bucket base gives every tile its global write offset per digit;
+//   * k_radix_pass: full tiles are staged into shared memory with two TMA bulk
+//     copies (keys, values) completing on one mbarrier; each warp ranks its
+//     keys in input order (stable) with eight ballots per key (lanes holding
+//     the same digit) and a per-warp shared digit counter; keys and values are
+//     re-ordered by digit inside the tile and each digit run is written
+//     contiguously at its offset.
+// No CTA waits on another (no look-back chain): on a GB300 the extra read of
+// the keys costs less than the L2 round trips a decoupled look-back spends.
+// The global digit histograms of all passes come from one upsweep over the
+// keys, or are accumulated by the producer of the keys.
 // This replaces the bucket/induction passes of libsais's SA-IS
 // (src/libsais.c:1586-1660 radix_sort_lms_suffixes, :4034 induce_partial_order)
 // as the ordering primitive of the prefix-doubling suffix sort.
@@ -26,9 +26,6 @@ namespace gsais {
 
 namespace {
 
-constexpr uint64_t kFlagAggregate = 1ull << 62;
-constexpr uint64_t kFlagPrefix = 2ull << 62;
-constexpr uint64_t kValueMask = (1ull << 62) - 1;
 constexpr int kHistCopies = 4;
 
 // Histograms of every digit pass in one read of the keys (used when the
@@ -67,131 +64,190 @@ __global__ void __launch_bounds__(256) k_bucket_bases(const uint32_t *__restrict
     bases[p * 256 + threadIdx.x] = e;
 }
 
-__device__ __forceinline__ uint32_t lookback_exclusive(uint64_t *status, uint32_t tile, uint32_t digit,
-                                                       uint32_t count, uint32_t *err)
-{
-    uint64_t *mine = status + (uint64_t)tile * 256 + digit;
-    if (tile == 0) {
-        st_relaxed_gpu(mine, kFlagPrefix | count);
-        return 0;
-    }
-    st_relaxed_gpu(mine, kFlagAggregate | count);
-    uint64_t excl = 0;
-    int64_t u = (int64_t)tile - 1;
-    uint32_t spins = 0;
-    uint64_t t0 = 0;
-    while (u >= 0) {
-        const uint64_t s = ld_relaxed_gpu(status + (uint64_t)u * 256 + digit);
-        const uint64_t f = s & ~kValueMask;
-        if (f == 0) {
-            if (spins == 0) t0 = global_ns();
-            if (++spins > GSAIS_SPIN_LIMIT || ((spins & 255) == 0 && global_ns() - t0 > GSAIS_SPIN_NS)) {
-                atomicOr(err, GSAIS_ERR_LOOKBACK_SPIN);
-                break;
-            }
-            __nanosleep(32);
-            continue;
-        }
-        excl += s & kValueMask;
-        if (f == kFlagPrefix) break;
-        --u;
-    }
-    st_relaxed_gpu(mine, kFlagPrefix | (excl + count));
-    return (uint32_t)excl;
-}
-
 template <typename K>
-struct OnesweepShape;
+struct PassShape;
 template <>
-struct OnesweepShape<uint64_t> {
+struct PassShape<uint64_t> {
     static constexpr int kThreads = 256, kItems = 16, kMinBlocks = 3;
 };
 template <>
-struct OnesweepShape<uint32_t> {
-    static constexpr int kThreads = 256, kItems = 16, kMinBlocks = 4;
+struct PassShape<uint32_t> {
+    static constexpr int kThreads = 256, kItems = 24, kMinBlocks = 3;
 };
 
 template <typename K>
-constexpr size_t onesweep_smem()
+__host__ __device__ constexpr int pass_tile()
 {
-    return (size_t)OnesweepShape<K>::kThreads * OnesweepShape<K>::kItems * (sizeof(K) + 2 * sizeof(uint32_t));
+    return PassShape<K>::kThreads * PassShape<K>::kItems;
 }
 
+// staged keys + values of one tile; values are re-ordered in place (they are
+// held in registers while the tile is ranked)
 template <typename K>
-__global__ void __launch_bounds__(OnesweepShape<K>::kThreads, OnesweepShape<K>::kMinBlocks)
-    k_onesweep(const K *__restrict__ kin, const uint32_t *__restrict__ vin, K *__restrict__ kout,
-               uint32_t *__restrict__ vout, uint64_t n, int shift, uint32_t mask, const uint32_t *__restrict__ bases,
-               uint64_t *status, uint32_t *counter, uint32_t *err)
+__host__ __device__ constexpr size_t pass_smem()
 {
-    constexpr int THREADS = OnesweepShape<K>::kThreads;
-    constexpr int ITEMS = OnesweepShape<K>::kItems;
+    return (size_t)pass_tile<K>() * (sizeof(K) + sizeof(uint32_t));
+}
+
+// Per-tile digit counts of one pass, digit-major: counts[d * tiles + t].
+// Bytes per key: sizeof(K) read.
+template <typename K>
+__global__ void __launch_bounds__(256) k_tile_counts(const K *__restrict__ keys, uint64_t n, int shift, uint32_t mask,
+                                                     uint32_t *__restrict__ counts, uint32_t tiles)
+{
+    constexpr int TILE = pass_tile<K>();
+    constexpr int PER_VEC = 16 / sizeof(K);
+    static_assert(TILE % (256 * PER_VEC) == 0, "tile is a whole number of 16-byte vectors per thread");
+    __shared__ uint32_t h[8][256];
+    const int tid = threadIdx.x, warp = tid >> 5;
+    for (int i = tid; i < 8 * 256; i += 256) (&h[0][0])[i] = 0;
+    __syncthreads();
+    const uint64_t base = (uint64_t)blockIdx.x * TILE;
+    if (base + TILE <= n && (reinterpret_cast<uintptr_t>(keys) & 15) == 0) {
+        const uint4 *k4 = reinterpret_cast<const uint4 *>(keys + base);
+#pragma unroll
+        for (int q = 0; q < TILE / (256 * PER_VEC); ++q) {
+            const uint4 v = k4[q * 256 + tid];
+            const K *kv = reinterpret_cast<const K *>(&v);
+#pragma unroll
+            for (int j = 0; j < PER_VEC; ++j) atomicAdd(&h[warp][(uint32_t)(kv[j] >> shift) & mask], 1u);
+        }
+    } else {
+        for (uint64_t i = base + tid; i < n && i < base + TILE; i += 256)
+            atomicAdd(&h[warp][(uint32_t)(keys[i] >> shift) & mask], 1u);
+    }
+    __syncthreads();
+    uint32_t c = 0;
+#pragma unroll
+    for (int w = 0; w < 8; ++w) c += h[w][tid];
+    counts[(uint64_t)tid * tiles + blockIdx.x] = c;
+}
+
+// One CTA per digit: offs[d * tiles + t] = bucket base of d + count of d in
+// tiles before t.
+__global__ void __launch_bounds__(1024) k_tile_offsets(const uint32_t *__restrict__ counts, uint32_t tiles,
+                                                       const uint32_t *__restrict__ bases, uint32_t *__restrict__ offs)
+{
+    __shared__ uint32_t wbuf[33];
+    const uint32_t d = blockIdx.x;
+    const uint32_t *c = counts + (uint64_t)d * tiles;
+    uint32_t *o = offs + (uint64_t)d * tiles;
+    uint32_t run = bases[d];
+    for (uint32_t b0 = 0; b0 < tiles; b0 += 1024 * 4) {
+        uint32_t v[4], s = 0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const uint32_t i = b0 + threadIdx.x * 4 + j;
+            v[j] = i < tiles ? c[i] : 0u;
+            s += v[j];
+        }
+        uint32_t total;
+        uint32_t a = run + block_exclusive_sum<uint32_t, 1024>(s, wbuf, total);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const uint32_t i = b0 + threadIdx.x * 4 + j;
+            if (i < tiles) o[i] = a;
+            a += v[j];
+        }
+        run += total;
+        __syncthreads();
+    }
+}
+
+// Digit pass of one tile (tile = blockIdx.x): stage, rank stably, re-order by
+// digit in shared memory, write each digit run to its global offset.
+template <typename K>
+__global__ void __launch_bounds__(PassShape<K>::kThreads, PassShape<K>::kMinBlocks)
+    k_radix_pass(const K *__restrict__ kin, const uint32_t *__restrict__ vin, K *__restrict__ kout,
+                 uint32_t *__restrict__ vout, uint64_t n, int shift, uint32_t mask,
+                 const uint32_t *__restrict__ offs, uint32_t tiles, uint32_t *err)
+{
+    constexpr int THREADS = PassShape<K>::kThreads;
+    constexpr int ITEMS = PassShape<K>::kItems;
     static_assert(THREADS == 256, "one thread per digit");
     constexpr int TILE = THREADS * ITEMS;
     constexpr int WARPS = THREADS / 32;
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    K *s_keys = reinterpret_cast<K *>(smem_raw);                                       // staged, then sorted
-    uint32_t *s_vin = reinterpret_cast<uint32_t *>(smem_raw + (size_t)TILE * sizeof(K));   // staged values
-    uint32_t *s_vout = s_vin + TILE;                                                    // sorted values
+    K *s_keys = reinterpret_cast<K *>(smem_raw);
+    uint32_t *s_vals = reinterpret_cast<uint32_t *>(smem_raw + (size_t)TILE * sizeof(K));
     __shared__ uint32_t s_whist[WARPS][256];
     __shared__ uint32_t s_lstart[256];
     __shared__ uint32_t s_gbase[256];
     __shared__ uint32_t s_scan[WARPS + 1];
     __shared__ __align__(8) uint64_t s_bar;
-    __shared__ uint32_t s_tile;
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-
-    if (tid == 0) {
-        const uint32_t t = atomicAdd(counter, 1u);
-        s_tile = t;
-        const uint64_t b = (uint64_t)t * TILE;
-        if (b + TILE <= n) {
-            mbar_init(&s_bar, 1);
-            mbar_arrive_expect_tx(&s_bar, TILE * (uint32_t)(sizeof(K) + sizeof(uint32_t)));
-            bulk_copy_g2s(s_keys, kin + b, TILE * sizeof(K), &s_bar);
-            bulk_copy_g2s(s_vin, vin + b, TILE * sizeof(uint32_t), &s_bar);
-        }
-    }
-    for (int i = tid; i < WARPS * 256; i += THREADS) (&s_whist[0][0])[i] = 0;
-    __syncthreads();
-
-    const uint32_t tile = s_tile;
+    const uint32_t tile = blockIdx.x;
     const uint64_t base = (uint64_t)tile * TILE;
     const uint32_t valid = (uint32_t)((n - base) < (uint64_t)TILE ? (n - base) : (uint64_t)TILE);
-    if (valid == TILE) {
+    const bool full = valid == TILE;
+    if (tid == 0 && full) {
+        mbar_init(&s_bar, 1);
+        mbar_arrive_expect_tx(&s_bar, TILE * (uint32_t)(sizeof(K) + sizeof(uint32_t)));
+        bulk_copy_g2s(s_keys, kin + base, TILE * sizeof(K), &s_bar);
+        bulk_copy_g2s(s_vals, vin + base, TILE * sizeof(uint32_t), &s_bar);
+    }
+    for (int i = tid; i < WARPS * 256; i += THREADS) (&s_whist[0][0])[i] = 0;
+    const uint32_t gofs = offs[(uint64_t)tid * tiles + tile];
+    __syncthreads();
+    if (full) {
         mbar_wait_bounded(&s_bar, 0, err);
     } else {
         for (uint32_t i = tid; i < valid; i += THREADS) {
             s_keys[i] = kin[base + i];
-            s_vin[i] = vin[base + i];
+            s_vals[i] = vin[base + i];
         }
         __syncthreads();
     }
 
-    // ---- rank keys inside each warp, in input order (stable)
+    // ---- rank inside each warp, in input order (stable).  Lanes with equal
+    // digits are found with eight ballots; the lowest such lane advances the
+    // warp's counter for that digit after every lane has read it.
     K kr[ITEMS];
+    uint32_t vr[ITEMS];
     uint16_t rk[ITEMS];
     const int wbase = warp * ITEMS * 32;
+    if (full) {
 #pragma unroll
-    for (int k = 0; k < ITEMS; ++k) {
-        const int idx = wbase + k * 32 + lane;
-        const bool ok = (uint32_t)idx < valid;
-        const K key = ok ? s_keys[idx] : K(0);
-        kr[k] = key;
-        const uint32_t d = ok ? (uint32_t)((key >> shift) & mask) : 256u;
-        const uint32_t peers = __match_any_sync(GSAIS_FULL_MASK, d);
-        const uint32_t before = __popc(peers & lanemask_lt());
-        // the lowest lane of each digit group bumps the warp's counter once;
-        // successive items of a warp hit the shared atomic unit in program
-        // order, so ranks stay in input order (stable)
-        uint32_t old = 0;
-        if (ok && before == 0) old = atomicAdd(&s_whist[warp][d], (uint32_t)__popc(peers));
-        old = __shfl_sync(GSAIS_FULL_MASK, old, __ffs(peers) - 1);
-        rk[k] = (uint16_t)(old + before);
+        for (int k = 0; k < ITEMS; ++k) {
+            const int idx = wbase + k * 32 + lane;
+            const K key = s_keys[idx];
+            kr[k] = key;
+            vr[k] = s_vals[idx];
+            const uint32_t d = (uint32_t)(key >> shift) & mask;
+            uint32_t peers = GSAIS_FULL_MASK;
+#pragma unroll
+            for (int b = 0; b < 8; ++b) {
+                const uint32_t bit = (d >> b) & 1u;
+                peers &= __ballot_sync(GSAIS_FULL_MASK, bit) ^ (bit - 1u);
+            }
+            const uint32_t before = __popc(peers & lanemask_lt());
+            const uint32_t old = s_whist[warp][d];
+            __syncwarp();
+            if (before == 0) s_whist[warp][d] = old + __popc(peers);
+            __syncwarp();
+            rk[k] = (uint16_t)(old + before);
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < ITEMS; ++k) {
+            const int idx = wbase + k * 32 + lane;
+            const bool ok = (uint32_t)idx < valid;
+            const K key = ok ? s_keys[idx] : K(0);
+            kr[k] = key;
+            vr[k] = ok ? s_vals[idx] : 0u;
+            const uint32_t d = ok ? ((uint32_t)(key >> shift) & mask) : 256u;
+            const uint32_t peers = __match_any_sync(GSAIS_FULL_MASK, d);
+            const uint32_t before = __popc(peers & lanemask_lt());
+            uint32_t old = 0;
+            if (ok && before == 0) old = atomicAdd(&s_whist[warp][d], (uint32_t)__popc(peers));
+            old = __shfl_sync(GSAIS_FULL_MASK, old, __ffs(peers) - 1);
+            rk[k] = (uint16_t)(old + before);
+        }
     }
     __syncthreads();
 
-    // ---- per-digit counts: exclusive over warps, then across tiles
+    // ---- per-digit counts: exclusive over warps, then over the tile
     const uint32_t digit = tid;
     uint32_t count = 0;
 #pragma unroll
@@ -200,38 +256,43 @@ __global__ void __launch_bounds__(OnesweepShape<K>::kThreads, OnesweepShape<K>::
         s_whist[w][digit] = count;
         count += c;
     }
-    const uint32_t excl = lookback_exclusive(status, tile, digit, count, err);
     uint32_t total;
     const uint32_t lstart = block_exclusive_sum<uint32_t, THREADS>(count, s_scan, total);
     s_lstart[digit] = lstart;
-    s_gbase[digit] = bases[digit] + excl - lstart;
+    s_gbase[digit] = gofs - lstart;
     __syncthreads();
 
-    // ---- reorder by digit inside the tile (keys from registers, values shared -> shared)
+    // ---- re-order by digit inside the tile (all staged reads are done)
 #pragma unroll
     for (int k = 0; k < ITEMS; ++k) {
         const int idx = wbase + k * 32 + lane;
-        if ((uint32_t)idx < valid) {
-            const uint32_t d = (uint32_t)((kr[k] >> shift) & mask);
+        if (full || (uint32_t)idx < valid) {
+            const uint32_t d = (uint32_t)(kr[k] >> shift) & mask;
             const uint32_t p = s_lstart[d] + s_whist[warp][d] + rk[k];
             s_keys[p] = kr[k];
-            s_vout[p] = s_vin[idx];
+            s_vals[p] = vr[k];
         }
     }
     __syncthreads();
 
     // ---- write digit runs to their global positions
-    for (uint32_t i = tid; i < valid; i += THREADS) {
-        const K key = s_keys[i];
-        const uint32_t d = (uint32_t)((key >> shift) & mask);
-        const uint32_t o = s_gbase[d] + i;
-        if ((uint64_t)o < n) {
-            kout[o] = key;
-            vout[o] = s_vout[i];
-        } else {
-            atomicOr(err, GSAIS_ERR_BOUNDS);
+    bool bad = false;
+#pragma unroll
+    for (int k = 0; k < ITEMS; ++k) {
+        const uint32_t i = k * THREADS + tid;
+        if (full || i < valid) {
+            const K key = s_keys[i];
+            const uint32_t d = (uint32_t)(key >> shift) & mask;
+            const uint32_t o = s_gbase[d] + i;
+            const bool ok = (uint64_t)o < n;
+            bad |= !ok;
+            if (ok) {
+                kout[o] = key;
+                vout[o] = s_vals[i];
+            }
         }
     }
+    if (bad) atomicOr(err, GSAIS_ERR_BOUNDS);
 }
 
 int sm_count()
@@ -243,15 +304,15 @@ int sm_count()
 }
 
 template <typename K>
-cudaError_t onesweep_attr()
+cudaError_t pass_attr()
 {
     // cudaFuncSetAttribute applies to the current device; remember per device
     static bool done[64] = {false};
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev >= 0 && dev < 64 && done[dev]) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(k_onesweep<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)onesweep_smem<K>());
+    cudaError_t e = cudaFuncSetAttribute(k_radix_pass<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)pass_smem<K>());
     if (e == cudaSuccess && dev >= 0 && dev < 64) done[dev] = true;
     return e;
 }
@@ -279,26 +340,32 @@ cudaError_t sort_impl(K *keys[2], uint32_t *vals[2], uint64_t n, int begin_bit, 
                              st)) != cudaSuccess)
         return e;
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
-    if ((e = onesweep_attr<K>()) != cudaSuccess) return e;
+    if ((e = pass_attr<K>()) != cudaSuccess) return e;
 
-    constexpr int TILE = OnesweepShape<K>::kThreads * OnesweepShape<K>::kItems;
+    constexpr int TILE = pass_tile<K>();
     const uint64_t tiles = (n + TILE - 1) / TILE;
+    if (tiles * 256 * 2 > (uint64_t)rs.status_words * 2) return cudaErrorInvalidValue;   // counts + offsets
+    uint32_t *counts = reinterpret_cast<uint32_t *>(rs.status);
+    uint32_t *offs = counts + tiles * 256;
     int cur = 0, ran = 0;
     for (int p = 0; p < passes; ++p) {
         bool trivial = false;
         for (int d = 0; d < 256; ++d)
             if (rs.h_hist[p * 256 + d] == n) { trivial = true; break; }
         if (trivial) continue;
-        if ((e = cudaMemsetAsync(rs.status, 0, (size_t)tiles * 256 * sizeof(uint64_t), st)) != cudaSuccess) return e;
-        if ((e = cudaMemsetAsync(rs.counters + p, 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
-        const int bits = end_bit - begin_bit - 8 * p < 8 ? end_bit - begin_bit - 8 * p : 8;
+        const int shift = begin_bit + 8 * p;
+        const int bits = end_bit - shift < 8 ? end_bit - shift : 8;
         const uint32_t mask = (1u << bits) - 1u;
+        cudaEvent_t ev0 = rs.prof ? rs.prof->begin(st) : nullptr;
+        GSAIS_COUNTED((k_tile_counts<K><<<(unsigned)tiles, 256, 0, st>>>(keys[cur], n, shift, mask, counts,
+                                                                          (uint32_t)tiles)));
+        GSAIS_COUNTED((k_tile_offsets<<<256, 1024, 0, st>>>(counts, (uint32_t)tiles, rs.bases + p * 256, offs)));
+        if (ev0) rs.prof->end(KK_TILE_COUNTS, ev0, st, n * sizeof(K));
         cudaEvent_t ev1 = rs.prof ? rs.prof->begin(st) : nullptr;
-        GSAIS_COUNTED((k_onesweep<K><<<(unsigned)tiles, OnesweepShape<K>::kThreads, onesweep_smem<K>(), st>>>(
-            keys[cur], vals[cur], keys[cur ^ 1], vals[cur ^ 1], n, begin_bit + 8 * p, mask, rs.bases + p * 256, rs.status,
-            rs.counters + p, d_err)));
+        GSAIS_COUNTED((k_radix_pass<K><<<(unsigned)tiles, PassShape<K>::kThreads, pass_smem<K>(), st>>>(
+            keys[cur], vals[cur], keys[cur ^ 1], vals[cur ^ 1], n, shift, mask, offs, (uint32_t)tiles, d_err)));
         // algorithmic bytes: every (key, value) pair read once and written once
-        if (ev1) rs.prof->end(KK_ONESWEEP, ev1, st, 2 * n * (sizeof(K) + sizeof(uint32_t)));
+        if (ev1) rs.prof->end(KK_RADIX_PASS, ev1, st, 2 * n * (sizeof(K) + sizeof(uint32_t)));
         cur ^= 1;
         ++ran;
     }
@@ -311,7 +378,10 @@ cudaError_t sort_impl(K *keys[2], uint32_t *vals[2], uint64_t n, int begin_bit, 
 
 size_t radix_status_words(uint64_t n)
 {
-    constexpr int TILE = 4096;   // the smallest onesweep tile of either key width
+    // per (tile, digit): one 32-bit count and one 32-bit offset; sized for the
+    // smallest pass tile of either key width
+    constexpr uint64_t TILE = (uint64_t)(pass_tile<uint64_t>() < pass_tile<uint32_t>() ? pass_tile<uint64_t>()
+                                                                                     : pass_tile<uint32_t>());
     const uint64_t tiles = (n + TILE - 1) / TILE;
     return (size_t)(tiles ? tiles : 1) * 256;
 }

@@ -410,7 +410,7 @@ __global__ void __launch_bounds__(kAssignThreads)
 
 // ------------------------------------------------- rounds: small / large
 // Groups of at most kSmallMax suffixes are split inside one warp (no global
-// sort); larger groups go through the onesweep radix sort keyed by
+// sort); larger groups go through the global radix sort keyed by
 // (dense large-group id, rank[i + h]).
 constexpr uint32_t kSmallMax = 32;      // <= this: split inside one warp
 constexpr uint32_t kMediumMax = 4096;   // <= this: sorted and split inside one CTA
@@ -907,7 +907,7 @@ size_t sort_workspace_bytes(uint64_t n, int symbytes)
     s += align_up((n + kSeedTile - 1) / kSeedTile * (kSeedTile / 2) + 16, A);   // packed codes (<= 4 bits each)
     s += 2 * align_up(8 * 256 * 4, A);             // radix hist + bases
     s += align_up(8 * 4, A);                       // radix counters
-    s += align_up(radix_status_words(n) * 8, A);   // look-back words
+    s += align_up(radix_status_words(n) * 8, A);   // radix tile counts + offsets
     return s;
 }
 
