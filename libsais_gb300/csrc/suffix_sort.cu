@@ -871,6 +871,130 @@ __global__ void __launch_bounds__(256) k_scatter_ranks(const uint32_t *__restric
     }
 }
 
+// ---- inverse permutation of the seed round: rank[pos[j]] = r[j] where pos
+// is a permutation of [0, N).  Two unstable partitions by the high bits of
+// pos (8 bits, then 8 more) leave every 2^shift2 consecutive positions in one
+// contiguous bucket of exactly that many entries; one CTA then scatters its
+// bucket into a shared-memory window and writes the window out coalesced.
+// Each level reads and writes 8 bytes per entry; the window pass reads 8 and
+// writes 4.  No random access reaches DRAM or L2.
+constexpr int kPermItems = 16;
+constexpr int kPermTile = 256 * kPermItems;
+
+__global__ void k_perm_cursors(uint32_t *__restrict__ cursor, uint32_t count, int shift, uint64_t N)
+{
+    const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d < count) {
+        const uint64_t s = (uint64_t)d << shift;
+        cursor[d] = (uint32_t)(s < N ? s : N);
+    }
+}
+
+// One partition level.  digit(p) = p >> shift; a tile's digits lie in
+// [lbase, lbase + RANGE) where lbase = (p0 >> lshift) << (lshift - shift) for
+// the tile's first position p0 (lshift = 0: lbase = 0).  Entries land at
+// cursor[digit]++ (order inside a digit is not kept: the scatter after the
+// last level does not need it).
+template <int RANGE>
+__global__ void __launch_bounds__(256) k_perm_partition(const uint32_t *__restrict__ in_pos,
+                                                        const uint32_t *__restrict__ in_r, uint64_t N, int shift,
+                                                        int lshift, uint32_t *__restrict__ cursor,
+                                                        uint32_t *__restrict__ out_pos, uint32_t *__restrict__ out_r,
+                                                        uint32_t *__restrict__ err)
+{
+    static_assert(RANGE % 256 == 0, "whole digits per thread");
+    constexpr int PER = RANGE / 256;
+    __shared__ uint32_t s_pos[kPermTile], s_r[kPermTile];
+    __shared__ uint32_t s_cnt[RANGE], s_lstart[RANGE], s_g[RANGE];
+    __shared__ uint32_t s_scan[9];
+    const int tid = threadIdx.x;
+    const uint64_t t0 = (uint64_t)blockIdx.x * kPermTile;
+    const uint32_t valid = (uint32_t)(N - t0 < (uint64_t)kPermTile ? N - t0 : (uint64_t)kPermTile);
+    for (int i = tid; i < RANGE; i += 256) s_cnt[i] = 0;
+    const uint32_t lbase = lshift ? ((in_pos[t0] >> lshift) << (lshift - shift)) : 0u;
+    __syncthreads();
+    uint32_t p[kPermItems], r[kPermItems];
+    uint16_t slot[kPermItems];
+    bool bad = false;
+#pragma unroll
+    for (int k = 0; k < kPermItems; ++k) {
+        const uint32_t i = k * 256 + tid;
+        p[k] = 0xFFFFFFFFu;
+        if (i < valid) {
+            p[k] = in_pos[t0 + i];
+            r[k] = in_r[t0 + i];
+            const uint32_t ld = (p[k] >> shift) - lbase;
+            if (ld < RANGE) {
+                slot[k] = (uint16_t)atomicAdd(&s_cnt[ld], 1u);
+            } else {
+                bad = true;
+                p[k] = 0xFFFFFFFFu;
+            }
+        }
+    }
+    __syncthreads();
+    // exclusive scan of the digit counts; reserve each digit's run globally
+    uint32_t c[PER], sum = 0;
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+        c[q] = s_cnt[tid * PER + q];
+        sum += c[q];
+    }
+    uint32_t total;
+    uint32_t a = block_exclusive_sum<uint32_t, 256>(sum, s_scan, total);
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+        const uint32_t ld = tid * PER + q;
+        s_lstart[ld] = a;
+        s_g[ld] = c[q] ? atomicAdd(&cursor[lbase + ld], c[q]) : 0u;
+        a += c[q];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kPermItems; ++k) {
+        if (p[k] != 0xFFFFFFFFu) {
+            const uint32_t ld = (p[k] >> shift) - lbase;
+            const uint32_t o = s_lstart[ld] + slot[k];
+            s_pos[o] = p[k];
+            s_r[o] = r[k];
+        }
+    }
+    __syncthreads();
+    const uint32_t kept = total;
+    for (uint32_t i = tid; i < kept; i += 256) {
+        const uint32_t q = s_pos[i];
+        const uint32_t ld = (q >> shift) - lbase;
+        const uint64_t o = (uint64_t)s_g[ld] + (i - s_lstart[ld]);
+        if (o < N) {
+            out_pos[o] = q;
+            out_r[o] = s_r[i];
+        } else {
+            bad = true;
+        }
+    }
+    if (bad) atomicOr(err, GSAIS_ERR_BOUNDS);
+}
+
+// Bucket b holds exactly the positions [b << shift, (b + 1) << shift).
+__global__ void __launch_bounds__(256) k_perm_window(const uint32_t *__restrict__ pos, const uint32_t *__restrict__ r,
+                                                     uint64_t N, int shift, uint32_t *__restrict__ rank,
+                                                     uint32_t *__restrict__ err)
+{
+    extern __shared__ uint32_t s_win[];
+    const uint64_t w0 = (uint64_t)blockIdx.x << shift;
+    const uint32_t W = (uint32_t)(N - w0 < (1ull << shift) ? N - w0 : (1ull << shift));
+    bool bad = false;
+    for (uint32_t i = threadIdx.x; i < W; i += 256) {
+        const uint32_t q = pos[w0 + i];
+        const uint64_t x = (uint64_t)q - w0;
+        if (q >= w0 && x < W) s_win[x] = r[w0 + i];
+        else bad = true;
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < W; i += 256) rank[w0 + i] = s_win[i];
+    if (bad) atomicOr(err, GSAIS_ERR_BOUNDS);
+}
+
 // GSA validity: T[n-1] == 0, T[0] != 0, no two adjacent zeros.
 template <typename Sym>
 __global__ void k_gsa_check(const Sym *__restrict__ T, uint64_t n, uint32_t *__restrict__ flag)
@@ -989,19 +1113,44 @@ static cudaError_t run_assign(const TileArgs &a, SortWorkspace &ws, uint32_t *ou
 }
 
 // Seed round: for a large rank domain the new ranks are written by list
-// position, partitioned by the top 8 bits of the suffix position and then
-// scattered inside L2-resident windows (instead of one random 4-byte write
-// per suffix into a rank array larger than L2).
+// position and then moved to text order without random writes into a rank
+// array larger than L2.  When the list is a permutation of [0, nr) the
+// three-level partition + shared-memory window scatter is used; otherwise
+// (gapped batch coordinates) a stable radix partition by the top 8 position
+// bits followed by a scatter inside L2-resident windows.
 static bool use_two_level_ranks(uint64_t nr) { return nr >= (1ull << 23); }
 
 static cudaError_t scatter_seed_ranks(SortWorkspace &ws, uint32_t *sorted_pos, uint32_t *ranks, uint64_t N,
                                       uint64_t nr, uint32_t *d_err, cudaStream_t st)
 {
-    const int b = gsais_bits_for(nr);
+    cudaError_t e;
+    const int b = gsais_bits_for(nr - 1);
+    const int shift1 = b - 8, shift2 = b - 16;
+    if (N == nr && b >= 23 && shift2 <= 15) {
+        // level 1: by bits [shift1, b) into lvals; level 2: by bits [shift2, b) back
+        uint32_t *cur = reinterpret_cast<uint32_t *>(ws.radix.status);
+        const uint64_t tiles = (N + kPermTile - 1) / kPermTile;
+        const uint32_t n1 = (uint32_t)(((N - 1) >> shift1) + 1), n2 = (uint32_t)(((N - 1) >> shift2) + 1);
+        if ((uint64_t)n1 + n2 > ws.radix.status_words * 2) return cudaErrorInvalidValue;
+        GSAIS_COUNTED((k_perm_cursors<<<(n1 + 255) / 256, 256, 0, st>>>(cur, n1, shift1, N)));
+        GSAIS_COUNTED((k_perm_cursors<<<(n2 + 255) / 256, 256, 0, st>>>(cur + n1, n2, shift2, N)));
+        GSAIS_COUNTED((k_perm_partition<256><<<(unsigned)tiles, 256, 0, st>>>(sorted_pos, ranks, N, shift1, 0, cur,
+                                                                              ws.lvals[0], ws.lvals[1], d_err)));
+        GSAIS_COUNTED((k_perm_partition<512><<<(unsigned)tiles, 256, 0, st>>>(
+            ws.lvals[0], ws.lvals[1], N, shift2, shift1, cur + n1, sorted_pos, ranks, d_err)));
+        const size_t smem = (size_t)4 << shift2;
+        if (smem > 48 * 1024 &&
+            (e = cudaFuncSetAttribute(k_perm_window, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+                cudaSuccess)
+            return e;
+        GSAIS_COUNTED((k_perm_window<<<n2, 256, smem, st>>>(sorted_pos, ranks, N, shift2, ws.rank, d_err)));
+        return cudaGetLastError();
+    }
+    const int bb = gsais_bits_for(nr);
     uint32_t *kk[2] = {sorted_pos, ws.lvals[0]};
     uint32_t *vv[2] = {ranks, ws.lvals[1]};
     int which = 0;
-    cudaError_t e = radix_partition32(kk, vv, N, b > 8 ? b - 8 : 0, b, ws.radix, d_err, st, &which);
+    e = radix_partition32(kk, vv, N, bb > 8 ? bb - 8 : 0, bb, ws.radix, d_err, st, &which);
     if (e != cudaSuccess) return e;
     GSAIS_COUNTED((k_scatter_ranks<<<stream_grid(N, 256), 256, 0, st>>>(kk[which], vv[which], N, nr, ws.rank,
                                                                         d_err)));
