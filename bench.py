@@ -545,7 +545,8 @@ def main():
                        "outputs": "SA + BWT + primary index", "l2": "inputs larger than L2 (text and SA > 129 MB)",
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "rounds": stats["rounds"], "seed_symbols": stats["seed_symbols"],
-                       "radix_passes": stats["radix_passes"]},
+                       "radix_passes": stats["radix_passes"], "active_total": stats["active_total"],
+                       "pairs_direct": stats["pairs_direct"], "large_total": stats["large_total"]},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
             "kernels": kernels, "clocks": clocks,
         }

@@ -131,6 +131,8 @@ extern "C" {
         int32_t radix_passes;    /* digit passes actually run (all sorts) */
         int64_t active_total;    /* sum over rounds of still-unsorted suffixes */
         int64_t workspace_bytes; /* device workspace held by the context */
+        int64_t large_total;     /* sum over rounds of suffixes sorted by the global radix path */
+        int64_t pairs_direct;    /* tied suffix pairs ordered by direct comparison of their text */
     } gsais_stats;
 
     int32_t gsais_last_stats(void * ctx, gsais_stats * out);

@@ -584,6 +584,8 @@ int32_t gsais_last_stats(void *ctx, gsais_stats *out)
     out->radix_passes = c->stats.radix_passes;
     out->active_total = (int64_t)c->stats.active_total;
     out->workspace_bytes = (int64_t)c->arena_bytes;
+    out->large_total = (int64_t)c->stats.large_total;
+    out->pairs_direct = (int64_t)c->stats.pairs_direct;
     return 0;
 }
 
@@ -612,8 +614,9 @@ int32_t gsais_profile_read(void *ctx, gsais_kernel_profile *out, int32_t max_kin
     gsais_ctx *c = resolve(ctx);
     if (!c || !out) return -1;
     std::lock_guard<std::mutex> lock(c->mu);
-    static const char *names[KK_COUNT] = {"radix_pass", "tile_counts",  "upsweep", "seed",
-                                          "round_keys", "tile_summary", "assign",  "small_groups"};
+    static const char *names[KK_COUNT] = {"radix_pass",   "tile_counts", "upsweep",      "seed",
+                                          "round_keys",   "tile_summary", "assign",      "small_groups",
+                                          "pair_compare"};
     int k = 0;
     for (; k < KK_COUNT && k < max_kinds; ++k) {
         out[k].name = names[k];

@@ -16,7 +16,7 @@ extern std::atomic<uint64_t> g_launches;
 // Optional per-kernel timing: CUDA events recorded on the launching stream
 // around each launch of the instrumented kernels, resolved after the stream
 // synchronises.  `bytes` is the algorithmic traffic of the launch.
-enum KernelKind { KK_RADIX_PASS = 0, KK_TILE_COUNTS, KK_UPSWEEP, KK_SEED, KK_ROUND_KEYS, KK_SUMMARY, KK_ASSIGN, KK_SMALL, KK_COUNT };
+enum KernelKind { KK_RADIX_PASS = 0, KK_TILE_COUNTS, KK_UPSWEEP, KK_SEED, KK_ROUND_KEYS, KK_SUMMARY, KK_ASSIGN, KK_SMALL, KK_PAIRS, KK_COUNT };
 
 struct KernelProfiler {
     bool enabled = false;
@@ -75,6 +75,7 @@ struct SortStats {
     int seed_bits = 0;             // bits per symbol code
     uint64_t active_total = 0;     // sum of active suffixes over rounds
     uint64_t large_total = 0;      // sum over rounds of suffixes in groups sorted by the radix path
+    uint64_t pairs_direct = 0;     // tied pairs ordered by direct comparison
     int radix_passes = 0;          // non-trivial digit passes over all sorts
 };
 

@@ -606,7 +606,9 @@ __global__ void __launch_bounds__(256) k_small_groups(const uint32_t *__restrict
                                                       uint32_t *__restrict__ out_i, uint32_t *__restrict__ out_pos,
                                                       uint32_t *__restrict__ out_gid,
                                                       uint32_t *__restrict__ gstart_out,
-                                                      unsigned long long *__restrict__ counter)
+                                                      unsigned long long *__restrict__ counter,
+                                                      uint32_t *__restrict__ pairs,
+                                                      unsigned long long *__restrict__ pair_count)
 {
     constexpr int WARPS = 8;
     __shared__ uint32_t s_we[WARPS], s_wg[WARPS];
@@ -704,6 +706,34 @@ __global__ void __launch_bounds__(256) k_small_groups(const uint32_t *__restrict
         } else {
             surv[e] = true;
             hsub[e] = before[e] == lt[e];
+        }
+    }
+    // A tied pair (a group of exactly two members with equal r2) leaves the
+    // doubling: its members go to sa[P], sa[P + 1] in either order and the
+    // slot P to the pair list, to be ordered by comparing the two suffixes
+    // directly (k_pair_compare).  The first member of an owned group always
+    // sits at offset gs < 32, i.e. in the first half of the window.
+    if (pairs) {
+        const uint32_t nx0 = __shfl_sync(GSAIS_FULL_MASK, i0, (lane + 1) & 31);
+        const uint32_t nx1 = __shfl_sync(GSAIS_FULL_MASK, i1, (lane + 1) & 31);
+        bool lead = false;
+        for (int e = 0; e < 2; ++e) {
+            if (own[e] && gend[e] - gs[e] == 2 && eq[e] == 2) {
+                surv[e] = false;
+                hsub[e] = false;
+                if (e == 0 && gs[0] == lane) lead = true;
+            }
+        }
+        const uint32_t m = __ballot_sync(GSAIS_FULL_MASK, lead);
+        if (m) {
+            uint32_t b = 0;
+            if (lane == 0) b = (uint32_t)atomicAdd(pair_count, (unsigned long long)__popc(m));
+            b = __shfl_sync(GSAIS_FULL_MASK, b, 0);
+            if (lead) {
+                sa[P[0]] = i0;
+                sa[P[0] + 1] = lane < 31 ? nx0 : nx1;
+                pairs[b + __popc(m & lanemask_lt())] = P[0];
+            }
         }
     }
     const uint64_t S = (uint64_t)__ballot_sync(GSAIS_FULL_MASK, surv[0]) |
@@ -871,6 +901,166 @@ __global__ void __launch_bounds__(256) k_scatter_ranks(const uint32_t *__restric
     }
 }
 
+
+// Packed dense codes of the text: PB bits per symbol, symbol j at bits
+// PB * (j % (64 / PB)) of 64-bit word j / (64 / PB).
+struct PackedWords {
+    const uint64_t *w;
+    uint64_t nwords;   // readable words (indexes are clamped to the last one)
+};
+
+
+// Orders the tied pairs found by k_small_groups by comparing the two
+// suffixes directly on the packed codes, from offset `skip` (a prefix both
+// are known to share) on: the first differing code decides, and when one
+// suffix ends inside the common part the shorter one is smaller (the
+// implicit sentinel of libsais, src/libsais.c:7018).  One lane per pair; a
+// step loads one aligned 16-byte block per side, keeps the previous block,
+// and aligns four 32-bit words (128 / PB symbols) with word selects and
+// funnel shifts.  A lane whose pair is done idles until a quarter of its
+// warp is idle; those lanes then take their next pairs together from a
+// global cursor, so the refill code runs rarely and work stays balanced.  A
+// pair still equal after `limit` more symbols goes back to the active list
+// as a two-member group.
+struct PairSide {
+    uint4 prev;      // last block loaded
+    uint32_t q;      // next block to load
+    uint32_t d;      // word offset of the window inside the block pair
+    int sh;          // bit offset of the window inside its first word
+};
+
+__device__ __forceinline__ void pair_window(const uint4 *__restrict__ W4, uint32_t last4, PairSide &s,
+                                            uint32_t out[4])
+{
+    const uint4 cur = W4[s.q < last4 ? s.q : last4];
+    ++s.q;
+    const uint32_t w[8] = {s.prev.x, s.prev.y, s.prev.z, s.prev.w, cur.x, cur.y, cur.z, cur.w};
+    uint32_t u[6], e[5];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) u[i] = (s.d & 2) ? w[i + 2] : w[i];
+#pragma unroll
+    for (int i = 0; i < 5; ++i) e[i] = (s.d & 1) ? u[i + 1] : u[i];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) out[i] = __funnelshift_r(e[i], e[i + 1], s.sh);
+    s.prev = cur;
+}
+
+template <int PB>
+__global__ void __launch_bounds__(256) k_pair_compare(const uint32_t *__restrict__ pairs,
+                                                      const unsigned long long *__restrict__ pair_count,
+                                                      unsigned long long *__restrict__ cursor, PackedWords pw,
+                                                      uint64_t n, uint64_t skip, uint32_t limit,
+                                                      uint32_t *__restrict__ sa, uint32_t *__restrict__ rank,
+                                                      uint32_t *__restrict__ out_i, uint32_t *__restrict__ out_pos,
+                                                      uint32_t *__restrict__ out_gid,
+                                                      uint32_t *__restrict__ gstart_out,
+                                                      unsigned long long *__restrict__ counter,
+                                                      uint32_t *__restrict__ err)
+{
+    constexpr uint32_t SPW = 32 / PB;   // symbols per 32-bit word
+    constexpr uint32_t STEP = 4 * SPW;
+    constexpr uint32_t CM = (1u << PB) - 1;
+    const uint64_t count = *pair_count;
+    const uint4 *W4 = reinterpret_cast<const uint4 *>(pw.w);
+    const uint32_t last4 = (uint32_t)(pw.nwords / 2 - 1);
+    const int lane = threadIdx.x & 31;
+
+    bool live = false, finished = false, at_end = false;
+    uint32_t P = 0, a = 0, b = 0, rem = 0;   // rem: symbols left before `stop`
+    PairSide A{}, B{};
+    auto init_side = [&](PairSide &s, uint64_t x) {
+        const uint64_t q = x / SPW;   // word holding symbol x
+        s.d = (uint32_t)(q & 3);
+        s.sh = (int)(x % SPW) * PB;
+        const uint32_t q4 = (uint32_t)(q >> 2);
+        s.prev = W4[q4 < last4 ? q4 : last4];
+        s.q = q4 + 1;
+    };
+    while (true) {
+        const uint32_t busy = __ballot_sync(GSAIS_FULL_MASK, live);
+        const uint32_t needy = __ballot_sync(GSAIS_FULL_MASK, !live && !finished);
+        if (busy == 0 && needy == 0) break;
+        if (needy && (busy == 0 || __popc(needy) >= 8)) {
+            unsigned long long base = 0;
+            if (lane == __ffs(needy) - 1) base = atomicAdd(cursor, (unsigned long long)__popc(needy));
+            base = __shfl_sync(GSAIS_FULL_MASK, base, __ffs(needy) - 1);
+            if (!live && !finished) {
+                const uint64_t jj = base + __popc(needy & lanemask_lt());
+                if (jj >= count) {
+                    finished = true;
+                } else {
+                    P = pairs[jj];
+                    const bool okp = (uint64_t)P + 1 < n;
+                    a = okp ? sa[P] : 0u;
+                    b = okp ? sa[P + 1] : 0u;
+                    if (okp && a < n && b < n && a != b) {
+                        const uint64_t la = n - a, lb = n - b;
+                        const uint64_t minlen = la < lb ? la : lb;
+                        const uint64_t stop = minlen < skip + limit ? minlen : skip + limit;
+                        at_end = stop == minlen;
+                        rem = (uint32_t)(stop - skip);
+                        init_side(A, a + skip);
+                        init_side(B, b + skip);
+                        live = true;
+                    } else {
+                        atomicOr(err, GSAIS_ERR_BOUNDS);
+                    }
+                }
+            }
+            continue;
+        }
+        if (!live) continue;
+        int res = 0;   // -1: a smaller, 1: b smaller, 2: equal up to `limit`, 0: go on
+        const int end_res = at_end ? ((n - a) < (n - b) ? -1 : 1) : 2;
+        if (rem == 0) {
+            res = end_res;
+        } else {
+            uint32_t va[4], vb[4];
+            pair_window(W4, last4, A, va);
+            pair_window(W4, last4, B, vb);
+            uint32_t x = 0, wa = 0, wb = 0, wi = 4;
+#pragma unroll
+            for (int i = 3; i >= 0; --i) {
+                const uint32_t xi = va[i] ^ vb[i];
+                if (xi) { x = xi; wa = va[i]; wb = vb[i]; wi = i; }
+            }
+            if (x) {
+                const uint32_t bit = (uint32_t)__ffs(x) - 1;
+                const uint32_t sym = wi * SPW + bit / PB;
+                if (sym < rem) {
+                    const int f = (int)(bit / PB * PB);
+                    res = ((wa >> f) & CM) < ((wb >> f) & CM) ? -1 : 1;
+                } else {
+                    res = end_res;
+                }
+            } else if (rem <= STEP) {
+                res = end_res;
+            } else {
+                rem -= STEP;
+            }
+        }
+        if (res == 0) continue;
+        if (res != 2) {
+            const uint32_t lo = res < 0 ? a : b, hi = res < 0 ? b : a;
+            sa[P] = lo;
+            sa[P + 1] = hi;
+            rank[lo] = P + 1;
+            rank[hi] = P + 2;
+        } else {
+            const unsigned long long r = atomicAdd(counter, (1ull << 32) | 2ull);
+            const uint32_t cc = (uint32_t)r, g = (uint32_t)(r >> 32);
+            out_i[cc] = a;
+            out_i[cc + 1] = b;
+            out_pos[cc] = P;
+            out_pos[cc + 1] = P + 1;
+            out_gid[cc] = g;
+            out_gid[cc + 1] = g;
+            gstart_out[g] = cc;
+        }
+        live = false;
+    }
+}
+
 // ---- inverse permutation of the seed round: rank[pos[j]] = r[j] where pos
 // is a permutation of [0, N).  Two unstable partitions by the high bits of
 // pos (8 bits, then 8 more) leave every 2^shift2 consecutive positions in one
@@ -1023,7 +1213,7 @@ size_t sort_workspace_bytes(uint64_t n, int symbytes)
     s += 2 * align_up(n * 4, A);                   // gid
     s += 4 * align_up((n / 2 + 2) * 4, A);         // gstart x2, lid, loff (at most n/2 groups are active)
     s += 3 * align_up(n * 4, A);                   // large list: values x2, slots
-    s += align_up(4 * 8, A);                       // round counters
+    s += align_up(8 * 8, A);                       // round counters
     s += 2 * align_up(tiles * 12, A);              // tile info + carry
     s += align_up(16 * 4, A);                      // totals
     s += align_up(65536 * 4, A);                   // hist
@@ -1054,7 +1244,7 @@ void sort_workspace_carve(SortWorkspace &ws, void *base, uint64_t n, int symbyte
     ws.loff = reinterpret_cast<uint32_t *>(take((n / 2 + 2) * 4));
     for (int i = 0; i < 2; ++i) ws.lvals[i] = reinterpret_cast<uint32_t *>(take(n * 4));
     ws.lpos = reinterpret_cast<uint32_t *>(take(n * 4));
-    ws.counters = reinterpret_cast<unsigned long long *>(take(4 * 8));
+    ws.counters = reinterpret_cast<unsigned long long *>(take(8 * 8));
     ws.tile_info = reinterpret_cast<uint32_t *>(take(tiles * 12));
     ws.tile_carry = reinterpret_cast<uint32_t *>(take(tiles * 12));
     ws.totals = reinterpret_cast<uint32_t *>(take(16 * 4));
@@ -1159,8 +1349,17 @@ static cudaError_t scatter_seed_ranks(SortWorkspace &ws, uint32_t *sorted_pos, u
 
 // Doubling rounds over the kept groups of the seed round until every suffix
 // is final.  nr = length of the rank domain (rank[nr] is the sentinel).
+// Tied pairs are ordered by direct comparison when the packed codes of the
+// text are available (single text, at most 16 symbols).
+struct PairSource {
+    int pack_bits = 0;   // 0: no direct comparison
+    PackedWords words{nullptr, 0};
+    uint64_t n = 0;
+};
+constexpr uint32_t kPairLimit = 1u << 16;   // symbols compared beyond the shared prefix
+
 static cudaError_t run_rounds(SortWorkspace &ws, uint64_t nr, int K, uint32_t kept, uint32_t groups, int av, int pg,
-                              uint32_t *d_err, cudaStream_t st, SortStats &S)
+                              uint32_t *d_err, cudaStream_t st, SortStats &S, const PairSource &ps)
 {
     cudaError_t e;
     int ran = 0;
@@ -1181,8 +1380,10 @@ static cudaError_t run_rounds(SortWorkspace &ws, uint64_t nr, int K, uint32_t ke
         uint32_t *act_i = ws.vals[av], *act_pos = ws.pos[pg], *act_gid = ws.gid[pg];
         uint32_t *out_i = ws.vals[av ^ 1], *out_pos = ws.pos[pg ^ 1], *out_gid = ws.gid[pg ^ 1];
         uint32_t *r2 = reinterpret_cast<uint32_t *>(ws.keys[1]);   // consumed before the large sort reuses keys[1]
-        // counters: [0] small+medium output, [1] large list, [2] medium groups
-        if ((e = cudaMemsetAsync(ws.counters, 0, 3 * sizeof(unsigned long long), st)) != cudaSuccess) return e;
+        // counters: [0] small+medium output, [1] large list, [2] medium groups, [3] tied pairs,
+        // [4] next tied pair to compare
+        if ((e = cudaMemsetAsync(ws.counters, 0, 5 * sizeof(unsigned long long), st)) != cudaSuccess) return e;
+        uint32_t *pairs = ps.pack_bits ? r2 + N : nullptr;   // after r2 in keys[1]: N/2 slots at most
         if ((e = cudaMemsetAsync(ws.radix.hist, 0, (size_t)passes * 256 * 4, st)) != cudaSuccess) return e;
         uint32_t *mlist = ws.lvals[1];   // free until the large sort's first pass
         GSAIS_COUNTED((k_classify<<<stream_grid(G, 256), 256, 0, st>>>(ws.gstart[pg], G, N, ws.lid, ws.loff,
@@ -1195,17 +1396,31 @@ static cudaError_t run_rounds(SortWorkspace &ws, uint64_t nr, int K, uint32_t ke
         cudaEvent_t ev_sm = ws.radix.prof ? ws.radix.prof->begin(st) : nullptr;
         GSAIS_COUNTED((k_small_groups<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(
             act_i, act_pos, act_gid, r2, N, ws.rank, ws.sa, out_i, out_pos, out_gid, ws.gstart[pg ^ 1],
-            ws.counters)));
+            ws.counters, pairs, ws.counters + 3)));
         if (ev_sm) ws.radix.prof->end(KK_SMALL, ev_sm, st, N * 32);
         GSAIS_COUNTED((k_medium_groups<<<stream_grid(G * 256, 256), 256, 0, st>>>(
             mlist, ws.counters + 2, ws.gstart[pg], G, N, act_i, act_pos, r2, ws.rank, ws.sa, out_i, out_pos, out_gid,
             ws.gstart[pg ^ 1], ws.counters)));
-        if ((e = cudaMemcpyAsync(ws.h_small, ws.counters, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+        if (pairs) {
+            cudaEvent_t ev_pc = ws.radix.prof ? ws.radix.prof->begin(st) : nullptr;
+            // members share 2h symbols: h by their group, h more by equal r2
+            if (ps.pack_bits == 2)
+                GSAIS_COUNTED((k_pair_compare<2><<<stream_grid(N / 2, 256), 256, 0, st>>>(
+                    pairs, ws.counters + 3, ws.counters + 4, ps.words, ps.n, 2 * h, kPairLimit, ws.sa, ws.rank, out_i,
+                    out_pos, out_gid, ws.gstart[pg ^ 1], ws.counters, d_err)));
+            else
+                GSAIS_COUNTED((k_pair_compare<4><<<stream_grid(N / 2, 256), 256, 0, st>>>(
+                    pairs, ws.counters + 3, ws.counters + 4, ps.words, ps.n, 2 * h, kPairLimit, ws.sa, ws.rank, out_i,
+                    out_pos, out_gid, ws.gstart[pg ^ 1], ws.counters, d_err)));
+            if (ev_pc) ws.radix.prof->end(KK_PAIRS, ev_pc, st, 0);
+        }
+        if ((e = cudaMemcpyAsync(ws.h_small, ws.counters, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                                  st)) != cudaSuccess)
             return e;
         if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
         const unsigned long long small_tot = reinterpret_cast<unsigned long long *>(ws.h_small)[0];
         const unsigned long long large_tot = reinterpret_cast<unsigned long long *>(ws.h_small)[1];
+        S.pairs_direct += reinterpret_cast<unsigned long long *>(ws.h_small)[3];
         const uint64_t NL = (uint32_t)large_tot;
         if (NL == 0) {
             kept = (uint32_t)small_tot;
@@ -1341,7 +1556,14 @@ cudaError_t suffix_sort(const void *d_T, int symbytes, uint64_t n, bool gsa, Sor
     if (a.rank_out && (e = scatter_seed_ranks(ws, ws.vals[w], a.rank_out, n, n, d_err, st)) != cudaSuccess) return e;
 
     // ---- doubling rounds over the active suffixes
-    if ((e = run_rounds(ws, n, K, kept, groups, av, pg, d_err, st, S)) != cudaSuccess) return e;
+    PairSource ps;
+    if (ws.pack_bits == 2 || ws.pack_bits == 4) {
+        ps.pack_bits = ws.pack_bits;
+        ps.words.w = reinterpret_cast<const uint64_t *>(ws.packed);
+        ps.words.nwords = (n + kSeedTile - 1) / kSeedTile * (uint64_t)kSeedTile * ws.pack_bits / 64;
+        ps.n = n;
+    }
+    if ((e = run_rounds(ws, n, K, kept, groups, av, pg, d_err, st, S, ps)) != cudaSuccess) return e;
     uint32_t herr = 0;
     if ((e = cudaMemcpyAsync(ws.h_small, d_err, 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
@@ -1450,7 +1672,7 @@ cudaError_t batch_suffix_sort(const uint8_t *d_T, uint64_t n, const uint64_t *d_
         return e;
     if (a.rank_out && (e = scatter_seed_ranks(ws, ws.vals[w], a.rank_out, n, nr, d_err, st)) != cudaSuccess)
         return e;
-    if ((e = run_rounds(ws, nr, K, kept, groups, av, pg, d_err, st, S)) != cudaSuccess) return e;
+    if ((e = run_rounds(ws, nr, K, kept, groups, av, pg, d_err, st, S, PairSource())) != cudaSuccess) return e;
     if ((e = cudaMemcpyAsync(ws.h_small, d_err, 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
     if (ws.radix.prof) ws.radix.prof->flush();

@@ -121,6 +121,34 @@ def test_runs_and_tandem_repeats(oracle):
         check_all(oracle, t, plcp=trial % 4 == 0, r=0)
 
 
+def test_copied_segments_pairs(oracle):
+    """Exact and near-exact copies: tied suffix pairs ordered by direct text
+    comparison, including copies that run to the end of the text (one suffix
+    ends inside the common part), copies longer than the comparison limit
+    (the pair goes back to doubling), 4-bit packed codes (8 and 16 symbols,
+    8- and 16-bit texts) and 2-bit codes."""
+    rng = np.random.default_rng(17)
+    cases = []
+    for sigma, dtype in ((4, np.uint8), (8, np.uint8), (16, np.uint16), (3, np.uint16)):
+        n = int(rng.integers(150_000, 300_000))
+        t = rng.integers(0, sigma, n).astype(dtype) + (65 if dtype == np.uint8 else 1000)
+        L = int(rng.integers(2_000, 20_000))
+        a = int(rng.integers(0, n // 3))
+        t[n - L:] = t[a:a + L]                             # copy reaching the end of the text
+        b = int(rng.integers(n // 3, n // 2))
+        t[b:b + 5_000] = t[a + 100:a + 5_100]               # copy inside the text
+        t[b + int(rng.integers(10, 4_000))] = t[0]          # one substitution in it
+        cases.append(t)
+    n = 200_000
+    t = (rng.integers(0, 4, n) + 65).astype(np.uint8)
+    t[110_000:190_000] = t[10_000:90_000]                  # 80 000-symbol exact copy: past the limit
+    cases.append(t)
+    for t in cases:
+        check_all(oracle, t, plcp=False, r=0)
+        st = G.last_stats()
+        assert st["pairs_direct"] > 0, st
+
+
 def random_gsa(rng, count, maxlen, k):
     parts = []
     for _ in range(count):
