@@ -6,7 +6,8 @@ computed on an NVIDIA GB300 GPU.  Same signatures and return codes; symbols
 are uint16_t and freq has 65536 entries.  `threads` and `fs` are validated
 and otherwise ignored; `A` is not written.
 
-Not provided here: libsais16_int and the inverse-BWT family.
+libsais16_int takes an integer string with symbols in [0, k) (-1 otherwise).
+The inverse BWT ignores `freq` and does not write `A`.
 
 --*/
 
@@ -47,6 +48,10 @@ extern "C" {
     LIBSAIS16_API int32_t libsais16_omp(const uint16_t * T, int32_t * SA, int32_t n, int32_t fs, int32_t * freq, int32_t threads);
     /* (ref include/libsais16.h:156) */
     LIBSAIS16_API int32_t libsais16_gsa_omp(const uint16_t * T, int32_t * SA, int32_t n, int32_t fs, int32_t * freq, int32_t threads);
+    /* (ref include/libsais16.h:107) */
+    LIBSAIS16_API int32_t libsais16_int(int32_t * T, int32_t * SA, int32_t n, int32_t k, int32_t fs);
+    /* (ref include/libsais16.h:169) */
+    LIBSAIS16_API int32_t libsais16_int_omp(int32_t * T, int32_t * SA, int32_t n, int32_t k, int32_t fs, int32_t threads);
 
     /* (ref include/libsais16.h:182) */
     LIBSAIS16_API int32_t libsais16_bwt(const uint16_t * T, uint16_t * U, int32_t * A, int32_t n, int32_t fs, int32_t * freq);
@@ -60,6 +65,25 @@ extern "C" {
     LIBSAIS16_API int32_t libsais16_bwt_omp(const uint16_t * T, uint16_t * U, int32_t * A, int32_t n, int32_t fs, int32_t * freq, int32_t threads);
     /* (ref include/libsais16.h:253) */
     LIBSAIS16_API int32_t libsais16_bwt_aux_omp(const uint16_t * T, uint16_t * U, int32_t * A, int32_t n, int32_t fs, int32_t * freq, int32_t r, int32_t * I, int32_t threads);
+
+    /* (ref include/libsais16.h:261) */
+    LIBSAIS16_API void * libsais16_unbwt_create_ctx(void);
+    /* (ref include/libsais16.h:270) */
+    LIBSAIS16_API void * libsais16_unbwt_create_ctx_omp(int32_t threads);
+    /* (ref include/libsais16.h:277) */
+    LIBSAIS16_API void libsais16_unbwt_free_ctx(void * ctx);
+    /* (ref include/libsais16.h:289) */
+    LIBSAIS16_API int32_t libsais16_unbwt(const uint16_t * T, uint16_t * U, int32_t * A, int32_t n, const int32_t * freq, int32_t i);
+    /* (ref include/libsais16.h:302) */
+    LIBSAIS16_API int32_t libsais16_unbwt_ctx(const void * ctx, const uint16_t * T, uint16_t * U, int32_t * A, int32_t n, const int32_t * freq, int32_t i);
+    /* (ref include/libsais16.h:315) */
+    LIBSAIS16_API int32_t libsais16_unbwt_aux(const uint16_t * T, uint16_t * U, int32_t * A, int32_t n, const int32_t * freq, int32_t r, const int32_t * I);
+    /* (ref include/libsais16.h:329) */
+    LIBSAIS16_API int32_t libsais16_unbwt_aux_ctx(const void * ctx, const uint16_t * T, uint16_t * U, int32_t * A, int32_t n, const int32_t * freq, int32_t r, const int32_t * I);
+    /* (ref include/libsais16.h:343) */
+    LIBSAIS16_API int32_t libsais16_unbwt_omp(const uint16_t * T, uint16_t * U, int32_t * A, int32_t n, const int32_t * freq, int32_t i, int32_t threads);
+    /* (ref include/libsais16.h:357) */
+    LIBSAIS16_API int32_t libsais16_unbwt_aux_omp(const uint16_t * T, uint16_t * U, int32_t * A, int32_t n, const int32_t * freq, int32_t r, const int32_t * I, int32_t threads);
 
     /* (ref include/libsais16.h:368) */
     LIBSAIS16_API int32_t libsais16_plcp(const uint16_t * T, const int32_t * SA, int32_t * PLCP, int32_t n);

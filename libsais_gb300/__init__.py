@@ -25,6 +25,9 @@ __all__ = [
     "libsais64_plcp_gsa", "libsais64_lcp", "libsais16", "libsais16_gsa", "libsais16_bwt", "libsais16_bwt_aux",
     "libsais16_plcp", "libsais16_plcp_gsa", "libsais16_lcp", "sa_bwt", "sa_device", "sa_bwt_device",
     "plcp_device", "lcp_device", "last_stats", "set_seed_key_bits", "EXPORTED_SYMBOLS",
+    "libsais_int", "libsais64_long", "libsais_plcp_int", "libsais_unbwt", "libsais_unbwt_aux", "libsais16_unbwt",
+    "libsais16_unbwt_aux", "libsais64_unbwt", "libsais64_unbwt_aux", "libsais16x64", "libsais16x64_bwt",
+    "libsais16x64_unbwt",
 ]
 
 _p = ctypes.c_void_p
@@ -89,6 +92,56 @@ _SIGS = {
     "libsais16_plcp_omp": (_i32, [_p, _p, _p, _i32, _i32]),
     "libsais16_plcp_gsa_omp": (_i32, [_p, _p, _p, _i32, _i32]),
     "libsais16_lcp_omp": (_i32, [_p, _p, _p, _i32, _i32]),
+    "libsais_int": (_i32, [_p, _p, _i32, _i32, _i32]),
+    "libsais_int_omp": (_i32, [_p, _p, _i32, _i32, _i32, _i32]),
+    "libsais_plcp_int": (_i32, [_p, _p, _p, _i32]),
+    "libsais_plcp_int_omp": (_i32, [_p, _p, _p, _i32, _i32]),
+    "libsais16_int": (_i32, [_p, _p, _i32, _i32, _i32]),
+    "libsais16_int_omp": (_i32, [_p, _p, _i32, _i32, _i32, _i32]),
+    "libsais64_long": (_i64, [_p, _p, _i64, _i64, _i64]),
+    "libsais64_long_omp": (_i64, [_p, _p, _i64, _i64, _i64, _i64]),
+    "libsais_unbwt_create_ctx": (_p, []),
+    "libsais_unbwt_create_ctx_omp": (_p, [_i32]),
+    "libsais_unbwt_free_ctx": (None, [_p]),
+    "libsais_unbwt": (_i32, [_p, _p, _p, _i32, _p, _i32]),
+    "libsais_unbwt_ctx": (_i32, [_p, _p, _p, _p, _i32, _p, _i32]),
+    "libsais_unbwt_aux": (_i32, [_p, _p, _p, _i32, _p, _i32, _p]),
+    "libsais_unbwt_aux_ctx": (_i32, [_p, _p, _p, _p, _i32, _p, _i32, _p]),
+    "libsais_unbwt_omp": (_i32, [_p, _p, _p, _i32, _p, _i32, _i32]),
+    "libsais_unbwt_aux_omp": (_i32, [_p, _p, _p, _i32, _p, _i32, _p, _i32]),
+    "libsais16_unbwt_create_ctx": (_p, []),
+    "libsais16_unbwt_create_ctx_omp": (_p, [_i32]),
+    "libsais16_unbwt_free_ctx": (None, [_p]),
+    "libsais16_unbwt": (_i32, [_p, _p, _p, _i32, _p, _i32]),
+    "libsais16_unbwt_ctx": (_i32, [_p, _p, _p, _p, _i32, _p, _i32]),
+    "libsais16_unbwt_aux": (_i32, [_p, _p, _p, _i32, _p, _i32, _p]),
+    "libsais16_unbwt_aux_ctx": (_i32, [_p, _p, _p, _p, _i32, _p, _i32, _p]),
+    "libsais16_unbwt_omp": (_i32, [_p, _p, _p, _i32, _p, _i32, _i32]),
+    "libsais16_unbwt_aux_omp": (_i32, [_p, _p, _p, _i32, _p, _i32, _p, _i32]),
+    "libsais64_unbwt": (_i64, [_p, _p, _p, _i64, _p, _i64]),
+    "libsais64_unbwt_aux": (_i64, [_p, _p, _p, _i64, _p, _i64, _p]),
+    "libsais64_unbwt_omp": (_i64, [_p, _p, _p, _i64, _p, _i64, _i64]),
+    "libsais64_unbwt_aux_omp": (_i64, [_p, _p, _p, _i64, _p, _i64, _p, _i64]),
+    "libsais16x64": (_i64, [_p, _p, _i64, _i64, _p]),
+    "libsais16x64_gsa": (_i64, [_p, _p, _i64, _i64, _p]),
+    "libsais16x64_long": (_i64, [_p, _p, _i64, _i64, _i64]),
+    "libsais16x64_omp": (_i64, [_p, _p, _i64, _i64, _p, _i64]),
+    "libsais16x64_gsa_omp": (_i64, [_p, _p, _i64, _i64, _p, _i64]),
+    "libsais16x64_long_omp": (_i64, [_p, _p, _i64, _i64, _i64, _i64]),
+    "libsais16x64_bwt": (_i64, [_p, _p, _p, _i64, _i64, _p]),
+    "libsais16x64_bwt_aux": (_i64, [_p, _p, _p, _i64, _i64, _p, _i64, _p]),
+    "libsais16x64_bwt_omp": (_i64, [_p, _p, _p, _i64, _i64, _p, _i64]),
+    "libsais16x64_bwt_aux_omp": (_i64, [_p, _p, _p, _i64, _i64, _p, _i64, _p, _i64]),
+    "libsais16x64_unbwt": (_i64, [_p, _p, _p, _i64, _p, _i64]),
+    "libsais16x64_unbwt_aux": (_i64, [_p, _p, _p, _i64, _p, _i64, _p]),
+    "libsais16x64_unbwt_omp": (_i64, [_p, _p, _p, _i64, _p, _i64, _i64]),
+    "libsais16x64_unbwt_aux_omp": (_i64, [_p, _p, _p, _i64, _p, _i64, _p, _i64]),
+    "libsais16x64_plcp": (_i64, [_p, _p, _p, _i64]),
+    "libsais16x64_plcp_gsa": (_i64, [_p, _p, _p, _i64]),
+    "libsais16x64_lcp": (_i64, [_p, _p, _p, _i64]),
+    "libsais16x64_plcp_omp": (_i64, [_p, _p, _p, _i64, _i64]),
+    "libsais16x64_plcp_gsa_omp": (_i64, [_p, _p, _p, _i64, _i64]),
+    "libsais16x64_lcp_omp": (_i64, [_p, _p, _p, _i64, _i64]),
     "gsais_sa_device": (_i64, [_p, _p, _i32, _i64, _i32, _p, _i32, _p]),
     "gsais_sa_bwt_device": (_i64, [_p, _p, _i32, _i64, _p, _i32, _p, _p]),
     "gsais_plcp_device": (_i64, [_p, _p, _i32, _p, _p, _i32, _i64, _i32, _p]),
@@ -269,6 +322,102 @@ def libsais64_bwt(T, fs=0, freq=True):
 
 def libsais64_bwt_aux(T, r, fs=0, freq=True):
     return _bwt_call("libsais64_bwt_aux", T, 8, r, fs, freq)
+
+
+# ------------------------------------------------------- integer alphabets
+def libsais_int(T, k, fs=0, threads=None):
+    """libsais_int (or libsais_int_omp): SA of an int32 string over [0, k)."""
+    lib = load()
+    T = np.ascontiguousarray(T, dtype=np.int32)
+    SA = np.zeros(max(T.size, 1) + fs, dtype=np.int32)
+    if threads is None:
+        rc = lib.libsais_int(_ptr(T), _ptr(SA), T.size, k, fs)
+    else:
+        rc = lib.libsais_int_omp(_ptr(T), _ptr(SA), T.size, k, fs, threads)
+    return int(rc), SA[: T.size]
+
+
+def libsais64_long(T, k, fs=0, name="libsais64_long"):
+    """libsais64_long (or libsais16x64_long): SA of an int64 string over [0, k)."""
+    lib = load()
+    T = np.ascontiguousarray(T, dtype=np.int64)
+    SA = np.zeros(max(T.size, 1) + fs, dtype=np.int64)
+    rc = getattr(lib, name)(_ptr(T), _ptr(SA), T.size, k, fs)
+    return int(rc), SA[: T.size]
+
+
+def libsais_plcp_int(T, SA):
+    lib = load()
+    T = np.ascontiguousarray(T, dtype=np.int32)
+    SA = np.ascontiguousarray(SA, dtype=np.int32)
+    P = np.zeros(max(T.size, 1), dtype=np.int32)
+    rc = lib.libsais_plcp_int(_ptr(T), _ptr(SA), _ptr(P), T.size)
+    return int(rc), P[: T.size]
+
+
+# ------------------------------------------------------------- inverse BWT
+def _unbwt_call(name, U, width, r, I, ctx=None, threads=None, out=None):
+    lib = load()
+    U = _text(U)
+    n = U.size
+    T = np.zeros(max(n, 1), dtype=U.dtype) if out is None else out
+    A = np.zeros(n + 1, dtype=np.int32 if width == 4 else np.int64)
+    f = getattr(lib, name)
+    args = [_ptr(U), _ptr(T), _ptr(A), n, None]
+    if r is None:
+        args.append(I)   # the primary index
+    else:
+        I = np.ascontiguousarray(I, dtype=A.dtype)
+        args += [r, _ptr(I)]
+    if threads is not None:
+        args.append(threads)
+    if ctx is not None:
+        args = [ctx.handle] + args
+    rc = f(*args)
+    return int(rc), T[:n]
+
+
+def libsais_unbwt(U, primary, ctx=None, threads=None, out=None):
+    name = "libsais_unbwt_ctx" if ctx else ("libsais_unbwt_omp" if threads is not None else "libsais_unbwt")
+    return _unbwt_call(name, np.asarray(U, dtype=np.uint8), 4, None, primary, ctx, threads, out)
+
+
+def libsais_unbwt_aux(U, r, I, ctx=None):
+    return _unbwt_call("libsais_unbwt_aux_ctx" if ctx else "libsais_unbwt_aux", np.asarray(U, dtype=np.uint8), 4, r,
+                       I, ctx)
+
+
+def libsais16_unbwt(U, primary, ctx=None):
+    return _unbwt_call("libsais16_unbwt_ctx" if ctx else "libsais16_unbwt", np.asarray(U, dtype=np.uint16), 4, None,
+                       primary, ctx)
+
+
+def libsais16_unbwt_aux(U, r, I):
+    return _unbwt_call("libsais16_unbwt_aux", np.asarray(U, dtype=np.uint16), 4, r, I)
+
+
+def libsais64_unbwt(U, primary):
+    return _unbwt_call("libsais64_unbwt", np.asarray(U, dtype=np.uint8), 8, None, primary)
+
+
+def libsais64_unbwt_aux(U, r, I):
+    return _unbwt_call("libsais64_unbwt_aux", np.asarray(U, dtype=np.uint8), 8, r, I)
+
+
+# ----------------------------------------------- 16-bit symbols, int64 index
+def libsais16x64(T, fs=0, freq=True, gsa=False):
+    return _sa_call("libsais16x64_gsa" if gsa else "libsais16x64", np.asarray(T, dtype=np.uint16), 8, fs, freq)
+
+
+def libsais16x64_bwt(T, r=0, fs=0, freq=True):
+    if r:
+        return _bwt_call("libsais16x64_bwt_aux", np.asarray(T, dtype=np.uint16), 8, r, fs, freq)
+    rc, U, _, F = _bwt_call("libsais16x64_bwt", np.asarray(T, dtype=np.uint16), 8, 0, fs, freq)
+    return rc, U, F
+
+
+def libsais16x64_unbwt(U, primary):
+    return _unbwt_call("libsais16x64_unbwt", np.asarray(U, dtype=np.uint16), 8, None, primary)
 
 
 def _plcp_call(name, T, SA, width):

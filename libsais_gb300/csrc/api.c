@@ -15,6 +15,7 @@
 #include "../../include/libsais.h"
 #include "../../include/libsais16.h"
 #include "../../include/libsais64.h"
+#include "../../include/libsais16x64.h"
 #include "gsais.h"
 
 /* ------------------------------------------------------------ helpers */
@@ -107,6 +108,40 @@ static int64_t do_lcp(const void *PLCP, const void *SA, void *LCP, int idx_bytes
         return 0;
     }
     return gsais_run_lcp(gsais_default_ctx(), PLCP, SA, LCP, idx_bytes, n);
+}
+
+/* SA of an integer string: (src/libsais.c:7050 libsais_int, src/libsais64.c:7118 libsais64_long) */
+static int64_t do_sa_int(const void *T, int tbytes, void *SA, int idx_bytes, int64_t n, int64_t k, int64_t fs)
+{
+    if (T == NULL || SA == NULL || n < 0 || fs < 0) return -1;
+    if (n <= 1) {
+        if (n == 1) put_index(SA, idx_bytes, 0, 0);
+        return 0;
+    }
+    return gsais_run_sa_int(gsais_default_ctx(), T, tbytes, n, k, SA, idx_bytes);
+}
+
+/* Inverse BWT: (src/libsais.c:8040 libsais_unbwt_aux; libsais_unbwt is r = n, I = &i, :8030) */
+static int64_t do_unbwt(gsais_ctx *ctx, const void *T, int symbytes, void *U, const void *A, int64_t n, int64_t r,
+                        const void *I, int idx_bytes)
+{
+    if (T == NULL || U == NULL || A == NULL || n < 0 || ((r != n) && ((r < 2) || ((r & (r - 1)) != 0))) ||
+        I == NULL)
+        return -1;
+    if (n <= 1) {
+        if (get_index(I, idx_bytes, 0) != n) return -1;
+        if (n == 1) {
+            if (symbytes == 1) ((uint8_t *)U)[0] = ((const uint8_t *)T)[0];
+            else ((uint16_t *)U)[0] = ((const uint16_t *)T)[0];
+        }
+        return 0;
+    }
+    for (int64_t t = 0; t <= (n - 1) / r; ++t) {
+        const int64_t v = get_index(I, idx_bytes, t);
+        if (v <= 0 || v > n) return -1;
+    }
+    if (ctx == NULL) return -2;
+    return gsais_run_unbwt(ctx, T, symbytes, n, get_index(I, idx_bytes, 0), U);
 }
 
 #define DEF_CTX gsais_default_ctx()
@@ -420,4 +455,305 @@ int32_t libsais16_lcp_omp(const int32_t *PLCP, const int32_t *SA, int32_t *LCP, 
 {
     if (threads < 0) return -1;
     return (int32_t)do_lcp(PLCP, SA, LCP, 4, n);
+}
+
+/* ------------------------------------ integer alphabets (libsais.h, libsais16.h, libsais64.h) */
+
+int32_t libsais_int(int32_t *T, int32_t *SA, int32_t n, int32_t k, int32_t fs)
+{
+    return (int32_t)do_sa_int(T, 4, SA, 4, n, k, fs);
+}
+
+int32_t libsais_int_omp(int32_t *T, int32_t *SA, int32_t n, int32_t k, int32_t fs, int32_t threads)
+{
+    if (threads < 0) return -1;
+    return (int32_t)do_sa_int(T, 4, SA, 4, n, k, fs);
+}
+
+int32_t libsais16_int(int32_t *T, int32_t *SA, int32_t n, int32_t k, int32_t fs)
+{
+    return (int32_t)do_sa_int(T, 4, SA, 4, n, k, fs);
+}
+
+int32_t libsais16_int_omp(int32_t *T, int32_t *SA, int32_t n, int32_t k, int32_t fs, int32_t threads)
+{
+    if (threads < 0) return -1;
+    return (int32_t)do_sa_int(T, 4, SA, 4, n, k, fs);
+}
+
+int64_t libsais64_long(int64_t *T, int64_t *SA, int64_t n, int64_t k, int64_t fs)
+{
+    return do_sa_int(T, 8, SA, 8, n, k, fs);
+}
+
+int64_t libsais64_long_omp(int64_t *T, int64_t *SA, int64_t n, int64_t k, int64_t fs, int64_t threads)
+{
+    if (threads < 0) return -1;
+    return do_sa_int(T, 8, SA, 8, n, k, fs);
+}
+
+/* (src/libsais.c:8399 libsais_plcp_int) */
+int32_t libsais_plcp_int(const int32_t *T, const int32_t *SA, int32_t *PLCP, int32_t n)
+{
+    if (T == NULL || SA == NULL || PLCP == NULL || n < 0) return -1;
+    if (n <= 1) {
+        if (n == 1) PLCP[0] = 0;
+        return 0;
+    }
+    return (int32_t)gsais_run_plcp(gsais_default_ctx(), T, 4, SA, PLCP, 4, n, 0);
+}
+
+int32_t libsais_plcp_int_omp(const int32_t *T, const int32_t *SA, int32_t *PLCP, int32_t n, int32_t threads)
+{
+    if (threads < 0) return -1;
+    return libsais_plcp_int(T, SA, PLCP, n);
+}
+
+/* ----------------------------------------------------- inverse BWT, 8-bit */
+
+void *libsais_unbwt_create_ctx(void) { return gsais_ctx_create(); }
+
+void *libsais_unbwt_create_ctx_omp(int32_t threads) { return threads < 0 ? NULL : gsais_ctx_create(); }
+
+void libsais_unbwt_free_ctx(void *ctx) { gsais_ctx_destroy((gsais_ctx *)ctx); }
+
+int32_t libsais_unbwt(const uint8_t *T, uint8_t *U, int32_t *A, int32_t n, const int32_t *freq, int32_t i)
+{
+    (void)freq;
+    return (int32_t)do_unbwt(DEF_CTX, T, 1, U, A, n, n, &i, 4);
+}
+
+int32_t libsais_unbwt_ctx(const void *ctx, const uint8_t *T, uint8_t *U, int32_t *A, int32_t n, const int32_t *freq,
+                          int32_t i)
+{
+    (void)freq;
+    return (int32_t)do_unbwt(USE_CTX(ctx), T, 1, U, A, n, n, &i, 4);
+}
+
+int32_t libsais_unbwt_aux(const uint8_t *T, uint8_t *U, int32_t *A, int32_t n, const int32_t *freq, int32_t r,
+                          const int32_t *I)
+{
+    (void)freq;
+    return (int32_t)do_unbwt(DEF_CTX, T, 1, U, A, n, r, I, 4);
+}
+
+int32_t libsais_unbwt_aux_ctx(const void *ctx, const uint8_t *T, uint8_t *U, int32_t *A, int32_t n,
+                              const int32_t *freq, int32_t r, const int32_t *I)
+{
+    (void)freq;
+    return (int32_t)do_unbwt(USE_CTX(ctx), T, 1, U, A, n, r, I, 4);
+}
+
+int32_t libsais_unbwt_omp(const uint8_t *T, uint8_t *U, int32_t *A, int32_t n, const int32_t *freq, int32_t i,
+                          int32_t threads)
+{
+    if (threads < 0) return -1;
+    return libsais_unbwt(T, U, A, n, freq, i);
+}
+
+int32_t libsais_unbwt_aux_omp(const uint8_t *T, uint8_t *U, int32_t *A, int32_t n, const int32_t *freq, int32_t r,
+                              const int32_t *I, int32_t threads)
+{
+    if (threads < 0) return -1;
+    return libsais_unbwt_aux(T, U, A, n, freq, r, I);
+}
+
+/* ---------------------------------------------------- inverse BWT, 16-bit */
+
+void *libsais16_unbwt_create_ctx(void) { return gsais_ctx_create(); }
+
+void *libsais16_unbwt_create_ctx_omp(int32_t threads) { return threads < 0 ? NULL : gsais_ctx_create(); }
+
+void libsais16_unbwt_free_ctx(void *ctx) { gsais_ctx_destroy((gsais_ctx *)ctx); }
+
+int32_t libsais16_unbwt(const uint16_t *T, uint16_t *U, int32_t *A, int32_t n, const int32_t *freq, int32_t i)
+{
+    (void)freq;
+    return (int32_t)do_unbwt(DEF_CTX, T, 2, U, A, n, n, &i, 4);
+}
+
+int32_t libsais16_unbwt_ctx(const void *ctx, const uint16_t *T, uint16_t *U, int32_t *A, int32_t n,
+                            const int32_t *freq, int32_t i)
+{
+    (void)freq;
+    return (int32_t)do_unbwt(USE_CTX(ctx), T, 2, U, A, n, n, &i, 4);
+}
+
+int32_t libsais16_unbwt_aux(const uint16_t *T, uint16_t *U, int32_t *A, int32_t n, const int32_t *freq, int32_t r,
+                            const int32_t *I)
+{
+    (void)freq;
+    return (int32_t)do_unbwt(DEF_CTX, T, 2, U, A, n, r, I, 4);
+}
+
+int32_t libsais16_unbwt_aux_ctx(const void *ctx, const uint16_t *T, uint16_t *U, int32_t *A, int32_t n,
+                                const int32_t *freq, int32_t r, const int32_t *I)
+{
+    (void)freq;
+    return (int32_t)do_unbwt(USE_CTX(ctx), T, 2, U, A, n, r, I, 4);
+}
+
+int32_t libsais16_unbwt_omp(const uint16_t *T, uint16_t *U, int32_t *A, int32_t n, const int32_t *freq, int32_t i,
+                            int32_t threads)
+{
+    if (threads < 0) return -1;
+    return libsais16_unbwt(T, U, A, n, freq, i);
+}
+
+int32_t libsais16_unbwt_aux_omp(const uint16_t *T, uint16_t *U, int32_t *A, int32_t n, const int32_t *freq,
+                                int32_t r, const int32_t *I, int32_t threads)
+{
+    if (threads < 0) return -1;
+    return libsais16_unbwt_aux(T, U, A, n, freq, r, I);
+}
+
+/* ---------------------------------------------- inverse BWT, 64-bit indexes */
+
+int64_t libsais64_unbwt(const uint8_t *T, uint8_t *U, int64_t *A, int64_t n, const int64_t *freq, int64_t i)
+{
+    (void)freq;
+    return do_unbwt(DEF_CTX, T, 1, U, A, n, n, &i, 8);
+}
+
+int64_t libsais64_unbwt_aux(const uint8_t *T, uint8_t *U, int64_t *A, int64_t n, const int64_t *freq, int64_t r,
+                            const int64_t *I)
+{
+    (void)freq;
+    return do_unbwt(DEF_CTX, T, 1, U, A, n, r, I, 8);
+}
+
+int64_t libsais64_unbwt_omp(const uint8_t *T, uint8_t *U, int64_t *A, int64_t n, const int64_t *freq, int64_t i,
+                            int64_t threads)
+{
+    if (threads < 0) return -1;
+    return libsais64_unbwt(T, U, A, n, freq, i);
+}
+
+int64_t libsais64_unbwt_aux_omp(const uint8_t *T, uint8_t *U, int64_t *A, int64_t n, const int64_t *freq, int64_t r,
+                                const int64_t *I, int64_t threads)
+{
+    if (threads < 0) return -1;
+    return libsais64_unbwt_aux(T, U, A, n, freq, r, I);
+}
+
+/* ---------------------------- libsais16x64.h: 16-bit symbols, 64-bit indexes
+ * (src/libsais16x64.c:7036-7230 and :7789-8100 delegate to the 16-bit code
+ * and widen the results; here the engine writes int64 directly) */
+
+int64_t libsais16x64(const uint16_t *T, int64_t *SA, int64_t n, int64_t fs, int64_t *freq)
+{
+    return do_sa(DEF_CTX, T, 2, SA, 8, n, fs, freq, 0);
+}
+
+int64_t libsais16x64_gsa(const uint16_t *T, int64_t *SA, int64_t n, int64_t fs, int64_t *freq)
+{
+    return do_sa(DEF_CTX, T, 2, SA, 8, n, fs, freq, 1);
+}
+
+int64_t libsais16x64_long(int64_t *T, int64_t *SA, int64_t n, int64_t k, int64_t fs)
+{
+    return do_sa_int(T, 8, SA, 8, n, k, fs);
+}
+
+int64_t libsais16x64_omp(const uint16_t *T, int64_t *SA, int64_t n, int64_t fs, int64_t *freq, int64_t threads)
+{
+    if (threads < 0) return -1;
+    return libsais16x64(T, SA, n, fs, freq);
+}
+
+int64_t libsais16x64_gsa_omp(const uint16_t *T, int64_t *SA, int64_t n, int64_t fs, int64_t *freq, int64_t threads)
+{
+    if (threads < 0) return -1;
+    return libsais16x64_gsa(T, SA, n, fs, freq);
+}
+
+int64_t libsais16x64_long_omp(int64_t *T, int64_t *SA, int64_t n, int64_t k, int64_t fs, int64_t threads)
+{
+    if (threads < 0) return -1;
+    return libsais16x64_long(T, SA, n, k, fs);
+}
+
+int64_t libsais16x64_bwt(const uint16_t *T, uint16_t *U, int64_t *A, int64_t n, int64_t fs, int64_t *freq)
+{
+    return do_bwt(DEF_CTX, T, 2, U, A, 8, n, fs, freq, 0, NULL, 0);
+}
+
+int64_t libsais16x64_bwt_aux(const uint16_t *T, uint16_t *U, int64_t *A, int64_t n, int64_t fs, int64_t *freq,
+                             int64_t r, int64_t *I)
+{
+    return do_bwt(DEF_CTX, T, 2, U, A, 8, n, fs, freq, r, I, 1);
+}
+
+int64_t libsais16x64_bwt_omp(const uint16_t *T, uint16_t *U, int64_t *A, int64_t n, int64_t fs, int64_t *freq,
+                             int64_t threads)
+{
+    if (threads < 0) return -1;
+    return libsais16x64_bwt(T, U, A, n, fs, freq);
+}
+
+int64_t libsais16x64_bwt_aux_omp(const uint16_t *T, uint16_t *U, int64_t *A, int64_t n, int64_t fs, int64_t *freq,
+                                 int64_t r, int64_t *I, int64_t threads)
+{
+    if (threads < 0) return -1;
+    return libsais16x64_bwt_aux(T, U, A, n, fs, freq, r, I);
+}
+
+int64_t libsais16x64_unbwt(const uint16_t *T, uint16_t *U, int64_t *A, int64_t n, const int64_t *freq, int64_t i)
+{
+    (void)freq;
+    return do_unbwt(DEF_CTX, T, 2, U, A, n, n, &i, 8);
+}
+
+int64_t libsais16x64_unbwt_aux(const uint16_t *T, uint16_t *U, int64_t *A, int64_t n, const int64_t *freq,
+                               int64_t r, const int64_t *I)
+{
+    (void)freq;
+    return do_unbwt(DEF_CTX, T, 2, U, A, n, r, I, 8);
+}
+
+int64_t libsais16x64_unbwt_omp(const uint16_t *T, uint16_t *U, int64_t *A, int64_t n, const int64_t *freq, int64_t i,
+                               int64_t threads)
+{
+    if (threads < 0) return -1;
+    return libsais16x64_unbwt(T, U, A, n, freq, i);
+}
+
+int64_t libsais16x64_unbwt_aux_omp(const uint16_t *T, uint16_t *U, int64_t *A, int64_t n, const int64_t *freq,
+                                   int64_t r, const int64_t *I, int64_t threads)
+{
+    if (threads < 0) return -1;
+    return libsais16x64_unbwt_aux(T, U, A, n, freq, r, I);
+}
+
+int64_t libsais16x64_plcp(const uint16_t *T, const int64_t *SA, int64_t *PLCP, int64_t n)
+{
+    return do_plcp(T, 2, SA, PLCP, 8, n, 0);
+}
+
+int64_t libsais16x64_plcp_gsa(const uint16_t *T, const int64_t *SA, int64_t *PLCP, int64_t n)
+{
+    return do_plcp(T, 2, SA, PLCP, 8, n, 1);
+}
+
+int64_t libsais16x64_lcp(const int64_t *PLCP, const int64_t *SA, int64_t *LCP, int64_t n)
+{
+    return do_lcp(PLCP, SA, LCP, 8, n);
+}
+
+int64_t libsais16x64_plcp_omp(const uint16_t *T, const int64_t *SA, int64_t *PLCP, int64_t n, int64_t threads)
+{
+    if (threads < 0) return -1;
+    return libsais16x64_plcp(T, SA, PLCP, n);
+}
+
+int64_t libsais16x64_plcp_gsa_omp(const uint16_t *T, const int64_t *SA, int64_t *PLCP, int64_t n, int64_t threads)
+{
+    if (threads < 0) return -1;
+    return libsais16x64_plcp_gsa(T, SA, PLCP, n);
+}
+
+int64_t libsais16x64_lcp_omp(const int64_t *PLCP, const int64_t *SA, int64_t *LCP, int64_t n, int64_t threads)
+{
+    if (threads < 0) return -1;
+    return libsais16x64_lcp(PLCP, SA, LCP, n);
 }

@@ -16,6 +16,7 @@
 #include "gsais.h"
 #include "libsais_gb300.h"
 #include "outputs.cuh"
+#include "unbwt.cuh"
 #include "suffix_sort.cuh"
 
 using namespace gsais;
@@ -25,6 +26,7 @@ struct gsais_ctx {
     bool ready = false;
     int device = -1;
     cudaStream_t stream = nullptr;
+    cudaStream_t copy_stream = nullptr;   // device->host copies that overlap later kernels
     void *arena = nullptr;
     size_t arena_bytes = 0;
     uint32_t *d_misc = nullptr;   // [0] error word, [1] validity flag
@@ -62,6 +64,7 @@ bool ctx_init(gsais_ctx *c)
     if (c->ready) return true;
     if (cudaGetDevice(&c->device) != cudaSuccess) return false;
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return false;
+    if (cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess) return false;
     if (cudaMalloc(&c->d_misc, 64) != cudaSuccess) return false;
     if (cudaMemset(c->d_misc, 0, 64) != cudaSuccess) return false;
     if (cudaMallocHost(&c->h_small, kSmallWords * sizeof(uint32_t)) != cudaSuccess) return false;
@@ -138,6 +141,15 @@ int64_t fail(cudaError_t)
         if (_e != cudaSuccess) return fail(_e);              \
     } while (0)
 
+// Waits for a stream when it goes out of scope.
+struct StreamJoin {
+    cudaStream_t s;
+    ~StreamJoin()
+    {
+        if (s) cudaStreamSynchronize(s);
+    }
+};
+
 PackedText packed_of(const SortWorkspace &ws)
 {
     PackedText pk;
@@ -164,7 +176,7 @@ SortPlan plan_sort(uint64_t n, int symbytes, size_t extra)
 // Sort a device text already placed in the arena.  `sa_override` (nullable)
 // receives SA directly when the caller wants uint32 output in its own buffer.
 int64_t run_sort(gsais_ctx *c, const void *d_T, int symbytes, uint64_t n, bool gsa, SortWorkspace &ws,
-                 cudaStream_t st)
+                 cudaStream_t st, uint32_t raw_max = 0)
 {
     if (gsa) {
         bool valid = true;
@@ -172,7 +184,9 @@ int64_t run_sort(gsais_ctx *c, const void *d_T, int symbytes, uint64_t n, bool g
         if (!valid) return -1;
     }
     ws.radix.prof = &c->prof;
-    GS_TRY(suffix_sort(d_T, symbytes, n, gsa, ws, c->opt, c->d_misc, st, &c->stats));
+    SortOptions opt = c->opt;
+    opt.raw_max = raw_max;
+    GS_TRY(suffix_sort(d_T, symbytes, n, gsa, ws, opt, c->d_misc, st, &c->stats));
     return 0;
 }
 
@@ -193,11 +207,13 @@ void gsais_ctx_destroy(gsais_ctx *c)
     if (c->ready) {
         DeviceGuard g(c->device);
         if (c->stream) cudaStreamSynchronize(c->stream);
+        if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
         if (c->arena) cudaFree(c->arena);
         if (c->d_misc) cudaFree(c->d_misc);
         if (c->h_small) cudaFreeHost(c->h_small);
         if (c->h_hist) cudaFreeHost(c->h_hist);
         if (c->stream) cudaStreamDestroy(c->stream);
+        if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     }
     delete c;
 }
@@ -248,6 +264,58 @@ int64_t gsais_run_sa(gsais_ctx *c, const void *T, int symbytes, int64_t n_, int 
     return 0;
 }
 
+int64_t gsais_run_sa_int(gsais_ctx *c, const void *T, int tbytes, int64_t n_, int64_t k, void *SA, int sa_bytes)
+{
+    if (!c || (tbytes != 4 && tbytes != 8)) return -2;
+    std::lock_guard<std::mutex> lock(c->mu);
+    const uint64_t n = (uint64_t)n_;
+    if (n > kMaxN) return -2;
+    if (!ctx_init(c)) return fail(cudaErrorUnknown);
+    DeviceGuard g(c->device);
+    cudaStream_t st = c->stream;
+    const size_t extra = align_up(n * tbytes) + align_up(n * 4) + (sa_bytes == 8 ? align_up(n * 8) : 0) + kAlign;
+    const SortPlan plan = plan_sort(n, 4, extra);
+    if (!ensure_arena(c, plan.total)) return -2;
+    Carver cv(c->arena);
+    uint8_t *d_T = cv.take<uint8_t>(n * tbytes);
+    uint8_t *d_N = cv.take<uint8_t>(n * 4);   // symbols narrowed to 16 or 32 bits
+    int64_t *d_wide = sa_bytes == 8 ? cv.take<int64_t>(n) : nullptr;
+    unsigned long long *d_scan = cv.take<unsigned long long>(2);
+    SortWorkspace ws;
+    sort_workspace_carve(ws, cv.p, n, 4, c->h_small, c->h_hist);
+    if (!clear_err(c, st)) return fail(cudaErrorUnknown);
+    GS_TRY(cudaMemcpyAsync(d_T, T, n * tbytes, cudaMemcpyHostToDevice, st));
+    GS_TRY(int_alphabet_scan(d_T, tbytes, n, k, d_scan, st));
+    unsigned long long *h_scan = reinterpret_cast<unsigned long long *>(c->h_small + 2);
+    GS_TRY(cudaMemcpyAsync(h_scan, d_scan, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    GS_TRY(cudaStreamSynchronize(st));
+    if (h_scan[1]) return -1;   // a symbol outside [0, k)
+    const unsigned long long mx = h_scan[0];
+    if (mx > 0xFFFFFFFFull) return -2;   // symbols wider than 32 bits are not supported
+    int64_t rc;
+    if (mx < 65536) {
+        // small alphabets take the 16-bit path (dense codes, packed text)
+        GS_TRY(int_narrow(d_T, tbytes, n, d_N, 2, st));
+        rc = run_sort(c, d_N, 2, n, false, ws, st);
+    } else {
+        const void *src = d_T;   // non-negative int32 symbols are uint32 symbols
+        if (tbytes == 8) {
+            GS_TRY(int_narrow(d_T, 8, n, d_N, 4, st));
+            src = d_N;
+        }
+        rc = run_sort(c, src, 4, n, false, ws, st, (uint32_t)mx);
+    }
+    if (rc != 0) return rc;
+    if (sa_bytes == 8) {
+        GS_TRY(widen_u32_to_i64(ws.sa, d_wide, n, st));
+        GS_TRY(cudaMemcpyAsync(SA, d_wide, n * 8, cudaMemcpyDeviceToHost, st));
+    } else {
+        GS_TRY(cudaMemcpyAsync(SA, ws.sa, n * 4, cudaMemcpyDeviceToHost, st));
+    }
+    GS_TRY(sync_checked(c, st));
+    return 0;
+}
+
 int64_t gsais_run_bwt(gsais_ctx *c, const void *T, int symbytes, int64_t n_, void *U, void *freq, int freq_bytes,
                       int64_t r, void *I, int idx_bytes, void *SA, int sa_bytes)
 {
@@ -274,23 +342,51 @@ int64_t gsais_run_bwt(gsais_ctx *c, const void *T, int symbytes, int64_t n_, voi
     GS_TRY(cudaMemcpyAsync(d_T, T, n * symbytes, cudaMemcpyHostToDevice, st));
     const int64_t rc = run_sort(c, d_T, symbytes, n, false, ws, st);
     if (rc != 0) return rc;
+    // the sort has completed (run_sort synchronises st): SA leaves on the copy
+    // stream while the BWT gather, which only reads SA, runs on st
+    cudaStream_t cs = c->copy_stream;
+    StreamJoin join{cs};   // no copy into the caller's buffer outlives the call, also on error returns
+    if (SA) {
+        if (sa_bytes == 8) {
+            GS_TRY(widen_u32_to_i64(ws.sa, d_wide, n, cs));
+            GS_TRY(cudaMemcpyAsync(SA, d_wide, n * 8, cudaMemcpyDeviceToHost, cs));
+        } else {
+            GS_TRY(cudaMemcpyAsync(SA, ws.sa, n * 4, cudaMemcpyDeviceToHost, cs));
+        }
+    }
     GS_TRY(bwt_gather(d_T, symbytes, ws.sa, ws.rank, n, d_U, packed_of(ws), c->d_misc, st));
     if (r > 0) GS_TRY(aux_sample(ws.rank, n, (uint64_t)r, d_I, idx_bytes, st));
     GS_TRY(cudaMemcpyAsync(c->h_small, ws.rank, 4, cudaMemcpyDeviceToHost, st));
     GS_TRY(cudaMemcpyAsync(U, d_U, n * symbytes, cudaMemcpyDeviceToHost, st));
     if (r > 0) GS_TRY(cudaMemcpyAsync(I, d_I, icount * idx_bytes, cudaMemcpyDeviceToHost, st));
-    if (SA) {
-        if (sa_bytes == 8) {
-            GS_TRY(widen_u32_to_i64(ws.sa, d_wide, n, st));
-            GS_TRY(cudaMemcpyAsync(SA, d_wide, n * 8, cudaMemcpyDeviceToHost, st));
-        } else {
-            GS_TRY(cudaMemcpyAsync(SA, ws.sa, n * 4, cudaMemcpyDeviceToHost, st));
-        }
-    }
+    const cudaError_t ce = cudaStreamSynchronize(cs);
     GS_TRY(sync_checked(c, st));
+    GS_TRY(ce);
     const int64_t prim = (int64_t)c->h_small[0];   // ISA[0] + 1
     emit_freq(c->h_small + 16, symbytes, freq, freq_bytes);
     return r > 0 ? 0 : prim;
+}
+
+int64_t gsais_run_unbwt(gsais_ctx *c, const void *T, int symbytes, int64_t n_, int64_t primary, void *U)
+{
+    if (!c) return -2;
+    std::lock_guard<std::mutex> lock(c->mu);
+    const uint64_t n = (uint64_t)n_;
+    if (n > kMaxN - 1 || primary < 1 || (uint64_t)primary > n) return n > kMaxN - 1 ? -2 : -1;
+    if (!ctx_init(c)) return fail(cudaErrorUnknown);
+    DeviceGuard g(c->device);
+    cudaStream_t st = c->stream;
+    const size_t total = 2 * align_up(n * symbytes) + unbwt_workspace_bytes(n);
+    if (!ensure_arena(c, total)) return -2;
+    Carver cv(c->arena);
+    uint8_t *d_in = cv.take<uint8_t>(n * symbytes);
+    uint8_t *d_out = cv.take<uint8_t>(n * symbytes);
+    if (!clear_err(c, st)) return fail(cudaErrorUnknown);
+    GS_TRY(cudaMemcpyAsync(d_in, T, n * symbytes, cudaMemcpyHostToDevice, st));
+    GS_TRY(unbwt_run(d_in, symbytes, n, (uint64_t)primary, d_out, cv.p, c->h_hist, &c->prof, c->d_misc, st));
+    GS_TRY(cudaMemcpyAsync(U, d_out, n * symbytes, cudaMemcpyDeviceToHost, st));
+    GS_TRY(sync_checked(c, st));
+    return 0;
 }
 
 int64_t gsais_run_plcp(gsais_ctx *c, const void *T, int symbytes, const void *SA, void *PLCP, int idx_bytes,

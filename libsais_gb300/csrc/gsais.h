@@ -30,11 +30,22 @@ gsais_ctx *gsais_default_ctx(void);
 int64_t gsais_run_sa(gsais_ctx *ctx, const void *T, int symbytes, int64_t n, int gsa, void *SA, int sa_bytes,
                      void *freq, int freq_bytes);
 
+/* SA of an integer string (tbytes 4: int32, 8: int64 symbols) over [0, k)
+ * (libsais_int, libsais64_long).  -1 if a symbol lies outside [0, k); -2 if a
+ * symbol is wider than 32 bits. */
+int64_t gsais_run_sa_int(gsais_ctx *ctx, const void *T, int tbytes, int64_t n, int64_t k, void *SA, int sa_bytes);
+
 /* BWT into U (libsais_bwt layout).  r > 0 also writes I[t] = ISA[t*r] + 1
  * (idx_bytes wide) and returns 0 instead of the primary index.  SA (may be
  * NULL) additionally receives the suffix array. */
 int64_t gsais_run_bwt(gsais_ctx *ctx, const void *T, int symbytes, int64_t n, void *U, void *freq, int freq_bytes,
                       int64_t r, void *I, int idx_bytes, void *SA, int sa_bytes);
+
+/* Text from its BWT T (libsais_bwt layout, symbytes 1 or 2) and primary
+ * index (1..n) into U (libsais_unbwt).  -1 for a primary index outside 1..n,
+ * -2 for device failures or a T that is not the BWT of any text with that
+ * primary index. */
+int64_t gsais_run_unbwt(gsais_ctx *ctx, const void *T, int symbytes, int64_t n, int64_t primary, void *U);
 
 /* PLCP of (T, SA) into PLCP (idx_bytes wide). */
 int64_t gsais_run_plcp(gsais_ctx *ctx, const void *T, int symbytes, const void *SA, void *PLCP, int idx_bytes,

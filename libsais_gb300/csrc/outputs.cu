@@ -88,6 +88,40 @@ __global__ void __launch_bounds__(256) k_narrow(const int64_t *__restrict__ s, u
     }
 }
 
+// Integer alphabets: the largest value and whether any value lies outside
+// [0, k) (libsais_int, src/libsais.c:7050; libsais64_long, src/libsais64.c:7118).
+// out[0] = max (as uint64), out[1] = 1 if a value is out of range.
+template <typename I>
+__global__ void __launch_bounds__(256) k_int_scan(const I *__restrict__ T, uint64_t n, int64_t k,
+                                                  unsigned long long *__restrict__ out)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    unsigned long long mx = 0;
+    bool bad = false;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const int64_t v = (int64_t)T[i];
+        bad |= v < 0 || v >= k;
+        if (v > 0 && (unsigned long long)v > mx) mx = (unsigned long long)v;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long y = __shfl_down_sync(GSAIS_FULL_MASK, mx, o);
+        if (y > mx) mx = y;
+    }
+    const bool anybad = __any_sync(GSAIS_FULL_MASK, bad);
+    if ((threadIdx.x & 31) == 0) {
+        if (mx) atomicMax(&out[0], mx);
+        if (anybad) atomicOr(&out[1], 1ull);
+    }
+}
+
+// Integer symbols narrowed to 16 or 32 bits (the caller checked the range).
+template <typename I, typename O>
+__global__ void __launch_bounds__(256) k_int_narrow(const I *__restrict__ T, uint64_t n, O *__restrict__ out)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) out[i] = (O)T[i];
+}
+
 // Phi[SA[j]] = SA[j-1], Phi[SA[0]] = n (src/libsais.c:8116 compute_phi).
 // Bytes per row: SA 4 + 4 read, Phi 4 scattered.
 __global__ void __launch_bounds__(256) k_phi(const uint32_t *__restrict__ SA, uint64_t n, uint32_t *__restrict__ phi,
@@ -281,6 +315,10 @@ cudaError_t plcp_build(const void *d_T, int symbytes, const uint32_t *d_SA, uint
                        uint32_t *d_sparse, uint32_t *err, cudaStream_t st)
 {
     if (n == 0) return cudaSuccess;
+    if (symbytes == 4) {   // integer symbols (libsais_plcp_int, src/libsais.c:8399): plain stop rule
+        const uint32_t *T = static_cast<const uint32_t *>(d_T);
+        return plcp_run<uint32_t, false>(T, d_SA, n, d_PLCP, d_sparse, err, st);
+    }
     if (symbytes == 1) {
         const uint8_t *T = static_cast<const uint8_t *>(d_T);
         return gsa ? plcp_run<uint8_t, true>(T, d_SA, n, d_PLCP, d_sparse, err, st)
@@ -289,6 +327,38 @@ cudaError_t plcp_build(const void *d_T, int symbytes, const uint32_t *d_SA, uint
     const uint16_t *T = static_cast<const uint16_t *>(d_T);
     return gsa ? plcp_run<uint16_t, true>(T, d_SA, n, d_PLCP, d_sparse, err, st)
                : plcp_run<uint16_t, false>(T, d_SA, n, d_PLCP, d_sparse, err, st);
+}
+
+cudaError_t int_alphabet_scan(const void *d_T, int tbytes, uint64_t n, int64_t k, unsigned long long *d_out,
+                              cudaStream_t st)
+{
+    cudaError_t e = cudaMemsetAsync(d_out, 0, 2 * sizeof(unsigned long long), st);
+    if (e != cudaSuccess || n == 0) return e;
+    if (tbytes == 4)
+        GSAIS_COUNTED((k_int_scan<int32_t><<<grid_for(n, 256), 256, 0, st>>>(static_cast<const int32_t *>(d_T), n, k,
+                                                                           d_out)));
+    else
+        GSAIS_COUNTED((k_int_scan<int64_t><<<grid_for(n, 256), 256, 0, st>>>(static_cast<const int64_t *>(d_T), n, k,
+                                                                           d_out)));
+    return cudaGetLastError();
+}
+
+cudaError_t int_narrow(const void *d_T, int tbytes, uint64_t n, void *d_out, int obytes, cudaStream_t st)
+{
+    if (n == 0) return cudaSuccess;
+    const int g = grid_for(n, 256);
+    if (tbytes == 4 && obytes == 2)
+        GSAIS_COUNTED((k_int_narrow<int32_t, uint16_t><<<g, 256, 0, st>>>(static_cast<const int32_t *>(d_T), n,
+                                                                           static_cast<uint16_t *>(d_out))));
+    else if (tbytes == 8 && obytes == 2)
+        GSAIS_COUNTED((k_int_narrow<int64_t, uint16_t><<<g, 256, 0, st>>>(static_cast<const int64_t *>(d_T), n,
+                                                                           static_cast<uint16_t *>(d_out))));
+    else if (tbytes == 8 && obytes == 4)
+        GSAIS_COUNTED((k_int_narrow<int64_t, uint32_t><<<g, 256, 0, st>>>(static_cast<const int64_t *>(d_T), n,
+                                                                           static_cast<uint32_t *>(d_out))));
+    else
+        return cudaErrorInvalidValue;
+    return cudaGetLastError();
 }
 
 cudaError_t lcp_gather(const uint32_t *d_PLCP, const uint32_t *d_SA, uint32_t *d_LCP, uint64_t n, uint32_t *err,

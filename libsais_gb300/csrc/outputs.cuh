@@ -33,6 +33,13 @@ size_t plcp_sparse_words(uint64_t n);
 cudaError_t plcp_build(const void *d_T, int symbytes, const uint32_t *d_SA, uint64_t n, bool gsa, uint32_t *d_PLCP,
                        uint32_t *d_sparse, uint32_t *err, cudaStream_t st);
 
+// Integer alphabets (int32 or int64 symbols, tbytes 4 or 8): d_out[0] = the
+// largest value, d_out[1] = 1 if some value lies outside [0, k).
+cudaError_t int_alphabet_scan(const void *d_T, int tbytes, uint64_t n, int64_t k, unsigned long long *d_out,
+                              cudaStream_t st);
+// Integer symbols copied to obytes-wide unsigned symbols (values already checked to fit).
+cudaError_t int_narrow(const void *d_T, int tbytes, uint64_t n, void *d_out, int obytes, cudaStream_t st);
+
 // LCP[i] = PLCP[SA[i]].
 cudaError_t lcp_gather(const uint32_t *d_PLCP, const uint32_t *d_SA, uint32_t *d_LCP, uint64_t n, uint32_t *err,
                        cudaStream_t st);

@@ -33,6 +33,8 @@
 #include "radix_hist.cuh"
 #include "suffix_sort.cuh"
 
+#include <type_traits>
+
 namespace gsais {
 
 namespace {
@@ -111,7 +113,11 @@ __global__ void __launch_bounds__(256) k_seed(const Sym *__restrict__ T, uint64_
                                               uint8_t *__restrict__ packed)
 {
     constexpr int PER = kSeedTile / 256;
-    __shared__ uint16_t sc[kSeedTile + 64];
+    // 32-bit symbols (integer alphabets) are their own codes; 8/16-bit
+    // symbols go through the dense code table
+    constexpr bool RAW = sizeof(Sym) == 4;
+    using CodeT = typename std::conditional<RAW, uint32_t, uint16_t>::type;
+    __shared__ CodeT sc[kSeedTile + 64];
     __shared__ KeyT sk[kSeedTile];
     __shared__ uint32_t sh[kMaxRadixPasses][256];
     radix_hist_zero(sh, passes);
@@ -123,7 +129,7 @@ __global__ void __launch_bounds__(256) k_seed(const Sym *__restrict__ T, uint64_
         __syncthreads();   // previous tile's sk/sc reads are done
         for (int q = threadIdx.x; q < kSeedTile + K - 1; q += blockDim.x) {
             const uint64_t p = base + q;
-            sc[q] = p < n ? codes[T[p]] : (uint16_t)0;
+            sc[q] = p < n ? (RAW ? (CodeT)T[p] : (CodeT)codes[T[p]]) : (CodeT)0;
         }
         __syncthreads();
         KeyT key = 0;
@@ -1464,23 +1470,32 @@ cudaError_t suffix_sort(const void *d_T, int symbytes, uint64_t n, bool gsa, Sor
     S = SortStats();
     if (n == 0) return cudaSuccess;
 
-    // ---- symbol histogram -> dense codes
+    // ---- symbol histogram -> dense codes (32-bit integer symbols are their own
+    // codes: bits = bits(opt.raw_max))
+    const bool raw = symbytes == 4;
     const int nsym = symbytes == 1 ? 256 : 65536;
     uint32_t *h_hist = ws.h_small + 16;
     uint16_t *h_codes = reinterpret_cast<uint16_t *>(ws.h_small + 16 + 65536);
-    if ((e = symbol_histogram(d_T, symbytes, n, ws.hist, h_hist, st)) != cudaSuccess) return e;
-    uint32_t sigma = 0;
-    for (int c = 0; c < nsym; ++c) {
-        h_codes[c] = (uint16_t)sigma;
-        if (h_hist[c]) ++sigma;
+    int bits;
+    if (raw) {
+        bits = gsais_bits_for(opt.raw_max > 1 ? opt.raw_max : 1);
+    } else {
+        if ((e = symbol_histogram(d_T, symbytes, n, ws.hist, h_hist, st)) != cudaSuccess) return e;
+        uint32_t sigma = 0;
+        for (int c = 0; c < nsym; ++c) {
+            h_codes[c] = (uint16_t)sigma;
+            if (h_hist[c]) ++sigma;
+        }
+        bits = gsais_bits_for(sigma > 1 ? sigma - 1 : 1);
     }
-    int bits = gsais_bits_for(sigma > 1 ? sigma - 1 : 1);
     int K = (opt.seed_key_bits <= 32 ? 32 : 64) / bits;
+    if (K < 2 && bits <= 32) K = 64 / bits;   // wide symbols: at least two per key
     if (K < 1) K = 1;
     if (K > 64) K = 64;
     S.seed_symbols = K;
     S.seed_bits = bits;
-    if ((e = cudaMemcpyAsync(ws.codes, h_codes, (size_t)nsym * 2, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+    if (!raw &&
+        (e = cudaMemcpyAsync(ws.codes, h_codes, (size_t)nsym * 2, cudaMemcpyHostToDevice, st)) != cudaSuccess)
         return e;
     if ((e = cudaMemsetAsync(ws.rank + n, 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
 
@@ -1488,8 +1503,8 @@ cudaError_t suffix_sort(const void *d_T, int symbytes, uint64_t n, bool gsa, Sor
     const int seed_end = K * bits;
     const int seed_passes = (seed_end + 7) / 8;
     const bool narrow = seed_end <= 32;   // 32-bit seed keys: less sort traffic
-    ws.pack_bits = gsa ? 0 : (bits <= 2 ? 2 : (bits <= 4 ? 4 : 0));
-    for (int c = 0, code = 0; c < nsym && code < 16; ++c)
+    ws.pack_bits = (gsa || raw) ? 0 : (bits <= 2 ? 2 : (bits <= 4 ? 4 : 0));
+    for (int c = 0, code = 0; !raw && c < nsym && code < 16; ++c)
         if (h_hist[c]) ws.decode[code++] = (uint16_t)c;
     const unsigned seed_grid = (unsigned)stream_grid((n + kSeedTile - 1) / kSeedTile * 256, 256);
     uint32_t *k32[2] = {reinterpret_cast<uint32_t *>(ws.keys[0]), reinterpret_cast<uint32_t *>(ws.keys[1])};
@@ -1505,6 +1520,16 @@ cudaError_t suffix_sort(const void *d_T, int symbytes, uint64_t n, bool gsa, Sor
             GSAIS_COUNTED((k_seed<uint8_t, uint64_t><<<seed_grid, 256, 0, st>>>(
                 T8, n, ws.codes, bits, K, gsa ? 1 : 0, ws.keys[0], ws.vals[0], seed_passes, seed_end, ws.radix.hist,
                 ws.pack_bits, ws.packed)));
+    } else if (raw) {
+        const uint32_t *T32 = static_cast<const uint32_t *>(d_T);
+        if (narrow)
+            GSAIS_COUNTED((k_seed<uint32_t, uint32_t><<<seed_grid, 256, 0, st>>>(
+                T32, n, ws.codes, bits, K, 0, k32[0], ws.vals[0], seed_passes, seed_end, ws.radix.hist, 0,
+                ws.packed)));
+        else
+            GSAIS_COUNTED((k_seed<uint32_t, uint64_t><<<seed_grid, 256, 0, st>>>(
+                T32, n, ws.codes, bits, K, 0, ws.keys[0], ws.vals[0], seed_passes, seed_end, ws.radix.hist, 0,
+                ws.packed)));
     } else {
         const uint16_t *T16 = static_cast<const uint16_t *>(d_T);
         if (narrow)

@@ -44,6 +44,7 @@ void sort_workspace_carve(SortWorkspace &ws, void *base, uint64_t n, int symbyte
 
 struct SortOptions {
     int seed_key_bits = 32;   // width of the packed seed prefix (32 or 64)
+    uint32_t raw_max = 0;     // 32-bit integer symbols: the largest symbol value
 };
 
 // Suffix array of the device text d_T (n symbols of `symbytes` bytes).  gsa

@@ -25,6 +25,11 @@
  *     `compute_plcp`, GSA variant :8215 `compute_plcp_gsa`) and LCP by
  *     gather (src/libsais.c:8311 `compute_lcp`).
  *   - symbol frequencies (src/libsais.c:1398-1427: freq[c] = count of c).
+ *   - PLCP of an integer string (src/libsais.c:8399 `libsais_plcp_int`,
+ *     :8263 `compute_plcp_int`): symbytes 4.
+ *   - inverse BWT (src/libsais.c:8030 `libsais_unbwt`): the text from U and
+ *     the primary index by the LF mapping, restated from the textbook
+ *     definition (not the reference's bigram decoder).
  *
  * Indices are int64 throughout so one code path serves the 32- and 64-bit
  * APIs; callers narrow.
@@ -250,7 +255,8 @@ void oracle_plcp(const void *T, int symbytes, const idx_t *SA, idx_t *PLCP, idx_
     if (n <= 0) return;
     idx_t k = n;
     for (idx_t i = 0; i < n; i++) { PLCP[SA[i]] = k; k = SA[i]; }
-    #define SYM(p) (symbytes == 1 ? (int32_t)((const uint8_t *)T)[p] : (int32_t)((const uint16_t *)T)[p])
+    #define SYM(p) (symbytes == 1 ? (int32_t)((const uint8_t *)T)[p] : \
+                    symbytes == 2 ? (int32_t)((const uint16_t *)T)[p] : ((const int32_t *)T)[p])
     idx_t l = 0;
     for (idx_t i = 0; i < n; i++) {
         idx_t j = PLCP[i];
@@ -264,6 +270,45 @@ void oracle_plcp(const void *T, int symbytes, const idx_t *SA, idx_t *PLCP, idx_
         l -= (l != 0);
     }
     #undef SYM
+}
+
+/*
+ * Inverse BWT.  Rows 0..n of the BWT matrix: row 0 is the empty suffix, row
+ * p (the primary index) has the sentinel as last symbol and is absent from U:
+ * L[r] = U[r] for r < p, U[r - 1] for r > p.  LF(r) = C[L[r]] + (occurrences
+ * of L[r] in L[0..r)), with C counting the sentinel.  Walking from row 0
+ * yields the text backwards: T[n-1-j] = L[LF^j(0)].
+ */
+int oracle_unbwt(const void *U, int symbytes, idx_t n, idx_t p, void *T)
+{
+    if (n <= 0) return 0;
+    if (p < 1 || p > n) return -1;
+    const idx_t k = symbytes == 1 ? 256 : 65536;
+    idx_t *C = calloc((size_t)k + 1, sizeof(idx_t));
+    idx_t *occ = calloc((size_t)k, sizeof(idx_t));
+    idx_t *lf = malloc((size_t)(n + 1) * sizeof(idx_t));
+    if (!C || !occ || !lf) { free(C); free(occ); free(lf); return -2; }
+    #define LSYM(r) (symbytes == 1 ? (idx_t)((const uint8_t *)U)[(r) < p ? (r) : (r) - 1] \
+                                   : (idx_t)((const uint16_t *)U)[(r) < p ? (r) : (r) - 1])
+    for (idx_t r = 0; r <= n; r++) if (r != p) C[LSYM(r) + 1]++;
+    C[0] = 1;   /* the sentinel row sorts first */
+    for (idx_t c = 1; c <= k; c++) C[c] += C[c - 1];
+    for (idx_t r = 0; r <= n; r++) {
+        if (r == p) { lf[r] = 0; continue; }
+        const idx_t c = LSYM(r);
+        lf[r] = C[c] + occ[c]++;
+    }
+    idx_t r = 0;
+    for (idx_t j = 0; j < n; j++) {
+        const idx_t c = LSYM(r);
+        if (symbytes == 1) ((uint8_t *)T)[n - 1 - j] = (uint8_t)c;
+        else ((uint16_t *)T)[n - 1 - j] = (uint16_t)c;
+        r = lf[r];
+        if (r == p && j + 1 < n) { free(C); free(occ); free(lf); return -1; }
+    }
+    #undef LSYM
+    free(C); free(occ); free(lf);
+    return 0;
 }
 
 /* LCP[i] = PLCP[SA[i]] (src/libsais.c:8311). */

@@ -51,7 +51,9 @@ def _symbytes(T: np.ndarray) -> int:
         return 1
     if T.dtype == np.uint16:
         return 2
-    raise TypeError("text must be uint8 or uint16")
+    if T.dtype == np.int32:
+        return 4
+    raise TypeError("text must be uint8, uint16 or int32")
 
 
 class Oracle:
@@ -77,6 +79,8 @@ class Oracle:
         lib.oracle_lcp.restype = None
         lib.oracle_check_sa.argtypes = [_p, ctypes.c_int, _p, _i64, ctypes.c_int]
         lib.oracle_check_sa.restype = ctypes.c_int
+        lib.oracle_unbwt.argtypes = [_p, ctypes.c_int, _i64, _i64, _p]
+        lib.oracle_unbwt.restype = ctypes.c_int
         self.lib = lib
 
     # -- primitives -----------------------------------------------------
@@ -92,6 +96,13 @@ class Oracle:
         SA = np.empty(max(T.size, 1), dtype=np.int64)[: T.size]
         rc = self.lib.oracle_sa_int(_ptr(T), _ptr(SA), T.size, k)
         return rc, SA
+
+    def sa_int_any(self, T: np.ndarray):
+        """SA of an integer string with arbitrary non-negative values: the values
+        are first replaced by their ranks (same order, so the same SA)."""
+        T = np.asarray(T)
+        vals, codes = np.unique(T, return_inverse=True)
+        return self.sa_int(codes.astype(np.int32), max(int(vals.size), 1))
 
     def gsa_valid(self, T: np.ndarray) -> bool:
         T = np.ascontiguousarray(T)
@@ -118,6 +129,13 @@ class Oracle:
         P = np.empty(max(T.size, 1), dtype=np.int64)[: T.size]
         self.lib.oracle_plcp(_ptr(T), _symbytes(T), _ptr(SA), _ptr(P), T.size, int(gsa))
         return P
+
+    def unbwt(self, U: np.ndarray, primary: int):
+        """(rc, T) from a BWT in libsais_bwt layout and its primary index."""
+        U = np.ascontiguousarray(U)
+        T = np.empty_like(U)
+        rc = self.lib.oracle_unbwt(_ptr(U), _symbytes(U), U.size, primary, _ptr(T))
+        return rc, T
 
     def lcp(self, PLCP: np.ndarray, SA: np.ndarray) -> np.ndarray:
         PLCP = np.ascontiguousarray(PLCP, dtype=np.int64)
@@ -201,7 +219,38 @@ class Reference:
             f.restype = _i64
         lib.libsais64_lcp.argtypes = [_p, _p, _p, _i64]
         lib.libsais64_lcp.restype = _i64
+        lib.libsais_int.argtypes = [_p, _p, _i32, _i32, _i32]
+        lib.libsais_int.restype = _i32
+        lib.libsais_plcp_int.argtypes = [_p, _p, _p, _i32]
+        lib.libsais_plcp_int.restype = _i32
+        lib.libsais_unbwt.argtypes = [_p, _p, _p, _i32, _p, _i32]
+        lib.libsais_unbwt.restype = _i32
+        lib.libsais16_unbwt.argtypes = [_p, _p, _p, _i32, _p, _i32]
+        lib.libsais16_unbwt.restype = _i32
         self.lib = lib
+
+    def libsais_int(self, T: np.ndarray, k: int):
+        """libsais_int on a copy of T (the reference permutes T while it works)."""
+        T = np.array(T, dtype=np.int32)
+        SA = np.empty(max(T.size, 1), dtype=np.int32)
+        rc = self.lib.libsais_int(_ptr(T), _ptr(SA), T.size, k, 0)
+        return int(rc), SA[: T.size]
+
+    def plcp_int(self, T: np.ndarray, SA: np.ndarray):
+        T = np.ascontiguousarray(T, dtype=np.int32)
+        SA = np.ascontiguousarray(SA, dtype=np.int32)
+        P = np.empty(max(T.size, 1), dtype=np.int32)
+        rc = self.lib.libsais_plcp_int(_ptr(T), _ptr(SA), _ptr(P), T.size)
+        return int(rc), P[: T.size]
+
+    def unbwt(self, U: np.ndarray, primary: int):
+        U = np.ascontiguousarray(U)
+        n = U.size
+        T = np.empty(max(n, 1), dtype=U.dtype)
+        A = np.empty(n + 1, dtype=np.int32)
+        f = self.lib.libsais16_unbwt if U.dtype == np.uint16 else self.lib.libsais_unbwt
+        rc = f(_ptr(U), _ptr(T), _ptr(A), n, None, primary)
+        return int(rc), T[:n]
 
     def libsais(self, T: np.ndarray, gsa: bool = False, threads: int = 1):
         T = np.ascontiguousarray(T)

@@ -46,7 +46,8 @@ def test_python_mirror_covers_headers():
 
 
 def test_header_compiles_as_c():
-    src = "#include <libsais.h>\n#include <libsais64.h>\n#include <libsais16.h>\n#include <libsais_gb300.h>\nint main(void){return 0;}\n"
+    src = ("#include <libsais.h>\n#include <libsais64.h>\n#include <libsais16.h>\n#include <libsais16x64.h>\n"
+           "#include <libsais_gb300.h>\nint main(void){return 0;}\n")
     r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I", INCLUDE, "-x", "c", "-", "-o", "/dev/null"],
                        input=src, text=True, capture_output=True)
     assert r.returncode == 0, r.stderr
@@ -118,3 +119,55 @@ def test_contexts_create_and_free(lib):
     c16 = lib.libsais16_create_ctx_omp(0)
     assert c16
     lib.libsais16_free_ctx(c16)
+
+
+def test_new_families_host_checks(lib):
+    """Integer alphabets, inverse BWT and 16x64: the reference's argument checks
+    and n <= 1 cases (src/libsais.c:7050, :8040, :8399; src/libsais64.c:7118,
+    :8039; src/libsais16x64.c:7036, :7789), all answered on the host."""
+    p = lambda a: a.ctypes.data
+    Ti = np.array([3, 1, 2], np.int32)
+    SA = np.full(4, 77, np.int32)
+    assert lib.libsais_int(None, p(SA), 3, 4, 0) == -1
+    assert lib.libsais_int(p(Ti), p(SA), -1, 4, 0) == -1
+    assert lib.libsais_int(p(Ti), p(SA), 3, 4, -1) == -1
+    assert lib.libsais_int_omp(p(Ti), p(SA), 3, 4, 0, -1) == -1
+    assert lib.libsais_int(p(Ti), p(SA), 1, 4, 0) == 0 and SA[0] == 0
+    assert lib.libsais16_int(p(Ti), p(SA), 0, 4, 0) == 0
+    S64 = np.full(2, 5, np.int64)
+    T64 = np.array([9], np.int64)
+    assert lib.libsais64_long(p(T64), p(S64), 1, 10, 0) == 0 and S64[0] == 0
+    assert lib.libsais64_long(p(T64), None, 1, 10, 0) == -1
+    assert lib.libsais16x64_long_omp(p(T64), p(S64), 1, 10, 0, -2) == -1
+    P = np.full(2, 9, np.int32)
+    assert lib.libsais_plcp_int(p(Ti), p(SA), p(P), 1) == 0 and P[0] == 0
+    assert lib.libsais_plcp_int(p(Ti), None, p(P), 3) == -1
+    # inverse BWT
+    U = np.array([65, 66, 67, 68], np.uint8)
+    O = np.zeros(4, np.uint8)
+    A = np.zeros(5, np.int32)
+    I = np.array([2, 3], np.int32)
+    assert lib.libsais_unbwt(p(U), p(O), None, 4, None, 1) == -1            # A NULL
+    assert lib.libsais_unbwt(p(U), p(O), p(A), 4, None, 0) == -1            # primary <= 0
+    assert lib.libsais_unbwt(p(U), p(O), p(A), 4, None, 5) == -1            # primary > n
+    assert lib.libsais_unbwt_aux(p(U), p(O), p(A), 4, None, 3, p(I)) == -1  # r not a power of two
+    assert lib.libsais_unbwt_aux(p(U), p(O), p(A), 4, None, 2, None) == -1
+    bad = np.array([2, 0], np.int32)
+    assert lib.libsais_unbwt_aux(p(U), p(O), p(A), 4, None, 2, p(bad)) == -1
+    assert lib.libsais_unbwt_omp(p(U), p(O), p(A), 4, None, 1, -1) == -1
+    assert lib.libsais_unbwt(p(U), p(O), p(A), 1, None, 1) == 0 and O[0] == 65
+    assert lib.libsais_unbwt(p(U), p(O), p(A), 1, None, 0) == -1            # n = 1 needs primary 1
+    assert lib.libsais_unbwt(p(U), p(O), p(A), 0, None, 0) == 0
+    c = lib.libsais_unbwt_create_ctx()
+    assert c
+    assert lib.libsais_unbwt_ctx(c, p(U), p(O), p(A), 4, None, 7) == -1
+    lib.libsais_unbwt_free_ctx(c)
+    assert lib.libsais_unbwt_create_ctx_omp(-1) is None
+    A64 = np.zeros(5, np.int64)
+    assert lib.libsais64_unbwt(p(U), p(O), p(A64), 4, None, 9) == -1
+    U16 = np.array([500], np.uint16)
+    O16 = np.zeros(1, np.uint16)
+    assert lib.libsais16x64_unbwt(p(U16), p(O16), p(A64), 1, None, 1) == 0 and O16[0] == 500
+    S16 = np.full(1, 3, np.int64)
+    F = np.zeros(65536, np.int64)
+    assert lib.libsais16x64(p(U16), p(S16), 1, 0, p(F)) == 0 and S16[0] == 0 and F[500] == 1

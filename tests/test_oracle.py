@@ -109,3 +109,69 @@ def test_oracle_matches_reference_random():
         assert np.array_equal(O.plcp(T, SA), P.astype(np.int64))
     T = (rng.integers(0, 4, 1 << 20) + 65).astype(np.uint8)
     assert np.array_equal(O.sa(T)[1], R.libsais(T)[1].astype(np.int64))
+
+
+def test_oracle_unbwt_round_trip(oracle):
+    """Inverse BWT restatement: BWT -> text on random and structured texts,
+    8- and 16-bit, including a primary index that is not a row of the text
+    (the walk must notice)."""
+    rng = np.random.default_rng(21)
+    texts = [np.frombuffer(b"banana", np.uint8).copy(), np.full(50, 65, np.uint8),
+             np.tile(np.frombuffer(b"ACGTACG", np.uint8), 30)]
+    for _ in range(300):
+        n = int(rng.integers(2, 300))
+        k = int(rng.integers(1, 6))
+        texts.append((rng.integers(0, k, n) + 65).astype(np.uint8))
+    for _ in range(50):
+        n = int(rng.integers(2, 300))
+        texts.append(rng.integers(0, 70000 % 65536, n).astype(np.uint16))
+    for T in texts:
+        p, U, _, _ = oracle.libsais_bwt(T)
+        rc, back = oracle.unbwt(U, p)
+        assert rc == 0 and np.array_equal(back, T)
+    assert oracle.unbwt(np.frombuffer(b"abc", np.uint8).copy(), 0)[0] == -1
+
+
+def test_oracle_plcp_int(oracle):
+    rng = np.random.default_rng(22)
+    for _ in range(100):
+        n = int(rng.integers(2, 200))
+        k = int(rng.integers(1, 1 << 20))
+        T = rng.integers(0, k, n).astype(np.int32)
+        _, SA = oracle.sa_int(T, k)
+        P = oracle.plcp(T, SA)
+        SAi = [tuple(T[i:]) for i in SA]
+        for j in range(n):
+            prev = SA[j - 1] if j else None
+            want = 0
+            if prev is not None:
+                a, b = T[SA[j]:], T[prev:]
+                while want < min(len(a), len(b)) and a[want] == b[want]:
+                    want += 1
+            assert P[SA[j]] == want
+        assert SAi == sorted(SAi)
+
+
+@pytest.mark.skipif(not os.path.exists(REF), reason="reference not compiled here")
+def test_oracle_new_families_match_reference():
+    """libsais_int, libsais_plcp_int and libsais_unbwt/libsais16_unbwt of the
+    compiled reference against the restatement."""
+    from oracle.oracle import Oracle, Reference
+    O, R = Oracle(), Reference()
+    rng = np.random.default_rng(23)
+    for _ in range(200):
+        n = int(rng.integers(2, 500))
+        k = int(rng.choice([2, 5, 300, 70000]))
+        T = rng.integers(0, k, n).astype(np.int32)
+        rc, SA = R.libsais_int(T, k)
+        assert rc == 0 and np.array_equal(O.sa_int(T, k)[1], SA.astype(np.int64))
+        rc, P = R.plcp_int(T, SA)
+        assert rc == 0 and np.array_equal(O.plcp(T, SA), P.astype(np.int64))
+    for _ in range(200):
+        n = int(rng.integers(2, 500))
+        sixteen = rng.random() < 0.3
+        T = rng.integers(0, 40000 if sixteen else 4, n).astype(np.uint16 if sixteen else np.uint8)
+        p, U, _, _ = O.libsais_bwt(T)
+        rc, back = R.unbwt(U, p)
+        assert rc == 0 and np.array_equal(back, T)
+        assert np.array_equal(O.unbwt(U, p)[1], back)
