@@ -379,6 +379,45 @@ def run_plcp_lcp(G, torch, dT, dSA, n: int):
             "lcp_mb_s": round(n / 1e6 / (lcp_ms / 1e3), 1), "lcp_ms": round(lcp_ms, 3)}
 
 
+def run_unbwt(G, U: np.ndarray, primary: int, T: np.ndarray, steps: int = 3, cpu_sample: int = 1 << 24):
+    """Inverse BWT of the workload's BWT through libsais_unbwt (host buffers:
+    the BWT goes up and the text comes back inside the timed call), the
+    device part from the library's CUDA events, and the oracle's LF walk on a
+    prefix-sized sample for scale."""
+    import time as _t
+    out = np.empty_like(U)
+    rc, _ = G.libsais_unbwt(U, primary, out=out)
+    if rc != 0 or not np.array_equal(out, T):
+        raise SystemExit(f"libsais_unbwt did not give the text back: {rc}")
+    G.profile_reset()
+    G.profile_enable(True)
+    t0 = _t.perf_counter()
+    for _ in range(steps):
+        G.libsais_unbwt(U, primary, out=out)
+    host_s = (_t.perf_counter() - t0) / steps
+    G.profile_enable(False)
+    dev = G.profile_read().get("unbwt", {"launches": 0, "total_ms": 0.0})
+    dev_ms = dev["total_ms"] / max(dev["launches"], 1)
+    n = U.size
+    res = {"n": n, "e2e_mb_s": round(n / 1e6 / host_s, 1), "e2e_ms": round(host_s * 1e3, 3),
+           "device_mb_s": round(n / 1e6 / (dev_ms / 1e3), 1) if dev_ms else None, "device_ms": round(dev_ms, 3),
+           "round_trip_identical": True}
+    try:
+        from oracle.oracle import Oracle
+        O = Oracle()
+        m = min(cpu_sample, n)
+        Ts = T[:m]
+        p, Us, _, _ = O.libsais_bwt(Ts)
+        t0 = _t.perf_counter()
+        O.unbwt(Us, p)
+        res["cpu_port_mb_s"] = round(m / 1e6 / (_t.perf_counter() - t0), 1)
+        res["cpu_sample"] = f"first {m} symbols, LF walk, 1 thread"
+    except Exception as exc:   # the oracle is a reported scale only
+        res["cpu_port_mb_s"] = None
+        res["cpu_note"] = str(exc)[:80]
+    return res
+
+
 def run_gsa(G, torch, reads: int = 1 << 20):
     """Generalized SA + GSA-PLCP + LCP of the read set: 2^20 reads of length
     N(150, 20) clipped to [50, 300] from a 4 Mbp reference with 1% substitutions,
@@ -528,6 +567,7 @@ def main():
     extras = {}
     if rank == 0 and world == 1 and not args.no_extras:
         extras["plcp_lcp"] = run_plcp_lcp(G, torch, dT, dSA, n)
+        extras["unbwt"] = run_unbwt(G, dU.cpu().numpy(), prim, T)
         G.release_workspace()
         extras["gsa"] = run_gsa(G, torch)
         G.release_workspace()

@@ -712,7 +712,7 @@ int32_t gsais_profile_read(void *ctx, gsais_kernel_profile *out, int32_t max_kin
     std::lock_guard<std::mutex> lock(c->mu);
     static const char *names[KK_COUNT] = {"radix_pass",   "tile_counts", "upsweep",      "seed",
                                           "round_keys",   "tile_summary", "assign",      "small_groups",
-                                          "pair_compare"};
+                                          "pair_compare", "unbwt"};
     int k = 0;
     for (; k < KK_COUNT && k < max_kinds; ++k) {
         out[k].name = names[k];

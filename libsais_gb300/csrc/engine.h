@@ -16,7 +16,7 @@ extern std::atomic<uint64_t> g_launches;
 // Optional per-kernel timing: CUDA events recorded on the launching stream
 // around each launch of the instrumented kernels, resolved after the stream
 // synchronises.  `bytes` is the algorithmic traffic of the launch.
-enum KernelKind { KK_RADIX_PASS = 0, KK_TILE_COUNTS, KK_UPSWEEP, KK_SEED, KK_ROUND_KEYS, KK_SUMMARY, KK_ASSIGN, KK_SMALL, KK_PAIRS, KK_COUNT };
+enum KernelKind { KK_RADIX_PASS = 0, KK_TILE_COUNTS, KK_UPSWEEP, KK_SEED, KK_ROUND_KEYS, KK_SUMMARY, KK_ASSIGN, KK_SMALL, KK_PAIRS, KK_UNBWT, KK_COUNT };
 
 struct KernelProfiler {
     bool enabled = false;

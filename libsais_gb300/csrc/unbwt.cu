@@ -199,6 +199,7 @@ cudaError_t unbwt_run(const void *d_U, int symbytes, uint64_t n, uint64_t p, voi
     rs.h_hist = h_hist;
     rs.prof = prof;
 
+    cudaEvent_t ev = prof ? prof->begin(st) : nullptr;
     const int g = unbwt_grid(n);
     if (symbytes == 1)
         GSAIS_COUNTED((k_unbwt_keys<uint8_t><<<g, 256, 0, st>>>(static_cast<const uint8_t *>(d_U), n, p, keys[0],
@@ -224,6 +225,8 @@ cudaError_t unbwt_run(const void *d_U, int symbytes, uint64_t n, uint64_t p, voi
     else
         GSAIS_COUNTED((k_unbwt_emit<uint16_t><<<gm, 256, 0, st>>>(PF, n, sp, N[cur], D[cur], len,
                                                                    static_cast<uint16_t *>(d_out), d_err)));
+    // bytes: BWT read, text written (the walks' random reads are not counted)
+    if (ev) prof->end(KK_UNBWT, ev, st, 2 * n * symbytes);
     return cudaGetLastError();
 }
 
