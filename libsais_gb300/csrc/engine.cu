@@ -386,6 +386,7 @@ int64_t gsais_run_unbwt(gsais_ctx *c, const void *T, int symbytes, int64_t n_, i
     GS_TRY(unbwt_run(d_in, symbytes, n, (uint64_t)primary, d_out, cv.p, c->h_hist, &c->prof, c->d_misc, st));
     GS_TRY(cudaMemcpyAsync(U, d_out, n * symbytes, cudaMemcpyDeviceToHost, st));
     GS_TRY(sync_checked(c, st));
+    c->prof.flush();
     return 0;
 }
 

@@ -35,29 +35,41 @@ __global__ void __launch_bounds__(256) k_bwt(const Sym *__restrict__ T, const ui
                                              const uint32_t *__restrict__ isa1, Sym *__restrict__ U, PackedText pk,
                                              uint32_t *__restrict__ err)
 {
+    constexpr int B = 8;   // rows per thread per step: all SA loads, then all gathers
     __shared__ Sym dec[16];
     if (threadIdx.x < 16) dec[threadIdx.x] = (Sym)pk.decode[threadIdx.x];
     __syncthreads();
     const uint64_t i0 = (uint64_t)isa1[0] - 1;   // SA row of suffix 0
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
-        if (k == 0) {
-            U[0] = T[n - 1];
-        } else {
+    const uint64_t span = (uint64_t)gridDim.x * blockDim.x * B;
+    for (uint64_t k0 = (uint64_t)blockIdx.x * blockDim.x * B + threadIdx.x; k0 < n; k0 += span) {
+        uint32_t p[B];
+#pragma unroll
+        for (int j = 0; j < B; ++j) {
+            const uint64_t k = k0 + (uint64_t)j * blockDim.x;
             const uint64_t row = k <= i0 ? k - 1 : k;
-            const uint64_t p = row < n ? SA[row] : 0;
-            if (p == 0 || p > n) {
+            p[j] = (k > 0 && k < n && row < n) ? SA[row] : 0u;
+        }
+#pragma unroll
+        for (int j = 0; j < B; ++j) {
+            const uint64_t k = k0 + (uint64_t)j * blockDim.x;
+            if (k >= n) break;
+            if (k == 0) {
+                U[0] = T[n - 1];
+                continue;
+            }
+            const uint64_t q = p[j];
+            if (q == 0 || q > n) {
                 atomicOr(err, GSAIS_ERR_BOUNDS);
                 continue;
             }
             if (pk.pack_bits == 2) {
-                const uint32_t w = reinterpret_cast<const uint16_t *>(pk.packed)[(p - 1) >> 3];
-                U[k] = dec[(w >> (2 * ((p - 1) & 7))) & 3u];
+                const uint32_t w = reinterpret_cast<const uint16_t *>(pk.packed)[(q - 1) >> 3];
+                U[k] = dec[(w >> (2 * ((q - 1) & 7))) & 3u];
             } else if (pk.pack_bits == 4) {
-                const uint32_t w = reinterpret_cast<const uint32_t *>(pk.packed)[(p - 1) >> 3];
-                U[k] = dec[(w >> (4 * ((p - 1) & 7))) & 15u];
+                const uint32_t w = reinterpret_cast<const uint32_t *>(pk.packed)[(q - 1) >> 3];
+                U[k] = dec[(w >> (4 * ((q - 1) & 7))) & 15u];
             } else {
-                U[k] = T[p - 1];
+                U[k] = T[q - 1];
             }
         }
     }
@@ -276,10 +288,10 @@ cudaError_t bwt_gather(const void *d_T, int symbytes, const uint32_t *d_SA, cons
 {
     if (n == 0) return cudaSuccess;
     if (symbytes == 1)
-        GSAIS_COUNTED((k_bwt<uint8_t><<<grid_for(n, 256), 256, 0, st>>>(
+        GSAIS_COUNTED((k_bwt<uint8_t><<<grid_for((n + 7) / 8, 256), 256, 0, st>>>(
             static_cast<const uint8_t *>(d_T), d_SA, n, d_isa1, static_cast<uint8_t *>(d_U), pk, err)));
     else
-        GSAIS_COUNTED((k_bwt<uint16_t><<<grid_for(n, 256), 256, 0, st>>>(
+        GSAIS_COUNTED((k_bwt<uint16_t><<<grid_for((n + 7) / 8, 256), 256, 0, st>>>(
             static_cast<const uint16_t *>(d_T), d_SA, n, d_isa1, static_cast<uint16_t *>(d_U), pk, err)));
     return cudaGetLastError();
 }

@@ -202,11 +202,25 @@ __device__ __forceinline__ uint32_t stage_tile(const TileArgs &a, uint64_t base,
                                                bool need_vals)
 {
     const uint32_t valid = (uint32_t)((a.N - base) < (uint64_t)kAssignTile ? (a.N - base) : (uint64_t)kAssignTile);
-    for (int x = threadIdx.x; x < (int)valid + 2; x += blockDim.x) {
+    // every load of the tile is issued before the first shared store
+    constexpr int SP = (kAssignTile + 2 + kAssignThreads - 1) / kAssignThreads;
+    uint64_t kv[SP];
+    uint32_t vv[SP];
+#pragma unroll
+    for (int q = 0; q < SP; ++q) {
+        const int x = (int)threadIdx.x + q * kAssignThreads;
         const int64_t j = (int64_t)base + x - 1;
-        const bool in = j >= 0 && (uint64_t)j < a.N;
-        s_keys[x] = in ? (a.keys32 ? (uint64_t)a.keys32[j] : a.keys[j]) : 0ull;
-        if (need_vals) s_vals[x] = in ? a.vals[j] : 0u;
+        const bool in = x < (int)valid + 2 && j >= 0 && (uint64_t)j < a.N;
+        kv[q] = in ? (a.keys32 ? (uint64_t)a.keys32[j] : a.keys[j]) : 0ull;
+        vv[q] = (in && need_vals) ? a.vals[j] : 0u;
+    }
+#pragma unroll
+    for (int q = 0; q < SP; ++q) {
+        const int x = (int)threadIdx.x + q * kAssignThreads;
+        if (x < (int)valid + 2) {
+            s_keys[x] = kv[q];
+            if (need_vals) s_vals[x] = vv[q];
+        }
     }
     __syncthreads();
     return valid;
@@ -565,31 +579,48 @@ __global__ void __launch_bounds__(256) k_round_r2(const uint32_t *__restrict__ a
     __shared__ uint32_t sh[kMaxRadixPasses][256];
     radix_hist_zero(sh, passes);
     __syncthreads();
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    // B entries per thread per step: the list loads, then the dependent
+    // gathers (rank[i+h], the group's class), then the writes
+    constexpr int B = 4;
+    const uint64_t span = (uint64_t)gridDim.x * blockDim.x * B;
     const uint64_t N_round = (N + 31) & ~31ull;   // whole warps iterate together
-    for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < N_round; j += stride) {
-        bool large = false;
-        uint64_t key = 0;
-        if (j < N) {
-            const uint64_t i = act_i[j];
-            // an active suffix has length >= h, so i + h <= n (rank[n] is the sentinel)
-            uint32_t r2 = 0;
-            if (i + h <= n) r2 = rank[i + h];
-            else atomicOr(err, GSAIS_ERR_BOUNDS);
-            const uint32_t g = act_gid[j];
-            const uint32_t L = lid[g];
-            if (L >= kMedium) {   // small or medium group: keep rank[i+h] by list position
-                r2o[j] = r2;
-            } else {
-                large = true;
-                const uint64_t d = (uint64_t)loff[g] + (j - gstart[g]);
-                key = ((uint64_t)L << b2) | r2;
-                lkeys[d] = key;
-                lvals[d] = (uint32_t)i;
-                lpos[d] = act_pos[j];
-            }
+    for (uint64_t j0 = (uint64_t)blockIdx.x * blockDim.x * B + threadIdx.x; j0 < N_round; j0 += span) {
+        uint32_t iv[B], gv[B], r2v[B], Lv[B];
+#pragma unroll
+        for (int b = 0; b < B; ++b) {
+            const uint64_t j = j0 + (uint64_t)b * blockDim.x;
+            iv[b] = j < N ? act_i[j] : 0u;
+            gv[b] = j < N ? act_gid[j] : 0u;
         }
-        radix_hist_add(sh, key, large, passes, end_bit);
+#pragma unroll
+        for (int b = 0; b < B; ++b) {
+            const uint64_t j = j0 + (uint64_t)b * blockDim.x;
+            // an active suffix has length >= h, so i + h <= n (rank[n] is the sentinel)
+            const bool ok = j < N && (uint64_t)iv[b] + h <= n;
+            r2v[b] = ok ? rank[iv[b] + h] : 0u;
+            Lv[b] = j < N ? lid[gv[b]] : kNoLarge;
+            if (j < N && !ok) atomicOr(err, GSAIS_ERR_BOUNDS);
+        }
+#pragma unroll
+        for (int b = 0; b < B; ++b) {
+            const uint64_t j = j0 + (uint64_t)b * blockDim.x;
+            bool large = false;
+            uint64_t key = 0;
+            if (j < N) {
+                const uint32_t g = gv[b], L = Lv[b];
+                if (L >= kMedium) {   // small or medium group: keep rank[i+h] by list position
+                    r2o[j] = r2v[b];
+                } else {
+                    large = true;
+                    const uint64_t d = (uint64_t)loff[g] + (j - gstart[g]);
+                    key = ((uint64_t)L << b2) | r2v[b];
+                    lkeys[d] = key;
+                    lvals[d] = iv[b];
+                    lpos[d] = act_pos[j];
+                }
+            }
+            radix_hist_add(sh, key, large, passes, end_bit);
+        }
     }
     __syncthreads();
     radix_hist_flush(sh, passes, hist);
@@ -1112,13 +1143,16 @@ __global__ void __launch_bounds__(256) k_perm_partition(const uint32_t *__restri
     uint32_t p[kPermItems], r[kPermItems];
     uint16_t slot[kPermItems];
     bool bad = false;
+    // all loads of the tile first, then the shared-memory slot counters
 #pragma unroll
     for (int k = 0; k < kPermItems; ++k) {
         const uint32_t i = k * 256 + tid;
-        p[k] = 0xFFFFFFFFu;
-        if (i < valid) {
-            p[k] = in_pos[t0 + i];
-            r[k] = in_r[t0 + i];
+        p[k] = i < valid ? in_pos[t0 + i] : 0xFFFFFFFFu;
+        r[k] = i < valid ? in_r[t0 + i] : 0u;
+    }
+#pragma unroll
+    for (int k = 0; k < kPermItems; ++k) {
+        if (p[k] != 0xFFFFFFFFu) {
             const uint32_t ld = (p[k] >> shift) - lbase;
             if (ld < RANGE) {
                 slot[k] = (uint16_t)atomicAdd(&s_cnt[ld], 1u);
