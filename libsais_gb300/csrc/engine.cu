@@ -40,7 +40,7 @@ struct gsais_ctx {
 namespace {
 
 constexpr size_t kAlign = 256;
-constexpr size_t kSmallWords = 16 + 65536 + 32768;
+constexpr size_t kSmallWords = kHostSmallWords;
 constexpr uint64_t kMaxN = 0xFFFFFFFFull;   // 32-bit internal indices
 
 inline size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }

@@ -40,7 +40,7 @@ constexpr int kMaxDevices = 64;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
 // Host-side read-back buffers (ordinary static storage, no allocation).
-alignas(16) static uint32_t g_host_small[16 + 65536 + 32768];
+alignas(16) static uint32_t g_host_small[kHostSmallWords];
 alignas(16) static uint32_t g_host_hist[8 * 256];
 static uint32_t g_host_flag[4];
 

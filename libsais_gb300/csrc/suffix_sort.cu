@@ -185,6 +185,8 @@ struct TileArgs {
     const uint32_t *vals;
     const uint32_t *pos;     // nullptr: identity (the seed round)
     uint32_t *rank_out;      // non-null: new ranks go here by list position (scattered later)
+    uint32_t *pairs;         // non-null (seed round, plain texts): groups of exactly two leave
+    unsigned long long *pair_count;   //   the list; their first slot is appended here
     uint64_t N;              // entries in this round
     uint64_t n;              // text length
     uint32_t K;              // seed symbols per key
@@ -196,28 +198,32 @@ __device__ __forceinline__ bool has_zero_field(uint64_t x, uint64_t lo, uint64_t
     return ((x - lo) & ~x & hi) != 0;
 }
 
-// Stage keys/vals[base-1 .. base+valid] into shared memory (one halo entry
-// on each side) and return the number of valid entries.
+// Entries staged on each side of a tile: head tests look one entry back, the
+// two-member group test two entries ahead and behind.
+constexpr int kHalo = 2;
+
+// Stage keys/vals[base-kHalo .. base+valid+kHalo) into shared memory and
+// return the number of valid entries.
 __device__ __forceinline__ uint32_t stage_tile(const TileArgs &a, uint64_t base, uint64_t *s_keys, uint32_t *s_vals,
                                                bool need_vals)
 {
     const uint32_t valid = (uint32_t)((a.N - base) < (uint64_t)kAssignTile ? (a.N - base) : (uint64_t)kAssignTile);
     // every load of the tile is issued before the first shared store
-    constexpr int SP = (kAssignTile + 2 + kAssignThreads - 1) / kAssignThreads;
+    constexpr int SP = (kAssignTile + 2 * kHalo + kAssignThreads - 1) / kAssignThreads;
     uint64_t kv[SP];
     uint32_t vv[SP];
 #pragma unroll
     for (int q = 0; q < SP; ++q) {
         const int x = (int)threadIdx.x + q * kAssignThreads;
-        const int64_t j = (int64_t)base + x - 1;
-        const bool in = x < (int)valid + 2 && j >= 0 && (uint64_t)j < a.N;
+        const int64_t j = (int64_t)base + x - kHalo;
+        const bool in = x < (int)valid + 2 * kHalo && j >= 0 && (uint64_t)j < a.N;
         kv[q] = in ? (a.keys32 ? (uint64_t)a.keys32[j] : a.keys[j]) : 0ull;
         vv[q] = (in && need_vals) ? a.vals[j] : 0u;
     }
 #pragma unroll
     for (int q = 0; q < SP; ++q) {
         const int x = (int)threadIdx.x + q * kAssignThreads;
-        if (x < (int)valid + 2) {
+        if (x < (int)valid + 2 * kHalo) {
             s_keys[x] = kv[q];
             if (need_vals) s_vals[x] = vv[q];
         }
@@ -231,7 +237,7 @@ template <int MODE>
 __device__ __forceinline__ bool head_at(const TileArgs &a, uint64_t base, int l, const uint64_t *s_keys,
                                         const uint32_t *s_vals)
 {
-    const uint64_t j = base + (uint64_t)l - 1;
+    const uint64_t j = base + (uint64_t)l - kHalo;
     if (j == 0 || j >= a.N) return true;
     const uint64_t k = s_keys[l], kp = s_keys[l - 1];
     if (k != kp) return true;
@@ -251,45 +257,67 @@ struct ElemFlags {
     uint32_t kept;  // 1 if the entry stays active
     uint32_t kh;    // 1 if the entry starts a group that stays active
     bool single;
+    bool pair;      // member of a group of exactly two taken out for direct comparison
+    bool pair_first;
 };
 
+// s_head[l] = head_at(l) for every staged index l >= 1, computed once per tile.
 template <int MODE>
-__device__ __forceinline__ ElemFlags elem_flags(const TileArgs &a, uint64_t base, int x, const uint64_t *s_keys,
-                                                const uint32_t *s_vals, uint32_t pos)
+__device__ __forceinline__ void stage_heads(const TileArgs &a, uint64_t base, uint32_t valid, const uint64_t *s_keys,
+                                            const uint32_t *s_vals, uint8_t *s_head)
+{
+    for (int l = threadIdx.x; l < (int)valid + 2 * kHalo; l += blockDim.x)
+        s_head[l] = l == 0 ? 1 : (uint8_t)head_at<MODE>(a, base, l, s_keys, s_vals);
+    __syncthreads();
+}
+
+template <int MODE>
+__device__ __forceinline__ ElemFlags elem_flags(const TileArgs &a, int x, const uint8_t *s_head, uint32_t pos)
 {
     ElemFlags f;
-    const bool head = head_at<MODE>(a, base, x + 1, s_keys, s_vals);
-    const bool last = head_at<MODE>(a, base, x + 2, s_keys, s_vals);
+    const bool head = s_head[x + kHalo];
+    const bool last = s_head[x + kHalo + 1];
     f.single = head && last;
+    f.pair = f.pair_first = false;
+    if (MODE == MODE_INIT_PLAIN && a.pairs && !f.single) {
+        // first of two: next entry is not a head, the one after it is;
+        // second of two: the previous entry is a head and the next one too
+        f.pair_first = head && s_head[x + kHalo + 2];
+        f.pair = f.pair_first || (last && s_head[x + kHalo - 1]);
+    }
     f.hv = head ? pos + 1 : 0u;
-    f.kept = f.single ? 0u : 1u;
-    f.kh = (head && !f.single) ? 1u : 0u;
+    f.kept = (f.single || f.pair) ? 0u : 1u;
+    f.kh = (head && f.kept) ? 1u : 0u;
     return f;
 }
 
-// Per-tile reduction: max group-start value, kept entries, kept groups.
+// Per-tile reduction: max group-start value, kept entries, kept groups,
+// two-member groups taken out of the list (seed round).
 // Bytes per entry: key 8 (+ value 4 and pos 4 when used).
 template <int MODE>
 __global__ void __launch_bounds__(kAssignThreads) k_tile_summary(TileArgs a, uint32_t *__restrict__ info)
 {
-    __shared__ uint64_t s_keys[kAssignTile + 2];
-    __shared__ uint32_t s_vals[kAssignTile + 2];
-    __shared__ uint32_t s_red[3][kAssignWarps];
+    __shared__ uint64_t s_keys[kAssignTile + 2 * kHalo];
+    __shared__ uint32_t s_vals[kAssignTile + 2 * kHalo];
+    __shared__ uint32_t s_red[4][kAssignWarps];
     __shared__ int s_redx[kAssignWarps];
     const uint64_t base = (uint64_t)blockIdx.x * kAssignTile;
+    __shared__ uint8_t s_head[kAssignTile + 2 * kHalo];
     const uint32_t valid = stage_tile(a, base, s_keys, s_vals, MODE == MODE_INIT_PLAIN);
-    uint32_t mx = 0, kept = 0, kh = 0;   // mx: value of the last head (highest index) of the tile
+    stage_heads<MODE>(a, base, valid, s_keys, s_vals, s_head);
+    uint32_t mx = 0, kept = 0, kh = 0, np = 0;   // mx: value of the last head (highest index) of the tile
     int mxx = -1;
     for (int x = threadIdx.x; x < (int)valid; x += blockDim.x) {
         const uint64_t j = base + x;
         const uint32_t pos = a.pos ? a.pos[j] : (uint32_t)j;
-        const ElemFlags f = elem_flags<MODE>(a, base, x, s_keys, s_vals, pos);
+        const ElemFlags f = elem_flags<MODE>(a, x, s_head, pos);
         if (f.hv) {
             mx = f.hv;
             mxx = x;
         }
         kept += f.kept;
         kh += f.kh;
+        np += f.pair_first ? 1u : 0u;
     }
     for (int o = 16; o > 0; o >>= 1) {
         const uint32_t m2 = __shfl_down_sync(GSAIS_FULL_MASK, mx, o);
@@ -300,12 +328,13 @@ __global__ void __launch_bounds__(kAssignThreads) k_tile_summary(TileArgs a, uin
         }
         kept += __shfl_down_sync(GSAIS_FULL_MASK, kept, o);
         kh += __shfl_down_sync(GSAIS_FULL_MASK, kh, o);
+        np += __shfl_down_sync(GSAIS_FULL_MASK, np, o);
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) { s_red[0][warp] = mx; s_red[1][warp] = kept; s_red[2][warp] = kh; s_redx[warp] = mxx; }
+    if (lane == 0) { s_red[0][warp] = mx; s_red[1][warp] = kept; s_red[2][warp] = kh; s_red[3][warp] = np; s_redx[warp] = mxx; }
     __syncthreads();
     if (threadIdx.x == 0) {
-        uint32_t M = 0, A = 0, B = 0;
+        uint32_t M = 0, A = 0, B = 0, C = 0;
         int MX = -1;
         for (int w = 0; w < kAssignWarps; ++w) {
             if (s_redx[w] > MX) {
@@ -314,80 +343,97 @@ __global__ void __launch_bounds__(kAssignThreads) k_tile_summary(TileArgs a, uin
             }
             A += s_red[1][w];
             B += s_red[2][w];
+            C += s_red[3][w];
         }
-        info[3 * blockIdx.x + 0] = M;
-        info[3 * blockIdx.x + 1] = A;
-        info[3 * blockIdx.x + 2] = B;
+        info[4 * blockIdx.x + 0] = M;
+        info[4 * blockIdx.x + 1] = A;
+        info[4 * blockIdx.x + 2] = B;
+        info[4 * blockIdx.x + 3] = C;
     }
 }
 
-// Exclusive scan of the tile summaries (single CTA): carry[t] = (max, sum, sum)
-// over tiles < t; totals[0] = kept entries, totals[1] = kept groups.
+// Exclusive scan of the tile summaries (single CTA): carry[t] = (max, sum,
+// sum, sum) over tiles < t; totals[0] = kept entries, totals[1] = kept
+// groups; *pair_total (nullable) = two-member groups taken out.
 // `base` (nullable) = (groups << 32 | entries) already emitted by the
 // small-group path of the same round; survivors and groups follow them.
 __global__ void __launch_bounds__(1024) k_tile_scan(const uint32_t *__restrict__ info, uint32_t *__restrict__ carry,
                                                     uint64_t tiles, uint32_t *__restrict__ totals,
-                                                    const unsigned long long *__restrict__ base)
+                                                    const unsigned long long *__restrict__ base,
+                                                    unsigned long long *__restrict__ pair_total)
 {
-    __shared__ uint32_t wb[3][33];
+    __shared__ uint32_t wb[4][33];
     const unsigned long long b0 = base ? *base : 0ull;
-    uint32_t cm = 0, ck = (uint32_t)b0, ch = (uint32_t)(b0 >> 32);
+    uint32_t cm = 0, ck = (uint32_t)b0, ch = (uint32_t)(b0 >> 32), cp = 0;
     for (uint64_t c0 = 0; c0 < tiles; c0 += 1024) {
         const uint64_t t = c0 + threadIdx.x;
         const bool ok = t < tiles;
-        const uint32_t m = ok ? info[3 * t + 0] : 0u;
-        const uint32_t k = ok ? info[3 * t + 1] : 0u;
-        const uint32_t h = ok ? info[3 * t + 2] : 0u;
-        uint32_t tk, th, tm;
+        const uint32_t m = ok ? info[4 * t + 0] : 0u;
+        const uint32_t k = ok ? info[4 * t + 1] : 0u;
+        const uint32_t h = ok ? info[4 * t + 2] : 0u;
+        const uint32_t p = ok ? info[4 * t + 3] : 0u;
+        uint32_t tk, th, tm, tp;
         const uint32_t em = block_exclusive_lastnz<1024>(m, wb[0], tm);
         const uint32_t ek = block_exclusive_sum<uint32_t, 1024>(k, wb[1], tk);
         const uint32_t eh = block_exclusive_sum<uint32_t, 1024>(h, wb[2], th);
+        const uint32_t ep = block_exclusive_sum<uint32_t, 1024>(p, wb[3], tp);
         if (ok) {
-            carry[3 * t + 0] = lastnz(cm, em);
-            carry[3 * t + 1] = ck + ek;
-            carry[3 * t + 2] = ch + eh;
+            carry[4 * t + 0] = lastnz(cm, em);
+            carry[4 * t + 1] = ck + ek;
+            carry[4 * t + 2] = ch + eh;
+            carry[4 * t + 3] = cp + ep;
         }
         cm = lastnz(cm, tm);
         ck += tk;
         ch += th;
+        cp += tp;
         __syncthreads();
     }
-    if (threadIdx.x == 0) { totals[0] = ck; totals[1] = ch; }
+    if (threadIdx.x == 0) {
+        totals[0] = ck;
+        totals[1] = ch;
+        if (pair_total) *pair_total = cp;
+    }
 }
 
 // Assign new ranks, emit singletons, compact the survivors.
 // Bytes per entry: key 8 + value 4 + pos 4 read; rank scatter 4; SA 4 for
 // singletons or 12 (index, pos, group) for survivors.
 template <int MODE>
-__global__ void __launch_bounds__(kAssignThreads)
+__global__ void __launch_bounds__(kAssignThreads, 3)
     k_assign(TileArgs a, const uint32_t *__restrict__ carry, uint32_t *__restrict__ rank, uint32_t *__restrict__ sa,
              uint32_t *__restrict__ out_i, uint32_t *__restrict__ out_pos, uint32_t *__restrict__ out_gid,
              uint32_t *__restrict__ gstart_out)
 {
-    __shared__ uint64_t s_keys[kAssignTile + 2];
-    __shared__ uint32_t s_vals[kAssignTile + 2];
-    __shared__ uint32_t s_w[3][kAssignWarps];
+    __shared__ uint64_t s_keys[kAssignTile + 2 * kHalo];
+    __shared__ uint32_t s_vals[kAssignTile + 2 * kHalo];
+    __shared__ uint32_t s_w[4][kAssignWarps];
+    __shared__ uint8_t s_head[kAssignTile + 2 * kHalo];
     const uint64_t base = (uint64_t)blockIdx.x * kAssignTile;
     const uint32_t valid = stage_tile(a, base, s_keys, s_vals, true);
+    stage_heads<MODE>(a, base, valid, s_keys, s_vals, s_head);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
     uint32_t hv_inc[kAssignPerLane], k_exc[kAssignPerLane], h_inc[kAssignPerLane], posv[kAssignPerLane];
-    bool single[kAssignPerLane], khead[kAssignPerLane];
-    uint32_t run_m = 0, run_k = 0, run_h = 0;
+    // per item q: bit q single, q + 8 kept head, q + 16 pair member, q + 24 first of a pair
+    static_assert(kAssignPerLane <= 8, "flag bits");
+    uint32_t fl = 0;
+    uint32_t run_m = 0, run_k = 0, run_h = 0, run_p = 0;
 #pragma unroll
     for (int q = 0; q < kAssignPerLane; ++q) {
         const int x = warp * 256 + q * 32 + lane;
         const bool ok = x < (int)valid;
-        ElemFlags f = {0u, 0u, 0u, false};
+        ElemFlags f = {0u, 0u, 0u, false, false, false};
         uint32_t pos = 0;
         if (ok) {
             const uint64_t j = base + x;
             pos = a.pos ? a.pos[j] : (uint32_t)j;
-            f = elem_flags<MODE>(a, base, x, s_keys, s_vals, pos);
+            f = elem_flags<MODE>(a, x, s_head, pos);
         }
         posv[q] = pos;
-        single[q] = f.single;
-        khead[q] = f.kh != 0;
+        fl |= (f.single ? 1u : 0u) << q | (f.kh ? 1u : 0u) << (q + 8) | (f.pair ? 1u : 0u) << (q + 16) |
+              (f.pair_first ? 1u : 0u) << (q + 24);
+        run_p += __popc(__ballot_sync(GSAIS_FULL_MASK, f.pair_first));
         uint32_t m = warp_inclusive_lastnz(f.hv);
         m = lastnz(run_m, m);
         const uint32_t ki = warp_inclusive_sum(f.kept);
@@ -399,9 +445,10 @@ __global__ void __launch_bounds__(kAssignThreads)
         run_k += __shfl_sync(GSAIS_FULL_MASK, ki, 31);
         run_h += __shfl_sync(GSAIS_FULL_MASK, hi, 31);
     }
-    if (lane == 0) { s_w[0][warp] = run_m; s_w[1][warp] = run_k; s_w[2][warp] = run_h; }
+    if (lane == 0) { s_w[0][warp] = run_m; s_w[1][warp] = run_k; s_w[2][warp] = run_h; s_w[3][warp] = run_p; }
     __syncthreads();
-    uint32_t wm = carry[3 * blockIdx.x + 0], wk = carry[3 * blockIdx.x + 1], wh = carry[3 * blockIdx.x + 2];
+
+    uint32_t wm = carry[4 * blockIdx.x + 0], wk = carry[4 * blockIdx.x + 1], wh = carry[4 * blockIdx.x + 2];
     for (int w = 0; w < warp; ++w) {
         wm = lastnz(wm, s_w[0][w]);
         wk += s_w[1][w];
@@ -411,19 +458,31 @@ __global__ void __launch_bounds__(kAssignThreads)
     for (int q = 0; q < kAssignPerLane; ++q) {
         const int x = warp * 256 + q * 32 + lane;
         if (x >= (int)valid) continue;
-        const uint32_t v = s_vals[x + 1];
+        const uint32_t v = s_vals[x + kHalo];
         const uint32_t r = lastnz(wm, hv_inc[q]);
         if (a.rank_out) a.rank_out[base + x] = r;
         else rank[v] = r;
-        if (single[q]) {
-            sa[posv[q]] = v;
+        if (fl & (0x10001u << q)) {
+            sa[posv[q]] = v;   // a single, or a pair's two members in either order until k_pair_compare
         } else {
             const uint32_t c = wk + k_exc[q];
             out_i[c] = v;
             out_pos[c] = posv[q];
             const uint32_t g = wh + h_inc[q] - 1;
             out_gid[c] = g;
-            if (khead[q]) gstart_out[g] = c;
+            if (fl & (0x100u << q)) gstart_out[g] = c;
+        }
+    }
+    if (MODE == MODE_INIT_PLAIN && a.pairs) {
+        uint32_t b = carry[4 * blockIdx.x + 3];   // pair-list slots of earlier tiles
+        for (int w = 0; w < warp; ++w) b += s_w[3][w];
+#pragma unroll
+        for (int q = 0; q < kAssignPerLane; ++q) {
+            const int x = warp * 256 + q * 32 + lane;
+            const bool lead = x < (int)valid && (fl & (0x1000000u << q));
+            const uint32_t m = __ballot_sync(GSAIS_FULL_MASK, lead);
+            if (lead) a.pairs[b + __popc(m & lanemask_lt())] = posv[q];
+            b += __popc(m);
         }
     }
 }
@@ -1254,7 +1313,7 @@ size_t sort_workspace_bytes(uint64_t n, int symbytes)
     s += 4 * align_up((n / 2 + 2) * 4, A);         // gstart x2, lid, loff (at most n/2 groups are active)
     s += 3 * align_up(n * 4, A);                   // large list: values x2, slots
     s += align_up(8 * 8, A);                       // round counters
-    s += 2 * align_up(tiles * 12, A);              // tile info + carry
+    s += 2 * align_up(tiles * 16, A);              // tile info + carry
     s += align_up(16 * 4, A);                      // totals
     s += align_up(65536 * 4, A);                   // hist
     s += align_up(65536 * 2, A);                   // codes
@@ -1285,8 +1344,8 @@ void sort_workspace_carve(SortWorkspace &ws, void *base, uint64_t n, int symbyte
     for (int i = 0; i < 2; ++i) ws.lvals[i] = reinterpret_cast<uint32_t *>(take(n * 4));
     ws.lpos = reinterpret_cast<uint32_t *>(take(n * 4));
     ws.counters = reinterpret_cast<unsigned long long *>(take(8 * 8));
-    ws.tile_info = reinterpret_cast<uint32_t *>(take(tiles * 12));
-    ws.tile_carry = reinterpret_cast<uint32_t *>(take(tiles * 12));
+    ws.tile_info = reinterpret_cast<uint32_t *>(take(tiles * 16));
+    ws.tile_carry = reinterpret_cast<uint32_t *>(take(tiles * 16));
     ws.totals = reinterpret_cast<uint32_t *>(take(16 * 4));
     ws.hist = reinterpret_cast<uint32_t *>(take(65536 * 4));
     ws.codes = reinterpret_cast<uint16_t *>(take(65536 * 2));
@@ -1327,7 +1386,8 @@ static cudaError_t run_assign(const TileArgs &a, SortWorkspace &ws, uint32_t *ou
     cudaEvent_t ev = prof ? prof->begin(st) : nullptr;
     GSAIS_COUNTED((k_tile_summary<MODE><<<(unsigned)tiles, kAssignThreads, 0, st>>>(a, ws.tile_info)));
     if (ev) prof->end(KK_SUMMARY, ev, st, a.N * (MODE == MODE_ROUND ? 12 : 16));
-    GSAIS_COUNTED((k_tile_scan<<<1, 1024, 0, st>>>(ws.tile_info, ws.tile_carry, tiles, ws.totals, base)));
+    GSAIS_COUNTED((k_tile_scan<<<1, 1024, 0, st>>>(ws.tile_info, ws.tile_carry, tiles, ws.totals, base,
+                                                   a.pairs ? a.pair_count : nullptr)));
     ev = prof ? prof->begin(st) : nullptr;
     GSAIS_COUNTED((k_assign<MODE><<<(unsigned)tiles, kAssignThreads, 0, st>>>(a, ws.tile_carry, ws.rank, ws.sa, out_i,
                                                                                 out_pos, out_gid, gstart_out)));
@@ -1398,6 +1458,27 @@ struct PairSource {
 };
 constexpr uint32_t kPairLimit = 1u << 16;   // symbols compared beyond the shared prefix
 
+// Orders the pairs listed in `pairs` (count in counters[3], cursor
+// counters[4]); members share `skip` symbols.  Unresolved pairs are appended
+// to the out lists behind the reservation counter counters[0].
+static cudaError_t run_pair_compare(SortWorkspace &ws, const PairSource &ps, const uint32_t *pairs, uint64_t max_pairs,
+                                    uint64_t skip, uint32_t *out_i, uint32_t *out_pos, uint32_t *out_gid,
+                                    uint32_t *gstart_out, uint32_t *d_err, cudaStream_t st)
+{
+    cudaEvent_t ev_pc = ws.radix.prof ? ws.radix.prof->begin(st) : nullptr;
+    const unsigned grid = (unsigned)stream_grid(max_pairs, 256);
+    if (ps.pack_bits == 2)
+        GSAIS_COUNTED((k_pair_compare<2><<<grid, 256, 0, st>>>(pairs, ws.counters + 3, ws.counters + 4, ps.words, ps.n,
+                                                              skip, kPairLimit, ws.sa, ws.rank, out_i, out_pos,
+                                                              out_gid, gstart_out, ws.counters, d_err)));
+    else
+        GSAIS_COUNTED((k_pair_compare<4><<<grid, 256, 0, st>>>(pairs, ws.counters + 3, ws.counters + 4, ps.words, ps.n,
+                                                              skip, kPairLimit, ws.sa, ws.rank, out_i, out_pos,
+                                                              out_gid, gstart_out, ws.counters, d_err)));
+    if (ev_pc) ws.radix.prof->end(KK_PAIRS, ev_pc, st, 0);
+    return cudaGetLastError();
+}
+
 static cudaError_t run_rounds(SortWorkspace &ws, uint64_t nr, int K, uint32_t kept, uint32_t groups, int av, int pg,
                               uint32_t *d_err, cudaStream_t st, SortStats &S, const PairSource &ps)
 {
@@ -1441,19 +1522,10 @@ static cudaError_t run_rounds(SortWorkspace &ws, uint64_t nr, int K, uint32_t ke
         GSAIS_COUNTED((k_medium_groups<<<stream_grid(G * 256, 256), 256, 0, st>>>(
             mlist, ws.counters + 2, ws.gstart[pg], G, N, act_i, act_pos, r2, ws.rank, ws.sa, out_i, out_pos, out_gid,
             ws.gstart[pg ^ 1], ws.counters)));
-        if (pairs) {
-            cudaEvent_t ev_pc = ws.radix.prof ? ws.radix.prof->begin(st) : nullptr;
-            // members share 2h symbols: h by their group, h more by equal r2
-            if (ps.pack_bits == 2)
-                GSAIS_COUNTED((k_pair_compare<2><<<stream_grid(N / 2, 256), 256, 0, st>>>(
-                    pairs, ws.counters + 3, ws.counters + 4, ps.words, ps.n, 2 * h, kPairLimit, ws.sa, ws.rank, out_i,
-                    out_pos, out_gid, ws.gstart[pg ^ 1], ws.counters, d_err)));
-            else
-                GSAIS_COUNTED((k_pair_compare<4><<<stream_grid(N / 2, 256), 256, 0, st>>>(
-                    pairs, ws.counters + 3, ws.counters + 4, ps.words, ps.n, 2 * h, kPairLimit, ws.sa, ws.rank, out_i,
-                    out_pos, out_gid, ws.gstart[pg ^ 1], ws.counters, d_err)));
-            if (ev_pc) ws.radix.prof->end(KK_PAIRS, ev_pc, st, 0);
-        }
+        // members of a tied pair share 2h symbols: h by their group, h more by equal r2
+        if (pairs && (e = run_pair_compare(ws, ps, pairs, N / 2, 2 * h, out_i, out_pos, out_gid, ws.gstart[pg ^ 1],
+                                           d_err, st)) != cudaSuccess)
+            return e;
         if ((e = cudaMemcpyAsync(ws.h_small, ws.counters, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                                  st)) != cudaSuccess)
             return e;
@@ -1479,6 +1551,8 @@ static cudaError_t run_rounds(SortWorkspace &ws, uint64_t nr, int K, uint32_t ke
             r.vals = vv[which];
             r.pos = ws.lpos;
             r.rank_out = nullptr;
+            r.pairs = nullptr;
+            r.pair_count = nullptr;
             r.N = NL;
             r.n = nr;
             r.K = (uint32_t)K;
@@ -1493,6 +1567,32 @@ static cudaError_t run_rounds(SortWorkspace &ws, uint64_t nr, int K, uint32_t ke
         h *= 2;
     }
     return cudaSuccess;
+}
+
+// Digit histograms of the seed keys from one histogram.  When a digit holds
+// d = 8 / bits whole codes, digit p of the key of suffix i is the d-gram of
+// codes starting at i + K - d (p + 1), so its histogram is the d-gram
+// histogram over the positions [s_p, n + s_p), s_p = K - d (p + 1).  The
+// seed kernel accumulates digit 0 only; digit p's histogram is digit 0's
+// plus the d*p grams at positions [s_p, s_0) and minus the d*p grams at
+// [n + s_p, n + s_0), which lie past the end of the text and are 0 (codes
+// past the end are 0, as in the keys).  `head` holds the codes of positions
+// [0, K).
+static void seed_hist_from_grams(uint32_t *hist, int passes, int bits, int K, const uint16_t *head)
+{
+    const int d = 8 / bits;
+    const int s0 = K - d;
+    for (int p = 1; p < passes; ++p) {
+        const int sp = K - d * (p + 1);
+        uint32_t *h = hist + 256 * p;
+        for (int v = 0; v < 256; ++v) h[v] = hist[v];
+        for (int j = sp; j < s0; ++j) {
+            uint32_t v = 0;
+            for (int q = 0; q < d; ++q) v = (v << bits) | head[j + q];
+            h[v] += 1;
+        }
+        h[0] -= (uint32_t)(s0 - sp);
+    }
 }
 
 cudaError_t suffix_sort(const void *d_T, int symbytes, uint64_t n, bool gsa, SortWorkspace &ws,
@@ -1541,6 +1641,10 @@ cudaError_t suffix_sort(const void *d_T, int symbytes, uint64_t n, bool gsa, Sor
     for (int c = 0, code = 0; !raw && c < nsym && code < 16; ++c)
         if (h_hist[c]) ws.decode[code++] = (uint16_t)c;
     const unsigned seed_grid = (unsigned)stream_grid((n + kSeedTile - 1) / kSeedTile * 256, 256);
+    // digits made of whole codes (plain texts, bits 1, 2, 4, 8): the seed
+    // kernel builds digit 0's histogram, the others follow on the host
+    const bool grams = !gsa && !raw && 8 % bits == 0 && seed_end % 8 == 0 && K <= 64 && n >= (uint64_t)(2 * K + 16);
+    const int hist_passes = grams ? 1 : seed_passes;
     uint32_t *k32[2] = {reinterpret_cast<uint32_t *>(ws.keys[0]), reinterpret_cast<uint32_t *>(ws.keys[1])};
     if ((e = cudaMemsetAsync(ws.radix.hist, 0, (size_t)seed_passes * 256 * 4, st)) != cudaSuccess) return e;
     cudaEvent_t ev_seed = ws.radix.prof ? ws.radix.prof->begin(st) : nullptr;
@@ -1548,34 +1652,49 @@ cudaError_t suffix_sort(const void *d_T, int symbytes, uint64_t n, bool gsa, Sor
         const uint8_t *T8 = static_cast<const uint8_t *>(d_T);
         if (narrow)
             GSAIS_COUNTED((k_seed<uint8_t, uint32_t><<<seed_grid, 256, 0, st>>>(
-                T8, n, ws.codes, bits, K, gsa ? 1 : 0, k32[0], ws.vals[0], seed_passes, seed_end, ws.radix.hist,
+                T8, n, ws.codes, bits, K, gsa ? 1 : 0, k32[0], ws.vals[0], hist_passes, seed_end, ws.radix.hist,
                 ws.pack_bits, ws.packed)));
         else
             GSAIS_COUNTED((k_seed<uint8_t, uint64_t><<<seed_grid, 256, 0, st>>>(
-                T8, n, ws.codes, bits, K, gsa ? 1 : 0, ws.keys[0], ws.vals[0], seed_passes, seed_end, ws.radix.hist,
+                T8, n, ws.codes, bits, K, gsa ? 1 : 0, ws.keys[0], ws.vals[0], hist_passes, seed_end, ws.radix.hist,
                 ws.pack_bits, ws.packed)));
     } else if (raw) {
         const uint32_t *T32 = static_cast<const uint32_t *>(d_T);
         if (narrow)
             GSAIS_COUNTED((k_seed<uint32_t, uint32_t><<<seed_grid, 256, 0, st>>>(
-                T32, n, ws.codes, bits, K, 0, k32[0], ws.vals[0], seed_passes, seed_end, ws.radix.hist, 0,
+                T32, n, ws.codes, bits, K, 0, k32[0], ws.vals[0], hist_passes, seed_end, ws.radix.hist, 0,
                 ws.packed)));
         else
             GSAIS_COUNTED((k_seed<uint32_t, uint64_t><<<seed_grid, 256, 0, st>>>(
-                T32, n, ws.codes, bits, K, 0, ws.keys[0], ws.vals[0], seed_passes, seed_end, ws.radix.hist, 0,
+                T32, n, ws.codes, bits, K, 0, ws.keys[0], ws.vals[0], hist_passes, seed_end, ws.radix.hist, 0,
                 ws.packed)));
     } else {
         const uint16_t *T16 = static_cast<const uint16_t *>(d_T);
         if (narrow)
             GSAIS_COUNTED((k_seed<uint16_t, uint32_t><<<seed_grid, 256, 0, st>>>(
-                T16, n, ws.codes, bits, K, gsa ? 1 : 0, k32[0], ws.vals[0], seed_passes, seed_end, ws.radix.hist,
+                T16, n, ws.codes, bits, K, gsa ? 1 : 0, k32[0], ws.vals[0], hist_passes, seed_end, ws.radix.hist,
                 ws.pack_bits, ws.packed)));
         else
             GSAIS_COUNTED((k_seed<uint16_t, uint64_t><<<seed_grid, 256, 0, st>>>(
-                T16, n, ws.codes, bits, K, gsa ? 1 : 0, ws.keys[0], ws.vals[0], seed_passes, seed_end, ws.radix.hist,
+                T16, n, ws.codes, bits, K, gsa ? 1 : 0, ws.keys[0], ws.vals[0], hist_passes, seed_end, ws.radix.hist,
                 ws.pack_bits, ws.packed)));
     }
     if (ev_seed) ws.radix.prof->end(KK_SEED, ev_seed, st, n * (symbytes + (narrow ? 8 : 12)));
+    if (grams) {
+        uint32_t *h_hist0 = ws.radix.h_hist;
+        uint8_t *h_edge = reinterpret_cast<uint8_t *>(ws.h_small + 16 + 65536 + 32768);
+        if ((e = cudaMemcpyAsync(h_hist0, ws.radix.hist, 256 * 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+        if ((e = cudaMemcpyAsync(h_edge, d_T, (size_t)K * symbytes, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+            return e;
+        if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+        uint16_t head[64];
+        for (int q = 0; q < K; ++q)
+            head[q] = h_codes[symbytes == 1 ? h_edge[q] : reinterpret_cast<const uint16_t *>(h_edge)[q]];
+        seed_hist_from_grams(h_hist0, seed_passes, bits, K, head);
+        if ((e = cudaMemcpyAsync(ws.radix.hist, h_hist0, (size_t)seed_passes * 256 * 4, cudaMemcpyHostToDevice, st)) !=
+            cudaSuccess)
+            return e;
+    }
     int w = 0, ran = 0;
     {
         uint32_t *vv[2] = {ws.vals[0], ws.vals[1]};
@@ -1596,6 +1715,8 @@ cudaError_t suffix_sort(const void *d_T, int symbytes, uint64_t n, bool gsa, Sor
     a.vals = ws.vals[w];
     a.pos = nullptr;
     a.rank_out = nullptr;
+    a.pairs = nullptr;
+    a.pair_count = nullptr;
     a.N = n;
     a.n = n;
     a.K = (uint32_t)K;
@@ -1605,6 +1726,20 @@ cudaError_t suffix_sort(const void *d_T, int symbytes, uint64_t n, bool gsa, Sor
     uint32_t kept = 0, groups = 0;
     int av = w ^ 1, pg = 0;
     if (use_two_level_ranks(n)) a.rank_out = reinterpret_cast<uint32_t *>(ws.keys[w ^ 1]);
+    PairSource ps;
+    if (ws.pack_bits == 2 || ws.pack_bits == 4) {
+        ps.pack_bits = ws.pack_bits;
+        ps.words.w = reinterpret_cast<const uint64_t *>(ws.packed);
+        ps.words.nwords = (n + kSeedTile - 1) / kSeedTile * (uint64_t)kSeedTile * ws.pack_bits / 64;
+        ps.n = n;
+    }
+    if (!gsa && ps.pack_bits) {
+        // groups of exactly two leave the seed round for direct comparison;
+        // their slots go after the ranks in keys[w ^ 1] (at most n / 2)
+        a.pairs = reinterpret_cast<uint32_t *>(ws.keys[w ^ 1]) + n;
+        a.pair_count = ws.counters + 3;
+        if ((e = cudaMemsetAsync(ws.counters, 0, 5 * sizeof(unsigned long long), st)) != cudaSuccess) return e;
+    }
     if (gsa)
         e = run_assign<MODE_INIT_GSA>(a, ws, ws.vals[av], ws.pos[pg], ws.gid[pg], ws.gstart[pg], nullptr, st, &kept,
                                       &groups);
@@ -1613,15 +1748,28 @@ cudaError_t suffix_sort(const void *d_T, int symbytes, uint64_t n, bool gsa, Sor
                                         &kept, &groups);
     if (e != cudaSuccess) return e;
     if (a.rank_out && (e = scatter_seed_ranks(ws, ws.vals[w], a.rank_out, n, n, d_err, st)) != cudaSuccess) return e;
+    if (a.pairs) {
+        // after the seed ranks are in place: order the pairs (they share the K
+        // seed symbols); unresolved ones are appended behind the survivors
+        unsigned long long *h = reinterpret_cast<unsigned long long *>(ws.h_small + 8);
+        h[0] = ((unsigned long long)groups << 32) | kept;
+        if ((e = cudaMemcpyAsync(ws.counters, h, sizeof(unsigned long long), cudaMemcpyHostToDevice, st)) !=
+            cudaSuccess)
+            return e;
+        if ((e = run_pair_compare(ws, ps, a.pairs, n / 2, (uint64_t)K, ws.vals[av], ws.pos[pg], ws.gid[pg],
+                                  ws.gstart[pg], d_err, st)) != cudaSuccess)
+            return e;
+        unsigned long long *hc = reinterpret_cast<unsigned long long *>(ws.h_small);
+        if ((e = cudaMemcpyAsync(hc, ws.counters, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st)) !=
+            cudaSuccess)
+            return e;
+        if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+        kept = (uint32_t)hc[0];
+        groups = (uint32_t)(hc[0] >> 32);
+        S.pairs_direct += hc[3];
+    }
 
     // ---- doubling rounds over the active suffixes
-    PairSource ps;
-    if (ws.pack_bits == 2 || ws.pack_bits == 4) {
-        ps.pack_bits = ws.pack_bits;
-        ps.words.w = reinterpret_cast<const uint64_t *>(ws.packed);
-        ps.words.nwords = (n + kSeedTile - 1) / kSeedTile * (uint64_t)kSeedTile * ws.pack_bits / 64;
-        ps.n = n;
-    }
     if ((e = run_rounds(ws, n, K, kept, groups, av, pg, d_err, st, S, ps)) != cudaSuccess) return e;
     uint32_t herr = 0;
     if ((e = cudaMemcpyAsync(ws.h_small, d_err, 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
@@ -1719,6 +1867,8 @@ cudaError_t batch_suffix_sort(const uint8_t *d_T, uint64_t n, const uint64_t *d_
     a.vals = ws.vals[w];
     a.pos = nullptr;
     a.rank_out = nullptr;
+    a.pairs = nullptr;
+    a.pair_count = nullptr;
     a.N = n;
     a.n = nr;
     a.K = (uint32_t)K;

@@ -31,7 +31,7 @@ struct SortWorkspace {
     int pack_bits = 0;                       // 0 (not packed), 2 or 4
     uint16_t decode[16] = {0};               // symbol of each code when packed
     RadixScratch radix;
-    uint32_t *h_small = nullptr;             // pinned host scratch (>= 65536 + 16 words)
+    uint32_t *h_small = nullptr;             // pinned host scratch (kHostSmallWords words)
 };
 
 // Bytes of device memory SortWorkspace needs for n symbols of `symbytes`
@@ -41,6 +41,12 @@ size_t sort_workspace_bytes(uint64_t n, int symbytes);
 // Carves a SortWorkspace out of `base` (which holds sort_workspace_bytes).
 void sort_workspace_carve(SortWorkspace &ws, void *base, uint64_t n, int symbytes, uint32_t *h_small,
                           uint32_t *h_hist);
+
+// Host scratch of a sort: 16 words of counters, a 65536-word symbol
+// histogram, 65536 16-bit codes, and kHostEdgeWords words for the symbols at
+// both ends of the text.
+constexpr size_t kHostEdgeWords = 256;
+constexpr size_t kHostSmallWords = 16 + 65536 + 32768 + kHostEdgeWords;
 
 struct SortOptions {
     int seed_key_bits = 32;   // width of the packed seed prefix (32 or 64)
