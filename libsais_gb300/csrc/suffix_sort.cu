@@ -1011,15 +1011,16 @@ struct PackedWords {
 // are known to share) on: the first differing code decides, and when one
 // suffix ends inside the common part the shorter one is smaller (the
 // implicit sentinel of libsais, src/libsais.c:7018).  One lane per pair; a
-// step loads one aligned 16-byte block per side, keeps the previous block,
-// and aligns four 32-bit words (128 / PB symbols) with word selects and
-// funnel shifts.  A lane whose pair is done idles until a quarter of its
+// step aligns four 32-bit words (128 / PB symbols) per side with word
+// selects and funnel shifts from two aligned 16-byte blocks, and loads the
+// block the following step needs.  A lane whose pair is done idles until a quarter of its
 // warp is idle; those lanes then take their next pairs together from a
 // global cursor, so the refill code runs rarely and work stays balanced.  A
 // pair still equal after `limit` more symbols goes back to the active list
 // as a two-member group.
 struct PairSide {
-    uint4 prev;      // last block loaded
+    uint4 prev;      // block holding the window's first word
+    uint4 next;      // the block after it, loaded one step ahead
     uint32_t q;      // next block to load
     uint32_t d;      // word offset of the window inside the block pair
     int sh;          // bit offset of the window inside its first word
@@ -1028,7 +1029,8 @@ struct PairSide {
 __device__ __forceinline__ void pair_window(const uint4 *__restrict__ W4, uint32_t last4, PairSide &s,
                                             uint32_t out[4])
 {
-    const uint4 cur = W4[s.q < last4 ? s.q : last4];
+    const uint4 cur = s.next;
+    s.next = W4[s.q < last4 ? s.q : last4];   // prefetch for the following step
     ++s.q;
     const uint32_t w[8] = {s.prev.x, s.prev.y, s.prev.z, s.prev.w, cur.x, cur.y, cur.z, cur.w};
     uint32_t u[6], e[5];
@@ -1070,7 +1072,8 @@ __global__ void __launch_bounds__(256) k_pair_compare(const uint32_t *__restrict
         s.sh = (int)(x % SPW) * PB;
         const uint32_t q4 = (uint32_t)(q >> 2);
         s.prev = W4[q4 < last4 ? q4 : last4];
-        s.q = q4 + 1;
+        s.next = W4[q4 + 1 < last4 ? q4 + 1 : last4];
+        s.q = q4 + 2;
     };
     while (true) {
         const uint32_t busy = __ballot_sync(GSAIS_FULL_MASK, live);
@@ -1519,7 +1522,10 @@ static cudaError_t run_rounds(SortWorkspace &ws, uint64_t nr, int K, uint32_t ke
             act_i, act_pos, act_gid, r2, N, ws.rank, ws.sa, out_i, out_pos, out_gid, ws.gstart[pg ^ 1],
             ws.counters, pairs, ws.counters + 3)));
         if (ev_sm) ws.radix.prof->end(KK_SMALL, ev_sm, st, N * 32);
-        GSAIS_COUNTED((k_medium_groups<<<stream_grid(G * 256, 256), 256, 0, st>>>(
+        // one CTA per medium group (their count is on the device; CTAs past it exit)
+        const uint64_t mcap = (uint64_t)stream_grid(~0ull >> 8, 256) * 4;   // 32 CTAs per SM
+        const unsigned mgrid = (unsigned)(G < mcap ? (G ? G : 1) : mcap);
+        GSAIS_COUNTED((k_medium_groups<<<mgrid, 256, 0, st>>>(
             mlist, ws.counters + 2, ws.gstart[pg], G, N, act_i, act_pos, r2, ws.rank, ws.sa, out_i, out_pos, out_gid,
             ws.gstart[pg ^ 1], ws.counters)));
         // members of a tied pair share 2h symbols: h by their group, h more by equal r2
