@@ -1006,41 +1006,60 @@ struct PackedWords {
 };
 
 
-// Orders the tied pairs found by k_small_groups by comparing the two
-// suffixes directly on the packed codes, from offset `skip` (a prefix both
-// are known to share) on: the first differing code decides, and when one
-// suffix ends inside the common part the shorter one is smaller (the
-// implicit sentinel of libsais, src/libsais.c:7018).  One lane per pair; a
-// step aligns four 32-bit words (128 / PB symbols) per side with word
-// selects and funnel shifts from two aligned 16-byte blocks, and loads the
-// block the following step needs.  A lane whose pair is done idles until a quarter of its
-// warp is idle; those lanes then take their next pairs together from a
-// global cursor, so the refill code runs rarely and work stays balanced.  A
-// pair still equal after `limit` more symbols goes back to the active list
-// as a two-member group.
+// Orders the tied pairs (two-member groups of the seed round, and tied pairs
+// found by k_small_groups) by comparing the two suffixes directly on the
+// packed codes, from offset `skip` (a prefix both are known to share) on:
+// the first differing code decides, and when one suffix ends inside the
+// common part the shorter one is smaller (the implicit sentinel of libsais,
+// src/libsais.c:7018).  One lane per pair; a step aligns 4 * kPairBlocks
+// 32-bit words per side with word selects and funnel shifts from aligned
+// 16-byte blocks, and loads the blocks the following step needs.  A lane
+// whose pair is done idles until a quarter of its warp is idle; those lanes
+// then take their next pairs together from a global cursor, so the refill
+// code runs rarely and work stays balanced.  A pair still equal after
+// `limit` more symbols goes back to the active list as a two-member group.
+constexpr int kPairBlocks = 2;   // 16-byte blocks per side per step
+
 struct PairSide {
-    uint4 prev;      // block holding the window's first word
-    uint4 next;      // the block after it, loaded one step ahead
-    uint32_t q;      // next block to load
-    uint32_t d;      // word offset of the window inside the block pair
-    int sh;          // bit offset of the window inside its first word
+    uint4 prev;               // block holding the window's first word
+    uint4 next[kPairBlocks];  // the blocks after it, loaded one step ahead
+    uint32_t q;               // next block to load
+    uint32_t d;               // word offset of the window inside the first block
+    int sh;                   // bit offset of the window inside its first word
 };
 
+// The 4 * kPairBlocks words of the window (aligned with word selects and
+// funnel shifts); loads the blocks of the following step.
 __device__ __forceinline__ void pair_window(const uint4 *__restrict__ W4, uint32_t last4, PairSide &s,
-                                            uint32_t out[4])
+                                            uint32_t out[4 * kPairBlocks])
 {
-    const uint4 cur = s.next;
-    s.next = W4[s.q < last4 ? s.q : last4];   // prefetch for the following step
-    ++s.q;
-    const uint32_t w[8] = {s.prev.x, s.prev.y, s.prev.z, s.prev.w, cur.x, cur.y, cur.z, cur.w};
-    uint32_t u[6], e[5];
+    constexpr int NW = 4 + 4 * kPairBlocks;
+    uint32_t w[NW];
+    w[0] = s.prev.x;
+    w[1] = s.prev.y;
+    w[2] = s.prev.z;
+    w[3] = s.prev.w;
 #pragma unroll
-    for (int i = 0; i < 6; ++i) u[i] = (s.d & 2) ? w[i + 2] : w[i];
+    for (int b = 0; b < kPairBlocks; ++b) {
+        w[4 + 4 * b] = s.next[b].x;
+        w[5 + 4 * b] = s.next[b].y;
+        w[6 + 4 * b] = s.next[b].z;
+        w[7 + 4 * b] = s.next[b].w;
+    }
+    s.prev = s.next[kPairBlocks - 1];
 #pragma unroll
-    for (int i = 0; i < 5; ++i) e[i] = (s.d & 1) ? u[i + 1] : u[i];
+    for (int b = 0; b < kPairBlocks; ++b) {
+        const uint32_t q = s.q + b;
+        s.next[b] = W4[q < last4 ? q : last4];   // prefetch for the following step
+    }
+    s.q += kPairBlocks;
+    uint32_t u[NW - 2], e[NW - 3];
 #pragma unroll
-    for (int i = 0; i < 4; ++i) out[i] = __funnelshift_r(e[i], e[i + 1], s.sh);
-    s.prev = cur;
+    for (int i = 0; i < NW - 2; ++i) u[i] = (s.d & 2) ? w[i + 2] : w[i];
+#pragma unroll
+    for (int i = 0; i < NW - 3; ++i) e[i] = (s.d & 1) ? u[i + 1] : u[i];
+#pragma unroll
+    for (int i = 0; i < 4 * kPairBlocks; ++i) out[i] = __funnelshift_r(e[i], e[i + 1], s.sh);
 }
 
 template <int PB>
@@ -1056,7 +1075,7 @@ __global__ void __launch_bounds__(256) k_pair_compare(const uint32_t *__restrict
                                                       uint32_t *__restrict__ err)
 {
     constexpr uint32_t SPW = 32 / PB;   // symbols per 32-bit word
-    constexpr uint32_t STEP = 4 * SPW;
+    constexpr uint32_t STEP = 4 * kPairBlocks * SPW;
     constexpr uint32_t CM = (1u << PB) - 1;
     const uint64_t count = *pair_count;
     const uint4 *W4 = reinterpret_cast<const uint4 *>(pw.w);
@@ -1072,8 +1091,9 @@ __global__ void __launch_bounds__(256) k_pair_compare(const uint32_t *__restrict
         s.sh = (int)(x % SPW) * PB;
         const uint32_t q4 = (uint32_t)(q >> 2);
         s.prev = W4[q4 < last4 ? q4 : last4];
-        s.next = W4[q4 + 1 < last4 ? q4 + 1 : last4];
-        s.q = q4 + 2;
+#pragma unroll
+        for (int b = 0; b < kPairBlocks; ++b) s.next[b] = W4[q4 + 1 + b < last4 ? q4 + 1 + b : last4];
+        s.q = q4 + 1 + kPairBlocks;
     };
     while (true) {
         const uint32_t busy = __ballot_sync(GSAIS_FULL_MASK, live);
@@ -1114,12 +1134,12 @@ __global__ void __launch_bounds__(256) k_pair_compare(const uint32_t *__restrict
         if (rem == 0) {
             res = end_res;
         } else {
-            uint32_t va[4], vb[4];
+            uint32_t va[4 * kPairBlocks], vb[4 * kPairBlocks];
             pair_window(W4, last4, A, va);
             pair_window(W4, last4, B, vb);
-            uint32_t x = 0, wa = 0, wb = 0, wi = 4;
+            uint32_t x = 0, wa = 0, wb = 0, wi = 4 * kPairBlocks;
 #pragma unroll
-            for (int i = 3; i >= 0; --i) {
+            for (int i = 4 * kPairBlocks - 1; i >= 0; --i) {
                 const uint32_t xi = va[i] ^ vb[i];
                 if (xi) { x = xi; wa = va[i]; wb = vb[i]; wi = i; }
             }
