@@ -434,16 +434,24 @@ __global__ void __launch_bounds__(kAssignThreads, 3)
         fl |= (f.single ? 1u : 0u) << q | (f.kh ? 1u : 0u) << (q + 8) | (f.pair ? 1u : 0u) << (q + 16) |
               (f.pair_first ? 1u : 0u) << (q + 24);
         run_p += __popc(__ballot_sync(GSAIS_FULL_MASK, f.pair_first));
-        uint32_t m = warp_inclusive_lastnz(f.hv);
-        m = lastnz(run_m, m);
-        const uint32_t ki = warp_inclusive_sum(f.kept);
-        const uint32_t hi = warp_inclusive_sum(f.kh);
+        // warp scans of the 0/1 flags by ballot: the last head at or before
+        // this lane gives the group start; kept counts give list offsets
+        const uint32_t le = lanemask_lt() | (1u << lane);
+        const uint32_t bh = __ballot_sync(GSAIS_FULL_MASK, f.hv != 0u);
+        const uint32_t bk = __ballot_sync(GSAIS_FULL_MASK, f.kept != 0u);
+        const uint32_t bkh = __ballot_sync(GSAIS_FULL_MASK, f.kh != 0u);
+        const uint32_t hm = bh & le;
+        const uint32_t src = hm ? 31u - (uint32_t)__clz(hm) : (uint32_t)lane;
+        uint32_t m = __shfl_sync(GSAIS_FULL_MASK, f.hv, src);
+        m = hm ? m : run_m;
+        const uint32_t ki = (uint32_t)__popc(bk & le);
+        const uint32_t hi = (uint32_t)__popc(bkh & le);
         hv_inc[q] = m;
         k_exc[q] = run_k + ki - f.kept;
         h_inc[q] = run_h + hi;
         run_m = __shfl_sync(GSAIS_FULL_MASK, m, 31);
-        run_k += __shfl_sync(GSAIS_FULL_MASK, ki, 31);
-        run_h += __shfl_sync(GSAIS_FULL_MASK, hi, 31);
+        run_k += (uint32_t)__popc(bk);
+        run_h += (uint32_t)__popc(bkh);
     }
     if (lane == 0) { s_w[0][warp] = run_m; s_w[1][warp] = run_k; s_w[2][warp] = run_h; s_w[3][warp] = run_p; }
     __syncthreads();
