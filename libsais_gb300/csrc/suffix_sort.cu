@@ -205,7 +205,7 @@ constexpr int kHalo = 2;
 // Stage keys/vals[base-kHalo .. base+valid+kHalo) into shared memory and
 // return the number of valid entries.
 __device__ __forceinline__ uint32_t stage_tile(const TileArgs &a, uint64_t base, uint64_t *s_keys, uint32_t *s_vals,
-                                               bool need_vals)
+                                               bool need_vals, bool need_keys = true)
 {
     const uint32_t valid = (uint32_t)((a.N - base) < (uint64_t)kAssignTile ? (a.N - base) : (uint64_t)kAssignTile);
     // every load of the tile is issued before the first shared store
@@ -217,14 +217,14 @@ __device__ __forceinline__ uint32_t stage_tile(const TileArgs &a, uint64_t base,
         const int x = (int)threadIdx.x + q * kAssignThreads;
         const int64_t j = (int64_t)base + x - kHalo;
         const bool in = x < (int)valid + 2 * kHalo && j >= 0 && (uint64_t)j < a.N;
-        kv[q] = in ? (a.keys32 ? (uint64_t)a.keys32[j] : a.keys[j]) : 0ull;
+        kv[q] = (in && need_keys) ? (a.keys32 ? (uint64_t)a.keys32[j] : a.keys[j]) : 0ull;
         vv[q] = (in && need_vals) ? a.vals[j] : 0u;
     }
 #pragma unroll
     for (int q = 0; q < SP; ++q) {
         const int x = (int)threadIdx.x + q * kAssignThreads;
         if (x < (int)valid + 2 * kHalo) {
-            s_keys[x] = kv[q];
+            if (need_keys) s_keys[x] = kv[q];
             if (need_vals) s_vals[x] = vv[q];
         }
     }
@@ -295,7 +295,8 @@ __device__ __forceinline__ ElemFlags elem_flags(const TileArgs &a, int x, const 
 // two-member groups taken out of the list (seed round).
 // Bytes per entry: key 8 (+ value 4 and pos 4 when used).
 template <int MODE>
-__global__ void __launch_bounds__(kAssignThreads) k_tile_summary(TileArgs a, uint32_t *__restrict__ info)
+__global__ void __launch_bounds__(kAssignThreads) k_tile_summary(TileArgs a, uint32_t *__restrict__ info,
+                                                                 uint32_t *__restrict__ heads)
 {
     __shared__ uint64_t s_keys[kAssignTile + 2 * kHalo];
     __shared__ uint32_t s_vals[kAssignTile + 2 * kHalo];
@@ -305,6 +306,12 @@ __global__ void __launch_bounds__(kAssignThreads) k_tile_summary(TileArgs a, uin
     __shared__ uint8_t s_head[kAssignTile + 2 * kHalo];
     const uint32_t valid = stage_tile(a, base, s_keys, s_vals, MODE == MODE_INIT_PLAIN);
     stage_heads<MODE>(a, base, valid, s_keys, s_vals, s_head);
+    // head bit of every entry of the tile, for k_assign (entries past the end read as heads)
+    for (int wd = (int)(threadIdx.x >> 5); wd < kAssignTile / 32; wd += kAssignWarps) {
+        const int x = wd * 32 + (int)(threadIdx.x & 31);
+        const uint32_t w = __ballot_sync(GSAIS_FULL_MASK, x >= (int)valid || s_head[x + kHalo]);
+        if ((threadIdx.x & 31) == 0) heads[base / 32 + wd] = w;
+    }
     uint32_t mx = 0, kept = 0, kh = 0, np = 0;   // mx: value of the last head (highest index) of the tile
     int mxx = -1;
     for (int x = threadIdx.x; x < (int)valid; x += blockDim.x) {
@@ -401,17 +408,21 @@ __global__ void __launch_bounds__(1024) k_tile_scan(const uint32_t *__restrict__
 // singletons or 12 (index, pos, group) for survivors.
 template <int MODE>
 __global__ void __launch_bounds__(kAssignThreads, 3)
-    k_assign(TileArgs a, const uint32_t *__restrict__ carry, uint32_t *__restrict__ rank, uint32_t *__restrict__ sa,
-             uint32_t *__restrict__ out_i, uint32_t *__restrict__ out_pos, uint32_t *__restrict__ out_gid,
-             uint32_t *__restrict__ gstart_out)
+    k_assign(TileArgs a, const uint32_t *__restrict__ carry, const uint32_t *__restrict__ heads,
+             uint32_t *__restrict__ rank, uint32_t *__restrict__ sa, uint32_t *__restrict__ out_i,
+             uint32_t *__restrict__ out_pos, uint32_t *__restrict__ out_gid, uint32_t *__restrict__ gstart_out)
 {
-    __shared__ uint64_t s_keys[kAssignTile + 2 * kHalo];
     __shared__ uint32_t s_vals[kAssignTile + 2 * kHalo];
     __shared__ uint32_t s_w[4][kAssignWarps];
     __shared__ uint8_t s_head[kAssignTile + 2 * kHalo];
     const uint64_t base = (uint64_t)blockIdx.x * kAssignTile;
-    const uint32_t valid = stage_tile(a, base, s_keys, s_vals, true);
-    stage_heads<MODE>(a, base, valid, s_keys, s_vals, s_head);
+    const uint32_t valid = stage_tile(a, base, nullptr, s_vals, true, false);
+    // head flags from the bits k_tile_summary wrote (out of range: head)
+    for (int l = threadIdx.x; l < (int)valid + 2 * kHalo; l += blockDim.x) {
+        const int64_t j = (int64_t)base + l - kHalo;
+        s_head[l] = (j < 0 || (uint64_t)j >= a.N) ? 1 : (uint8_t)((heads[j >> 5] >> (j & 31)) & 1u);
+    }
+    __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
     uint32_t hv_inc[kAssignPerLane], k_exc[kAssignPerLane], h_inc[kAssignPerLane], posv[kAssignPerLane];
@@ -1345,6 +1356,7 @@ size_t sort_workspace_bytes(uint64_t n, int symbytes)
     s += 3 * align_up(n * 4, A);                   // large list: values x2, slots
     s += align_up(8 * 8, A);                       // round counters
     s += 2 * align_up(tiles * 16, A);              // tile info + carry
+    s += align_up((tiles * kAssignTile / 32 + 2) * 4, A);   // head bits of the assign tiles
     s += align_up(16 * 4, A);                      // totals
     s += align_up(65536 * 4, A);                   // hist
     s += align_up(65536 * 2, A);                   // codes
@@ -1377,6 +1389,7 @@ void sort_workspace_carve(SortWorkspace &ws, void *base, uint64_t n, int symbyte
     ws.counters = reinterpret_cast<unsigned long long *>(take(8 * 8));
     ws.tile_info = reinterpret_cast<uint32_t *>(take(tiles * 16));
     ws.tile_carry = reinterpret_cast<uint32_t *>(take(tiles * 16));
+    ws.heads = reinterpret_cast<uint32_t *>(take((tiles * kAssignTile / 32 + 2) * 4));
     ws.totals = reinterpret_cast<uint32_t *>(take(16 * 4));
     ws.hist = reinterpret_cast<uint32_t *>(take(65536 * 4));
     ws.codes = reinterpret_cast<uint16_t *>(take(65536 * 2));
@@ -1415,13 +1428,13 @@ static cudaError_t run_assign(const TileArgs &a, SortWorkspace &ws, uint32_t *ou
     const uint64_t tiles = (a.N + kAssignTile - 1) / kAssignTile;
     KernelProfiler *prof = ws.radix.prof;
     cudaEvent_t ev = prof ? prof->begin(st) : nullptr;
-    GSAIS_COUNTED((k_tile_summary<MODE><<<(unsigned)tiles, kAssignThreads, 0, st>>>(a, ws.tile_info)));
+    GSAIS_COUNTED((k_tile_summary<MODE><<<(unsigned)tiles, kAssignThreads, 0, st>>>(a, ws.tile_info, ws.heads)));
     if (ev) prof->end(KK_SUMMARY, ev, st, a.N * (MODE == MODE_ROUND ? 12 : 16));
     GSAIS_COUNTED((k_tile_scan<<<1, 1024, 0, st>>>(ws.tile_info, ws.tile_carry, tiles, ws.totals, base,
                                                    a.pairs ? a.pair_count : nullptr)));
     ev = prof ? prof->begin(st) : nullptr;
-    GSAIS_COUNTED((k_assign<MODE><<<(unsigned)tiles, kAssignThreads, 0, st>>>(a, ws.tile_carry, ws.rank, ws.sa, out_i,
-                                                                                out_pos, out_gid, gstart_out)));
+    GSAIS_COUNTED((k_assign<MODE><<<(unsigned)tiles, kAssignThreads, 0, st>>>(
+        a, ws.tile_carry, ws.heads, ws.rank, ws.sa, out_i, out_pos, out_gid, gstart_out)));
     // algorithmic bytes: key 8 + value 4 + slot 4 read, rank 4 scattered, and
     // 4 (SA) or 12 (survivor lists) written -- counted as 28 per entry
     if (ev) prof->end(KK_ASSIGN, ev, st, a.N * 28);

@@ -20,6 +20,7 @@ struct SortWorkspace {
     uint32_t *loff = nullptr;                // per group: first slot in the large list
     uint32_t *lvals[2] = {nullptr, nullptr};   // large list: suffix indexes (sort ping-pong)
     uint32_t *lpos = nullptr;                // large list: SA slot of each entry
+    uint32_t *heads = nullptr;               // head bit of every entry of an assign (summary -> assign)
     unsigned long long *counters = nullptr;  // 8 round counters: output reservation (groups<<32 | entries),
                                              // large list, medium groups, tied pairs, pair cursor
     uint32_t *tile_info = nullptr;           // 3 words per assign tile
