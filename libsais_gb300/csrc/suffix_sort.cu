@@ -198,166 +198,126 @@ __device__ __forceinline__ bool has_zero_field(uint64_t x, uint64_t lo, uint64_t
     return ((x - lo) & ~x & hi) != 0;
 }
 
-// Entries staged on each side of a tile: head tests look one entry back, the
-// two-member group test two entries ahead and behind.
-constexpr int kHalo = 2;
+// ---- group heads as bits.  Word w of `heads` holds the head flags of list
+// entries [32w, 32w + 32); entries past N read as heads.  A head is an entry
+// whose key differs from the previous entry's (the seed round also splits
+// equal keys of different tail lengths, and for the GSA keys that hold a
+// separator; these mirror libsais's implicit sentinel and separator order).
+// The per-entry flags of the assign follow from three words with shifts:
+//   single     h(j) & h(j+1)
+//   pair first h(j) & !h(j+1) & h(j+2)    (seed round, plain texts)
+//   pair other !h(j) & h(j-1) & h(j+1)
+//   kept       !(single | pair),  kept head = h(j) & kept.
+constexpr int kAssignWordsPerTile = kAssignTile / 32;
 
-// Stage keys/vals[base-kHalo .. base+valid+kHalo) into shared memory and
-// return the number of valid entries.
-__device__ __forceinline__ uint32_t stage_tile(const TileArgs &a, uint64_t base, uint64_t *s_keys, uint32_t *s_vals,
-                                               bool need_vals, bool need_keys = true)
-{
-    const uint32_t valid = (uint32_t)((a.N - base) < (uint64_t)kAssignTile ? (a.N - base) : (uint64_t)kAssignTile);
-    // every load of the tile is issued before the first shared store
-    constexpr int SP = (kAssignTile + 2 * kHalo + kAssignThreads - 1) / kAssignThreads;
-    uint64_t kv[SP];
-    uint32_t vv[SP];
-#pragma unroll
-    for (int q = 0; q < SP; ++q) {
-        const int x = (int)threadIdx.x + q * kAssignThreads;
-        const int64_t j = (int64_t)base + x - kHalo;
-        const bool in = x < (int)valid + 2 * kHalo && j >= 0 && (uint64_t)j < a.N;
-        kv[q] = (in && need_keys) ? (a.keys32 ? (uint64_t)a.keys32[j] : a.keys[j]) : 0ull;
-        vv[q] = (in && need_vals) ? a.vals[j] : 0u;
-    }
-#pragma unroll
-    for (int q = 0; q < SP; ++q) {
-        const int x = (int)threadIdx.x + q * kAssignThreads;
-        if (x < (int)valid + 2 * kHalo) {
-            if (need_keys) s_keys[x] = kv[q];
-            if (need_vals) s_vals[x] = vv[q];
-        }
-    }
-    __syncthreads();
-    return valid;
-}
-
-// Head test for global entry j = base + l - 1 (l indexes the staged arrays).
 template <int MODE>
-__device__ __forceinline__ bool head_at(const TileArgs &a, uint64_t base, int l, const uint64_t *s_keys,
-                                        const uint32_t *s_vals)
+__device__ __forceinline__ uint64_t list_key(const TileArgs &a, uint64_t j)
 {
-    const uint64_t j = base + (uint64_t)l - kHalo;
-    if (j == 0 || j >= a.N) return true;
-    const uint64_t k = s_keys[l], kp = s_keys[l - 1];
-    if (k != kp) return true;
-    if (MODE == MODE_INIT_PLAIN) {
-        const uint64_t v = s_vals[l], vp = s_vals[l - 1];
-        const uint64_t lc = a.n - v < a.K ? a.n - v : a.K;
-        const uint64_t lcp = a.n - vp < a.K ? a.n - vp : a.K;
-        return lc != lcp;
-    } else if (MODE == MODE_INIT_GSA) {
-        return has_zero_field(k, a.zlo, a.zhi);   // k == kp here
-    }
-    return false;
+    return a.keys32 ? (uint64_t)a.keys32[j] : a.keys[j];
 }
 
-struct ElemFlags {
-    uint32_t hv;    // 1 + SA position if the entry starts a group, else 0
-    uint32_t kept;  // 1 if the entry stays active
-    uint32_t kh;    // 1 if the entry starts a group that stays active
-    bool single;
-    bool pair;      // member of a group of exactly two taken out for direct comparison
-    bool pair_first;
+// One warp per word: keys (and values) of 32 entries, the previous entry's
+// through a shuffle.  Bytes per entry: key 4 or 8 (+ value 4 in the plain seed round).
+template <int MODE>
+__global__ void __launch_bounds__(256) k_heads(TileArgs a, uint32_t *__restrict__ heads)
+{
+    const uint64_t words = (a.N + 31) / 32;
+    const int lane = threadIdx.x & 31;
+    const uint64_t nw = (uint64_t)gridDim.x * (blockDim.x / 32);
+    for (uint64_t w = (uint64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); w < words; w += nw) {
+        const uint64_t j = w * 32 + lane;
+        const bool in = j < a.N;
+        const uint64_t k = in ? list_key<MODE>(a, j) : 0ull;
+        const uint32_t v = (MODE == MODE_INIT_PLAIN && in) ? a.vals[j] : 0u;
+        uint64_t kp = __shfl_up_sync(GSAIS_FULL_MASK, k, 1);
+        uint32_t vp = __shfl_up_sync(GSAIS_FULL_MASK, v, 1);
+        if (lane == 0 && j > 0 && in) {
+            kp = list_key<MODE>(a, j - 1);
+            if (MODE == MODE_INIT_PLAIN) vp = a.vals[j - 1];
+        }
+        bool head = !in || j == 0 || k != kp;
+        if (!head && MODE == MODE_INIT_PLAIN) {
+            // equal padded keys: suffixes shorter than K differ in length class
+            const uint64_t lc = a.n - v < a.K ? a.n - v : a.K;
+            const uint64_t lcp = a.n - vp < a.K ? a.n - vp : a.K;
+            head = lc != lcp;
+        } else if (!head && MODE == MODE_INIT_GSA) {
+            head = has_zero_field(k, a.zlo, a.zhi);
+        }
+        const uint32_t bits = __ballot_sync(GSAIS_FULL_MASK, head);
+        if (lane == 0) heads[w] = bits;
+    }
+}
+
+struct RowFlags {
+    uint32_t head, single, pair, first, kept, kh;   // bit l: entry 32 r + l of the row
 };
 
-// s_head[l] = head_at(l) for every staged index l >= 1, computed once per tile.
-template <int MODE>
-__device__ __forceinline__ void stage_heads(const TileArgs &a, uint64_t base, uint32_t valid, const uint64_t *s_keys,
-                                            const uint32_t *s_vals, uint8_t *s_head)
+// Flags of the 32 entries of word r from words r - 1, r, r + 1, r + 2 of the
+// heads (words outside [0, words) read as all heads).
+__device__ __forceinline__ RowFlags row_flags(const uint32_t *__restrict__ heads, uint64_t r, uint64_t words,
+                                              bool pairs)
 {
-    for (int l = threadIdx.x; l < (int)valid + 2 * kHalo; l += blockDim.x)
-        s_head[l] = l == 0 ? 1 : (uint8_t)head_at<MODE>(a, base, l, s_keys, s_vals);
-    __syncthreads();
-}
-
-template <int MODE>
-__device__ __forceinline__ ElemFlags elem_flags(const TileArgs &a, int x, const uint8_t *s_head, uint32_t pos)
-{
-    ElemFlags f;
-    const bool head = s_head[x + kHalo];
-    const bool last = s_head[x + kHalo + 1];
-    f.single = head && last;
-    f.pair = f.pair_first = false;
-    if (MODE == MODE_INIT_PLAIN && a.pairs && !f.single) {
-        // first of two: next entry is not a head, the one after it is;
-        // second of two: the previous entry is a head and the next one too
-        f.pair_first = head && s_head[x + kHalo + 2];
-        f.pair = f.pair_first || (last && s_head[x + kHalo - 1]);
-    }
-    f.hv = head ? pos + 1 : 0u;
-    f.kept = (f.single || f.pair) ? 0u : 1u;
-    f.kh = (head && f.kept) ? 1u : 0u;
+    const uint32_t W = r < words ? heads[r] : ~0u;
+    const uint32_t Wp = (r > 0 && r - 1 < words) ? heads[r - 1] : ~0u;
+    const uint32_t Wn = r + 1 < words ? heads[r + 1] : ~0u;
+    const uint32_t N1 = (W >> 1) | (Wn << 31);
+    const uint32_t N2 = (W >> 2) | (Wn << 30);
+    const uint32_t P1 = (W << 1) | (Wp >> 31);
+    RowFlags f;
+    f.head = W;
+    f.single = W & N1;
+    f.first = pairs ? (W & ~N1 & N2) : 0u;
+    f.pair = pairs ? (f.first | (~W & P1 & N1)) : 0u;
+    f.kept = ~(f.single | f.pair);
+    f.kh = W & f.kept;
     return f;
 }
 
-// Per-tile reduction: max group-start value, kept entries, kept groups,
-// two-member groups taken out of the list (seed round).
-// Bytes per entry: key 8 (+ value 4 and pos 4 when used).
+// Per-tile reduction over the head bits: (value of the tile's last head, kept
+// entries, kept groups, two-member groups taken out).  One warp per tile,
+// two words per lane.
 template <int MODE>
-__global__ void __launch_bounds__(kAssignThreads) k_tile_summary(TileArgs a, uint32_t *__restrict__ info,
-                                                                 uint32_t *__restrict__ heads)
+__global__ void __launch_bounds__(256) k_tile_summary(TileArgs a, const uint32_t *__restrict__ heads,
+                                                      uint32_t *__restrict__ info)
 {
-    __shared__ uint64_t s_keys[kAssignTile + 2 * kHalo];
-    __shared__ uint32_t s_vals[kAssignTile + 2 * kHalo];
-    __shared__ uint32_t s_red[4][kAssignWarps];
-    __shared__ int s_redx[kAssignWarps];
-    const uint64_t base = (uint64_t)blockIdx.x * kAssignTile;
-    __shared__ uint8_t s_head[kAssignTile + 2 * kHalo];
-    const uint32_t valid = stage_tile(a, base, s_keys, s_vals, MODE == MODE_INIT_PLAIN);
-    stage_heads<MODE>(a, base, valid, s_keys, s_vals, s_head);
-    // head bit of every entry of the tile, for k_assign (entries past the end read as heads)
-    for (int wd = (int)(threadIdx.x >> 5); wd < kAssignTile / 32; wd += kAssignWarps) {
-        const int x = wd * 32 + (int)(threadIdx.x & 31);
-        const uint32_t w = __ballot_sync(GSAIS_FULL_MASK, x >= (int)valid || s_head[x + kHalo]);
-        if ((threadIdx.x & 31) == 0) heads[base / 32 + wd] = w;
-    }
-    uint32_t mx = 0, kept = 0, kh = 0, np = 0;   // mx: value of the last head (highest index) of the tile
-    int mxx = -1;
-    for (int x = threadIdx.x; x < (int)valid; x += blockDim.x) {
-        const uint64_t j = base + x;
-        const uint32_t pos = a.pos ? a.pos[j] : (uint32_t)j;
-        const ElemFlags f = elem_flags<MODE>(a, x, s_head, pos);
-        if (f.hv) {
-            mx = f.hv;
-            mxx = x;
-        }
-        kept += f.kept;
-        kh += f.kh;
-        np += f.pair_first ? 1u : 0u;
+    const uint64_t tiles = (a.N + kAssignTile - 1) / kAssignTile;
+    const uint64_t words = (a.N + 31) / 32;
+    const int lane = threadIdx.x & 31;
+    const bool pairs = MODE == MODE_INIT_PLAIN && a.pairs;
+    const uint64_t t = (uint64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+    if (t >= tiles) return;
+    uint32_t kept = 0, kh = 0, np = 0;
+    int64_t last = -1;   // list index of the last head
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+        const uint64_t r = t * kAssignWordsPerTile + 2 * lane + e;
+        if (r >= words) continue;
+        const RowFlags f = row_flags(heads, r, words, pairs);
+        const uint64_t j0 = r * 32;
+        const uint32_t valid = a.N - j0 >= 32 ? ~0u : ((1u << (a.N - j0)) - 1u);
+        kept += __popc(f.kept & valid);
+        kh += __popc(f.kh & valid);
+        np += __popc(f.first & valid);
+        if (f.head & valid) last = (int64_t)(j0 + 31 - __clz(f.head & valid));
     }
     for (int o = 16; o > 0; o >>= 1) {
-        const uint32_t m2 = __shfl_down_sync(GSAIS_FULL_MASK, mx, o);
-        const int x2 = __shfl_down_sync(GSAIS_FULL_MASK, mxx, o);
-        if (x2 > mxx) {
-            mxx = x2;
-            mx = m2;
-        }
         kept += __shfl_down_sync(GSAIS_FULL_MASK, kept, o);
         kh += __shfl_down_sync(GSAIS_FULL_MASK, kh, o);
         np += __shfl_down_sync(GSAIS_FULL_MASK, np, o);
+        const int64_t l2 = __shfl_down_sync(GSAIS_FULL_MASK, last, o);
+        if (l2 > last) last = l2;
     }
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) { s_red[0][warp] = mx; s_red[1][warp] = kept; s_red[2][warp] = kh; s_red[3][warp] = np; s_redx[warp] = mxx; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        uint32_t M = 0, A = 0, B = 0, C = 0;
-        int MX = -1;
-        for (int w = 0; w < kAssignWarps; ++w) {
-            if (s_redx[w] > MX) {
-                MX = s_redx[w];
-                M = s_red[0][w];
-            }
-            A += s_red[1][w];
-            B += s_red[2][w];
-            C += s_red[3][w];
-        }
-        info[4 * blockIdx.x + 0] = M;
-        info[4 * blockIdx.x + 1] = A;
-        info[4 * blockIdx.x + 2] = B;
-        info[4 * blockIdx.x + 3] = C;
+    if (lane == 0) {
+        uint32_t M = 0;
+        if (last >= 0) M = 1 + (a.pos ? a.pos[last] : (uint32_t)last);
+        info[4 * t + 0] = M;
+        info[4 * t + 1] = kept;
+        info[4 * t + 2] = kh;
+        info[4 * t + 3] = np;
     }
 }
+
 
 // Exclusive scan of the tile summaries (single CTA): carry[t] = (max, sum,
 // sum, sum) over tiles < t; totals[0] = kept entries, totals[1] = kept
@@ -403,66 +363,59 @@ __global__ void __launch_bounds__(1024) k_tile_scan(const uint32_t *__restrict__
     }
 }
 
-// Assign new ranks, emit singletons, compact the survivors.
-// Bytes per entry: key 8 + value 4 + pos 4 read; rank scatter 4; SA 4 for
-// singletons or 12 (index, pos, group) for survivors.
+// Assign new ranks, emit singletons, compact the survivors.  Flags come from
+// the head bits (one word per 32 entries, rows aligned to words), values and
+// slots are read in place; nothing is staged.
+// Bytes per entry: value 4 (+ slot 4 in the rounds) and 1/8 head bit read;
+// rank 4; SA 4 for singletons or 12 (index, slot, group) for survivors.
 template <int MODE>
 __global__ void __launch_bounds__(kAssignThreads, 3)
     k_assign(TileArgs a, const uint32_t *__restrict__ carry, const uint32_t *__restrict__ heads,
              uint32_t *__restrict__ rank, uint32_t *__restrict__ sa, uint32_t *__restrict__ out_i,
              uint32_t *__restrict__ out_pos, uint32_t *__restrict__ out_gid, uint32_t *__restrict__ gstart_out)
 {
-    __shared__ uint32_t s_vals[kAssignTile + 2 * kHalo];
     __shared__ uint32_t s_w[4][kAssignWarps];
-    __shared__ uint8_t s_head[kAssignTile + 2 * kHalo];
     const uint64_t base = (uint64_t)blockIdx.x * kAssignTile;
-    const uint32_t valid = stage_tile(a, base, nullptr, s_vals, true, false);
-    // head flags from the bits k_tile_summary wrote (out of range: head)
-    for (int l = threadIdx.x; l < (int)valid + 2 * kHalo; l += blockDim.x) {
-        const int64_t j = (int64_t)base + l - kHalo;
-        s_head[l] = (j < 0 || (uint64_t)j >= a.N) ? 1 : (uint8_t)((heads[j >> 5] >> (j & 31)) & 1u);
-    }
-    __syncthreads();
+    const uint64_t words = (a.N + 31) / 32;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const bool pairs = MODE == MODE_INIT_PLAIN && a.pairs;
+    const uint32_t le = lanemask_lt() | (1u << lane);
 
-    uint32_t hv_inc[kAssignPerLane], k_exc[kAssignPerLane], h_inc[kAssignPerLane], posv[kAssignPerLane];
-    // per item q: bit q single, q + 8 kept head, q + 16 pair member, q + 24 first of a pair
-    static_assert(kAssignPerLane <= 8, "flag bits");
-    uint32_t fl = 0;
+    uint32_t hv_inc[kAssignPerLane], k_exc[kAssignPerLane], h_inc[kAssignPerLane];
+    uint32_t vv[kAssignPerLane], pv[kAssignPerLane];
+    RowFlags rf[kAssignPerLane];
     uint32_t run_m = 0, run_k = 0, run_h = 0, run_p = 0;
 #pragma unroll
     for (int q = 0; q < kAssignPerLane; ++q) {
-        const int x = warp * 256 + q * 32 + lane;
-        const bool ok = x < (int)valid;
-        ElemFlags f = {0u, 0u, 0u, false, false, false};
-        uint32_t pos = 0;
-        if (ok) {
-            const uint64_t j = base + x;
-            pos = a.pos ? a.pos[j] : (uint32_t)j;
-            f = elem_flags<MODE>(a, x, s_head, pos);
-        }
-        posv[q] = pos;
-        fl |= (f.single ? 1u : 0u) << q | (f.kh ? 1u : 0u) << (q + 8) | (f.pair ? 1u : 0u) << (q + 16) |
-              (f.pair_first ? 1u : 0u) << (q + 24);
-        run_p += __popc(__ballot_sync(GSAIS_FULL_MASK, f.pair_first));
-        // warp scans of the 0/1 flags by ballot: the last head at or before
-        // this lane gives the group start; kept counts give list offsets
-        const uint32_t le = lanemask_lt() | (1u << lane);
-        const uint32_t bh = __ballot_sync(GSAIS_FULL_MASK, f.hv != 0u);
-        const uint32_t bk = __ballot_sync(GSAIS_FULL_MASK, f.kept != 0u);
-        const uint32_t bkh = __ballot_sync(GSAIS_FULL_MASK, f.kh != 0u);
-        const uint32_t hm = bh & le;
+        const uint64_t j = base + (uint64_t)(warp * 256 + q * 32 + lane);
+        const bool ok = j < a.N;
+        vv[q] = ok ? a.vals[j] : 0u;
+        pv[q] = ok ? (a.pos ? a.pos[j] : (uint32_t)j) : 0u;
+    }
+#pragma unroll
+    for (int q = 0; q < kAssignPerLane; ++q) {
+        const uint64_t r = base / 32 + (uint64_t)(warp * 8 + q);
+        const uint64_t j0 = r * 32;
+        const uint32_t valid = j0 >= a.N ? 0u : (a.N - j0 >= 32 ? ~0u : ((1u << (a.N - j0)) - 1u));
+        RowFlags f = row_flags(heads, r, words, pairs);
+        f.head &= valid;
+        f.kept &= valid;
+        f.kh &= valid;
+        f.first &= valid;
+        rf[q] = f;
+        run_p += (uint32_t)__popc(f.first);
+        // the last head at or before this lane gives the group start
+        const uint32_t hm = f.head & le;
         const uint32_t src = hm ? 31u - (uint32_t)__clz(hm) : (uint32_t)lane;
-        uint32_t m = __shfl_sync(GSAIS_FULL_MASK, f.hv, src);
+        uint32_t m = __shfl_sync(GSAIS_FULL_MASK, pv[q] + 1, src);
         m = hm ? m : run_m;
-        const uint32_t ki = (uint32_t)__popc(bk & le);
-        const uint32_t hi = (uint32_t)__popc(bkh & le);
+        const uint32_t kbit = (f.kept >> lane) & 1u;
         hv_inc[q] = m;
-        k_exc[q] = run_k + ki - f.kept;
-        h_inc[q] = run_h + hi;
+        k_exc[q] = run_k + (uint32_t)__popc(f.kept & le) - kbit;
+        h_inc[q] = run_h + (uint32_t)__popc(f.kh & le);
         run_m = __shfl_sync(GSAIS_FULL_MASK, m, 31);
-        run_k += (uint32_t)__popc(bk);
-        run_h += (uint32_t)__popc(bkh);
+        run_k += (uint32_t)__popc(f.kept);
+        run_h += (uint32_t)__popc(f.kh);
     }
     if (lane == 0) { s_w[0][warp] = run_m; s_w[1][warp] = run_k; s_w[2][warp] = run_h; s_w[3][warp] = run_p; }
     __syncthreads();
@@ -475,33 +428,32 @@ __global__ void __launch_bounds__(kAssignThreads, 3)
     }
 #pragma unroll
     for (int q = 0; q < kAssignPerLane; ++q) {
-        const int x = warp * 256 + q * 32 + lane;
-        if (x >= (int)valid) continue;
-        const uint32_t v = s_vals[x + kHalo];
+        const uint64_t x = (uint64_t)(warp * 256 + q * 32 + lane);
+        if (base + x >= a.N) continue;
+        const uint32_t v = vv[q];
         const uint32_t r = lastnz(wm, hv_inc[q]);
         if (a.rank_out) a.rank_out[base + x] = r;
         else rank[v] = r;
-        if (fl & (0x10001u << q)) {
-            sa[posv[q]] = v;   // a single, or a pair's two members in either order until k_pair_compare
+        const uint32_t bit = 1u << lane;
+        if ((rf[q].single | rf[q].pair) & bit) {
+            sa[pv[q]] = v;   // a single, or a pair's two members in either order until k_pair_compare
         } else {
             const uint32_t c = wk + k_exc[q];
             out_i[c] = v;
-            out_pos[c] = posv[q];
+            out_pos[c] = pv[q];
             const uint32_t g = wh + h_inc[q] - 1;
             out_gid[c] = g;
-            if (fl & (0x100u << q)) gstart_out[g] = c;
+            if (rf[q].kh & bit) gstart_out[g] = c;
         }
     }
-    if (MODE == MODE_INIT_PLAIN && a.pairs) {
+    if (pairs) {
         uint32_t b = carry[4 * blockIdx.x + 3];   // pair-list slots of earlier tiles
         for (int w = 0; w < warp; ++w) b += s_w[3][w];
 #pragma unroll
         for (int q = 0; q < kAssignPerLane; ++q) {
-            const int x = warp * 256 + q * 32 + lane;
-            const bool lead = x < (int)valid && (fl & (0x1000000u << q));
-            const uint32_t m = __ballot_sync(GSAIS_FULL_MASK, lead);
-            if (lead) a.pairs[b + __popc(m & lanemask_lt())] = posv[q];
-            b += __popc(m);
+            const uint32_t m = rf[q].first;
+            if ((m >> lane) & 1u) a.pairs[b + __popc(m & lanemask_lt())] = pv[q];
+            b += (uint32_t)__popc(m);
         }
     }
 }
@@ -1428,7 +1380,10 @@ static cudaError_t run_assign(const TileArgs &a, SortWorkspace &ws, uint32_t *ou
     const uint64_t tiles = (a.N + kAssignTile - 1) / kAssignTile;
     KernelProfiler *prof = ws.radix.prof;
     cudaEvent_t ev = prof ? prof->begin(st) : nullptr;
-    GSAIS_COUNTED((k_tile_summary<MODE><<<(unsigned)tiles, kAssignThreads, 0, st>>>(a, ws.tile_info, ws.heads)));
+    const uint64_t words = (a.N + 31) / 32;
+    GSAIS_COUNTED((k_heads<MODE><<<(unsigned)(words < (1u << 20) ? (words + 7) / 8 : (1u << 17)), 256, 0, st>>>(
+        a, ws.heads)));
+    GSAIS_COUNTED((k_tile_summary<MODE><<<(unsigned)((tiles + 7) / 8), 256, 0, st>>>(a, ws.heads, ws.tile_info)));
     if (ev) prof->end(KK_SUMMARY, ev, st, a.N * (MODE == MODE_ROUND ? 12 : 16));
     GSAIS_COUNTED((k_tile_scan<<<1, 1024, 0, st>>>(ws.tile_info, ws.tile_carry, tiles, ws.totals, base,
                                                    a.pairs ? a.pair_count : nullptr)));
