@@ -217,35 +217,51 @@ __device__ __forceinline__ uint64_t list_key(const TileArgs &a, uint64_t j)
 }
 
 // One warp per word: keys (and values) of 32 entries, the previous entry's
-// through a shuffle.  Bytes per entry: key 4 or 8 (+ value 4 in the plain seed round).
+// through a shuffle; each warp takes four words per step with all loads
+// issued first.  Bytes per entry: key 4 or 8 (+ value 4 in the plain seed round).
 template <int MODE>
 __global__ void __launch_bounds__(256) k_heads(TileArgs a, uint32_t *__restrict__ heads)
 {
+    constexpr int WPS = 4;   // words per warp per step
     const uint64_t words = (a.N + 31) / 32;
     const int lane = threadIdx.x & 31;
-    const uint64_t nw = (uint64_t)gridDim.x * (blockDim.x / 32);
-    for (uint64_t w = (uint64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); w < words; w += nw) {
-        const uint64_t j = w * 32 + lane;
-        const bool in = j < a.N;
-        const uint64_t k = in ? list_key<MODE>(a, j) : 0ull;
-        const uint32_t v = (MODE == MODE_INIT_PLAIN && in) ? a.vals[j] : 0u;
-        uint64_t kp = __shfl_up_sync(GSAIS_FULL_MASK, k, 1);
-        uint32_t vp = __shfl_up_sync(GSAIS_FULL_MASK, v, 1);
-        if (lane == 0 && j > 0 && in) {
-            kp = list_key<MODE>(a, j - 1);
-            if (MODE == MODE_INIT_PLAIN) vp = a.vals[j - 1];
+    const uint64_t nw = (uint64_t)gridDim.x * (blockDim.x / 32) * WPS;
+    for (uint64_t w0 = ((uint64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5)) * WPS; w0 < words; w0 += nw) {
+        uint64_t k[WPS], kp0[WPS];
+        uint32_t v[WPS], vp0[WPS];
+#pragma unroll
+        for (int u = 0; u < WPS; ++u) {
+            const uint64_t j = (w0 + u) * 32 + lane;
+            const bool in = j < a.N;
+            k[u] = in ? list_key<MODE>(a, j) : 0ull;
+            v[u] = (MODE == MODE_INIT_PLAIN && in) ? a.vals[j] : 0u;
+            const bool first = lane == 0 && j > 0 && in;   // lane 0 loads its predecessor
+            kp0[u] = first ? list_key<MODE>(a, j - 1) : 0ull;
+            vp0[u] = (MODE == MODE_INIT_PLAIN && first) ? a.vals[j - 1] : 0u;
         }
-        bool head = !in || j == 0 || k != kp;
-        if (!head && MODE == MODE_INIT_PLAIN) {
-            // equal padded keys: suffixes shorter than K differ in length class
-            const uint64_t lc = a.n - v < a.K ? a.n - v : a.K;
-            const uint64_t lcp = a.n - vp < a.K ? a.n - vp : a.K;
-            head = lc != lcp;
-        } else if (!head && MODE == MODE_INIT_GSA) {
-            head = has_zero_field(k, a.zlo, a.zhi);
+#pragma unroll
+        for (int u = 0; u < WPS; ++u) {
+            const uint64_t w = w0 + u;
+            const uint64_t j = w * 32 + lane;
+            const bool in = j < a.N;
+            uint64_t kp = __shfl_up_sync(GSAIS_FULL_MASK, k[u], 1);
+            uint32_t vp = __shfl_up_sync(GSAIS_FULL_MASK, v[u], 1);
+            if (lane == 0) {
+                kp = kp0[u];
+                vp = vp0[u];
+            }
+            bool head = !in || j == 0 || k[u] != kp;
+            if (!head && MODE == MODE_INIT_PLAIN) {
+                // equal padded keys: suffixes shorter than K differ in length class
+                const uint64_t lc = a.n - v[u] < a.K ? a.n - v[u] : a.K;
+                const uint64_t lcp = a.n - vp < a.K ? a.n - vp : a.K;
+                head = lc != lcp;
+            } else if (!head && MODE == MODE_INIT_GSA) {
+                head = has_zero_field(k[u], a.zlo, a.zhi);
+            }
+            const uint32_t bits = __ballot_sync(GSAIS_FULL_MASK, head);
+            if (lane == 0 && w < words) heads[w] = bits;
         }
-        const uint32_t bits = __ballot_sync(GSAIS_FULL_MASK, head);
-        if (lane == 0) heads[w] = bits;
     }
 }
 
@@ -329,26 +345,39 @@ __global__ void __launch_bounds__(1024) k_tile_scan(const uint32_t *__restrict__
                                                     const unsigned long long *__restrict__ base,
                                                     unsigned long long *__restrict__ pair_total)
 {
+    // each thread scans 32 consecutive tiles sequentially; one block scan per
+    // 32768 tiles combines the threads
+    constexpr int PT = 32;
     __shared__ uint32_t wb[4][33];
+    const uint4 *in4 = reinterpret_cast<const uint4 *>(info);
+    uint4 *out4 = reinterpret_cast<uint4 *>(carry);
     const unsigned long long b0 = base ? *base : 0ull;
     uint32_t cm = 0, ck = (uint32_t)b0, ch = (uint32_t)(b0 >> 32), cp = 0;
-    for (uint64_t c0 = 0; c0 < tiles; c0 += 1024) {
-        const uint64_t t = c0 + threadIdx.x;
-        const bool ok = t < tiles;
-        const uint32_t m = ok ? info[4 * t + 0] : 0u;
-        const uint32_t k = ok ? info[4 * t + 1] : 0u;
-        const uint32_t h = ok ? info[4 * t + 2] : 0u;
-        const uint32_t p = ok ? info[4 * t + 3] : 0u;
+    for (uint64_t c0 = 0; c0 < tiles; c0 += 1024 * PT) {
+        const uint64_t t0 = c0 + (uint64_t)threadIdx.x * PT;
+        uint32_t m = 0, k = 0, h = 0, p = 0;
+        for (int i = 0; i < PT; ++i) {
+            if (t0 + i >= tiles) break;
+            const uint4 x = in4[t0 + i];
+            m = lastnz(m, x.x);
+            k += x.y;
+            h += x.z;
+            p += x.w;
+        }
         uint32_t tk, th, tm, tp;
         const uint32_t em = block_exclusive_lastnz<1024>(m, wb[0], tm);
         const uint32_t ek = block_exclusive_sum<uint32_t, 1024>(k, wb[1], tk);
         const uint32_t eh = block_exclusive_sum<uint32_t, 1024>(h, wb[2], th);
         const uint32_t ep = block_exclusive_sum<uint32_t, 1024>(p, wb[3], tp);
-        if (ok) {
-            carry[4 * t + 0] = lastnz(cm, em);
-            carry[4 * t + 1] = ck + ek;
-            carry[4 * t + 2] = ch + eh;
-            carry[4 * t + 3] = cp + ep;
+        uint32_t rm = lastnz(cm, em), rk = ck + ek, rh = ch + eh, rp = cp + ep;
+        for (int i = 0; i < PT; ++i) {
+            if (t0 + i >= tiles) break;
+            const uint4 x = in4[t0 + i];
+            out4[t0 + i] = make_uint4(rm, rk, rh, rp);
+            rm = lastnz(rm, x.x);
+            rk += x.y;
+            rh += x.z;
+            rp += x.w;
         }
         cm = lastnz(cm, tm);
         ck += tk;
@@ -1381,7 +1410,8 @@ static cudaError_t run_assign(const TileArgs &a, SortWorkspace &ws, uint32_t *ou
     KernelProfiler *prof = ws.radix.prof;
     cudaEvent_t ev = prof ? prof->begin(st) : nullptr;
     const uint64_t words = (a.N + 31) / 32;
-    GSAIS_COUNTED((k_heads<MODE><<<(unsigned)(words < (1u << 20) ? (words + 7) / 8 : (1u << 17)), 256, 0, st>>>(
+    const uint64_t hsteps = (words + 31) / 32;   // 8 warps x 4 words per block step
+    GSAIS_COUNTED((k_heads<MODE><<<(unsigned)(hsteps < (1u << 16) ? (hsteps ? hsteps : 1) : (1u << 16)), 256, 0, st>>>(
         a, ws.heads)));
     GSAIS_COUNTED((k_tile_summary<MODE><<<(unsigned)((tiles + 7) / 8), 256, 0, st>>>(a, ws.heads, ws.tile_info)));
     if (ev) prof->end(KK_SUMMARY, ev, st, a.N * (MODE == MODE_ROUND ? 12 : 16));
