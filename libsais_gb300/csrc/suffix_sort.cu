@@ -93,6 +93,80 @@ __global__ void __launch_bounds__(256) k_hist_u16(const uint16_t *__restrict__ T
     }
 }
 
+// Seed keys for 2- and 4-bit codes with 32-bit keys (plain texts): the tile's
+// codes are packed most-significant-first into shared words, so the key of
+// position x (the K = 32 / B codes from x) is one funnel shift of two words.
+// Also writes the packed text (least-significant-first, the layout the BWT
+// gather and the pair comparison read) and digit 0's histogram.
+// Bytes per suffix: T s read, key 4 + value 4 written (+ B/8 packed).
+template <typename Sym, int B>
+__global__ void __launch_bounds__(256) k_seed_packed(const Sym *__restrict__ T, uint64_t n,
+                                                     const uint16_t *__restrict__ codes, uint32_t *__restrict__ keys,
+                                                     uint32_t *__restrict__ vals, int end_bit,
+                                                     uint32_t *__restrict__ hist, uint8_t *__restrict__ packed)
+{
+    static_assert(B == 2 || B == 4, "2- or 4-bit codes");
+    constexpr int PER = kSeedTile / 256;   // 8 codes per thread
+    constexpr int CPW = 32 / B;            // codes per word
+    constexpr int WORDS = kSeedTile / CPW; // words of the tile, plus one halo word
+    __shared__ uint32_t w[WORDS + 1];
+    __shared__ uint32_t sh[1][256];
+    radix_hist_zero(sh, 1);
+    const uint64_t tiles = (n + kSeedTile - 1) / kSeedTile;
+    const int tid = threadIdx.x, lane = tid & 31;
+    for (uint64_t t = blockIdx.x; t < tiles; t += gridDim.x) {
+        const uint64_t base = t * kSeedTile;
+        // codes of positions base + PER * tid .. + PER (past the end: 0)
+        uint32_t c[PER];
+#pragma unroll
+        for (int r = 0; r < PER; ++r) {
+            const uint64_t p = base + (uint64_t)tid * PER + r;
+            c[r] = p < n ? codes[T[p]] : 0u;
+        }
+        // packed text, least significant first
+        uint32_t lsb = 0, msb = 0;
+#pragma unroll
+        for (int r = 0; r < PER; ++r) {
+            lsb |= c[r] << (B * r);
+            msb = (msb << B) | c[r];
+        }
+        if (B == 2) reinterpret_cast<uint16_t *>(packed)[(base / PER) + tid] = (uint16_t)lsb;
+        else reinterpret_cast<uint32_t *>(packed)[(base / PER) + tid] = lsb;
+        __syncthreads();   // the previous tile's keys are read
+        if (B == 4) {
+            w[tid] = msb;
+        } else {
+            const uint32_t lo = __shfl_down_sync(GSAIS_FULL_MASK, msb, 1);
+            if ((lane & 1) == 0) w[tid >> 1] = (msb << 16) | lo;
+        }
+        if (tid == 0) {   // halo word: the CPW codes after the tile
+            uint32_t h = 0;
+            for (int q = 0; q < CPW; ++q) {
+                const uint64_t p = base + kSeedTile + q;
+                h = (h << B) | (p < n ? (uint32_t)codes[T[p]] : 0u);
+            }
+            w[WORDS] = h;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < PER; ++r) {
+            const int x = tid + 256 * r;
+            const int i = x / CPW, s = (x % CPW) * B;
+            const uint32_t key = __funnelshift_l(w[i + 1], w[i], s);
+            const uint64_t p = base + (uint64_t)x;
+            const bool ok = p < n;
+            if (ok) {
+                const uint64_t j = n - 1 - p;   // reverse text order: shorter suffixes first
+                keys[j] = key;
+                vals[j] = (uint32_t)p;
+            }
+            radix_hist_add(sh, (uint64_t)key, ok, 1, end_bit);
+        }
+    }
+    __syncthreads();
+    radix_hist_flush(sh, 1, hist);
+}
+
 // ------------------------------------------------------------------ seed
 // Packed K-symbol prefix of every suffix.  Each thread builds the keys of 8
 // consecutive positions: the highest one from its K codes, the others by
@@ -1680,7 +1754,23 @@ cudaError_t suffix_sort(const void *d_T, int symbytes, uint64_t n, bool gsa, Sor
     uint32_t *k32[2] = {reinterpret_cast<uint32_t *>(ws.keys[0]), reinterpret_cast<uint32_t *>(ws.keys[1])};
     if ((e = cudaMemsetAsync(ws.radix.hist, 0, (size_t)seed_passes * 256 * 4, st)) != cudaSuccess) return e;
     cudaEvent_t ev_seed = ws.radix.prof ? ws.radix.prof->begin(st) : nullptr;
-    if (symbytes == 1) {
+    const bool fast_seed = grams && narrow && (bits == 2 || bits == 4) && ws.pack_bits == bits;
+    if (fast_seed) {
+        if (symbytes == 1 && bits == 2)
+            GSAIS_COUNTED((k_seed_packed<uint8_t, 2><<<seed_grid, 256, 0, st>>>(
+                static_cast<const uint8_t *>(d_T), n, ws.codes, k32[0], ws.vals[0], seed_end, ws.radix.hist, ws.packed)));
+        else if (symbytes == 1)
+            GSAIS_COUNTED((k_seed_packed<uint8_t, 4><<<seed_grid, 256, 0, st>>>(
+                static_cast<const uint8_t *>(d_T), n, ws.codes, k32[0], ws.vals[0], seed_end, ws.radix.hist, ws.packed)));
+        else if (bits == 2)
+            GSAIS_COUNTED((k_seed_packed<uint16_t, 2><<<seed_grid, 256, 0, st>>>(
+                static_cast<const uint16_t *>(d_T), n, ws.codes, k32[0], ws.vals[0], seed_end, ws.radix.hist,
+                ws.packed)));
+        else
+            GSAIS_COUNTED((k_seed_packed<uint16_t, 4><<<seed_grid, 256, 0, st>>>(
+                static_cast<const uint16_t *>(d_T), n, ws.codes, k32[0], ws.vals[0], seed_end, ws.radix.hist,
+                ws.packed)));
+    } else if (symbytes == 1) {
         const uint8_t *T8 = static_cast<const uint8_t *>(d_T);
         if (narrow)
             GSAIS_COUNTED((k_seed<uint8_t, uint32_t><<<seed_grid, 256, 0, st>>>(
