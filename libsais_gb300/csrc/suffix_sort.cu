@@ -567,6 +567,7 @@ __global__ void __launch_bounds__(kAssignThreads, 3)
 // (dense large-group id, rank[i + h]).
 constexpr uint32_t kSmallMax = 32;      // <= this: split inside one warp
 constexpr uint32_t kMediumMax = 4096;   // <= this: sorted and split inside one CTA
+constexpr uint32_t kMediumSmall = 512;   // <= this: the 128-thread CTA tier
 constexpr uint32_t kNoLarge = 0xFFFFFFFFu;
 constexpr uint32_t kMedium = 0xFFFFFFFEu;
 
@@ -577,7 +578,9 @@ constexpr uint32_t kMedium = 0xFFFFFFFEu;
 __global__ void __launch_bounds__(256) k_classify(const uint32_t *__restrict__ gstart, uint64_t G, uint64_t N,
                                                   uint32_t *__restrict__ lid, uint32_t *__restrict__ loff,
                                                   unsigned long long *__restrict__ lcount,
-                                                  uint32_t *__restrict__ mlist, unsigned long long *__restrict__ mcount)
+                                                  uint32_t *__restrict__ mlist, unsigned long long *__restrict__ mcount,
+                                                  uint32_t *__restrict__ mlist2,
+                                                  unsigned long long *__restrict__ mcount2)
 {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < G; g += stride) {
@@ -588,6 +591,9 @@ __global__ void __launch_bounds__(256) k_classify(const uint32_t *__restrict__ g
             const unsigned long long old = atomicAdd(lcount, (1ull << 32) | size);
             lid[g] = (uint32_t)(old >> 32);
             loff[g] = (uint32_t)old;
+        } else if (size > kMediumSmall) {
+            lid[g] = kMedium;
+            mlist2[atomicAdd(mcount2, 1ull)] = (uint32_t)g;
         } else if (size > kSmallMax) {
             lid[g] = kMedium;
             mlist[atomicAdd(mcount, 1ull)] = (uint32_t)g;
@@ -597,14 +603,67 @@ __global__ void __launch_bounds__(256) k_classify(const uint32_t *__restrict__ g
     }
 }
 
-// Splits the medium groups (kSmallMax < size <= kMediumMax), one group per
-// CTA iteration: keys (rank[i+h] << 12 | member) are bitonic-sorted in
-// shared memory; a member's new slot is the group's first slot plus its
+// Bitonic sort of THREADS * R keys held R to a thread (thread t holds
+// positions t*R .. t*R+R-1), stages k <= pw only (pw a power of two; the
+// positions >= pw are never touched).  A compare-exchange partner t ^ j is
+// in the same thread for j < R, in another lane of the warp for
+// j < 32 * R (shuffles) and in another warp otherwise (shared memory).
+template <int THREADS, int R>
+__device__ __forceinline__ void block_bitonic(uint64_t (&v)[R], uint64_t *__restrict__ sm, uint32_t pw)
+{
+    const uint32_t base = threadIdx.x * R;
+    for (uint32_t k = 2; k <= pw; k <<= 1) {
+        for (uint32_t j = k >> 1; j >= (uint32_t)R; j >>= 1) {
+            if (j >= 32u * R) {
+#pragma unroll
+                for (int r = 0; r < R; ++r) sm[base + r] = v[r];
+                __syncthreads();
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    const uint32_t t = base + r;
+                    const uint64_t b = sm[t ^ j];
+                    const bool lo = ((t & j) == 0) == ((t & k) == 0);
+                    v[r] = lo ? (v[r] < b ? v[r] : b) : (v[r] > b ? v[r] : b);
+                }
+                __syncthreads();
+            } else {
+                const int lx = (int)(j / R);
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    const uint32_t t = base + r;
+                    const uint64_t b = __shfl_xor_sync(GSAIS_FULL_MASK, v[r], lx);
+                    const bool lo = ((t & j) == 0) == ((t & k) == 0);
+                    v[r] = lo ? (v[r] < b ? v[r] : b) : (v[r] > b ? v[r] : b);
+                }
+            }
+        }
+#pragma unroll
+        for (int jj = R / 2; jj > 0; jj >>= 1) {
+            if ((uint32_t)jj < k) {
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    if (r & jj) continue;
+                    const bool asc = ((base + r) & k) == 0;
+                    const uint64_t a = v[r], b = v[r | jj];
+                    const uint64_t mn = a < b ? a : b, mx = a < b ? b : a;
+                    v[r] = asc ? mn : mx;
+                    v[r | jj] = asc ? mx : mn;
+                }
+            }
+        }
+    }
+}
+
+// Splits the medium groups (kSmallMax < size <= MAXN), one group per CTA
+// iteration (two tiers: 128 threads for groups of at most kMediumSmall, 256
+// for the rest): keys (rank[i+h] << 12 | member) are bitonic-sorted in
+// registers (block_bitonic); a member's new slot is the group's first slot plus its
 // sorted position, its rank 1 + the first slot of its run of equal keys; a
 // run of one is final; survivors are appended behind the same atomic
 // (groups, entries) reservation as the warp path.
 // Bytes per suffix: r2 4 + index 4 read, rank scatter 4, SA 4 or survivors 12.
-__global__ void __launch_bounds__(256) k_medium_groups(const uint32_t *__restrict__ mlist,
+template <int THREADS, uint32_t MAXN>
+__global__ void __launch_bounds__(THREADS) k_medium_groups(const uint32_t *__restrict__ mlist,
                                                        const unsigned long long *__restrict__ mcount,
                                                        const uint32_t *__restrict__ gstart, uint64_t G, uint64_t N,
                                                        const uint32_t *__restrict__ act_i,
@@ -615,10 +674,14 @@ __global__ void __launch_bounds__(256) k_medium_groups(const uint32_t *__restric
                                                        uint32_t *__restrict__ gstart_out,
                                                        unsigned long long *__restrict__ counter)
 {
-    constexpr int THREADS = 256;
-    __shared__ uint64_t key[kMediumMax];
-    __shared__ uint32_t wb[3][THREADS / 32 + 1];
+    constexpr int R = (int)(MAXN / THREADS);
+    static_assert(R * THREADS == (int)MAXN && (R & (R - 1)) == 0, "MAXN = THREADS * power of two");
+    constexpr uint32_t kFewOthers = 128;   // one warp's register sort
+    __shared__ uint64_t key[MAXN];
+    __shared__ uint64_t few[kFewOthers];
+    __shared__ uint32_t wb[2][THREADS / 32 + 1];
     __shared__ unsigned long long s_base;
+    __shared__ uint32_t s_lt;
     const uint32_t M = (uint32_t)*mcount;
     const int tid = threadIdx.x;
     for (uint32_t m = blockIdx.x; m < M; m += gridDim.x) {
@@ -629,24 +692,79 @@ __global__ void __launch_bounds__(256) k_medium_groups(const uint32_t *__restric
         const uint32_t P = act_pos[s];
         uint32_t pw = 64;
         while (pw < size) pw <<= 1;
-        for (uint32_t t = tid; t < pw; t += THREADS)
-            key[t] = t < size ? (((uint64_t)r2[s + t] << 12) | t) : ~0ull;
-        __syncthreads();
-        for (uint32_t k = 2; k <= pw; k <<= 1) {
-            for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-                for (uint32_t t = tid; t < pw; t += THREADS) {
-                    const uint32_t x = t ^ j;
-                    if (x > t) {
-                        const uint64_t a = key[t], b = key[x];
-                        if ((a > b) == ((t & k) == 0)) {
-                            key[t] = b;
-                            key[x] = a;
-                        }
-                    }
-                }
-                __syncthreads();
-            }
+        const uint32_t r0 = r2[s];
+        bool same = true;
+        uint64_t v[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const uint32_t t = tid * R + r;
+            const uint32_t rt = t < size ? r2[s + t] : r0;
+            same &= rt == r0;
+            v[r] = t < size ? (((uint64_t)rt << 12) | t) : ~0ull;
         }
+        if (__syncthreads_and(same)) {
+            // No member differs at this depth (copies of one long repeat):
+            // the group survives whole, in member order, and its ranks
+            // (1 + its first slot) stay as they are.
+            if (tid == 0) s_base = atomicAdd(counter, (1ull << 32) | size);
+            __syncthreads();
+            const uint32_t base_e = (uint32_t)s_base, gid = (uint32_t)(s_base >> 32);
+            for (uint32_t t = tid; t < size; t += THREADS) {
+                out_i[base_e + t] = act_i[s + t];
+                out_pos[base_e + t] = P + t;
+                out_gid[base_e + t] = gid;
+            }
+            if (tid == 0) gstart_out[gid] = base_e;
+            // s_base is next written after the next group's __syncthreads_and,
+            // which every thread reaches only after reading it here
+            continue;
+        }
+        // Mostly one value (a run of periodic repeats loses a few members a
+        // round): the D members whose r2 differs from the middle member's are
+        // sorted by warp 0 when D <= kFewOthers, and the others form one run,
+        // in member order, between the smaller and the larger ones; the
+        // result equals the full sort of the keys.
+        const uint32_t c = r2[s + size / 2];
+        uint32_t nb = 0;
+#pragma unroll
+        for (int r = 0; r < R; ++r) nb += tid * R + r < size && (uint32_t)(v[r] >> 12) != c;
+        uint32_t D;
+        const uint32_t nb_ex = block_exclusive_sum<uint32_t, THREADS>(nb, wb[1], D);
+        if (D <= kFewOthers) {
+            uint32_t o = nb_ex;
+#pragma unroll
+            for (int r = 0; r < R; ++r)
+                if (tid * R + r < size && (uint32_t)(v[r] >> 12) != c) few[o++] = v[r];
+            __syncthreads();
+            if (tid < 32) {
+                uint32_t pd = 2;
+                while (pd < D) pd <<= 1;
+                uint64_t w[4];
+#pragma unroll
+                for (int r = 0; r < 4; ++r) w[r] = (uint32_t)(tid * 4 + r) < D ? few[tid * 4 + r] : ~0ull;
+                block_bitonic<32, 4>(w, nullptr, pd);   // pd <= 128: every partner is in this warp
+                uint32_t lt = 0;
+                const uint32_t B = size - D;
+#pragma unroll
+                for (int r = 0; r < 4; ++r) {
+                    const uint32_t x = tid * 4 + r;
+                    const uint32_t rw = (uint32_t)(w[r] >> 12);
+                    lt += __popc(__ballot_sync(GSAIS_FULL_MASK, x < D && rw < c));
+                    if (x < D) key[x + (rw > c ? B : 0u)] = w[r];
+                }
+                if (tid == 0) s_lt = lt;
+            }
+            __syncthreads();
+            uint32_t b = s_lt + tid * R - nb_ex;   // slot of this thread's first member of the run
+#pragma unroll
+            for (int r = 0; r < R; ++r)
+                if (tid * R + r < size && (uint32_t)(v[r] >> 12) == c) key[b++] = v[r];
+        } else {
+            block_bitonic<THREADS, R>(v, key, pw);
+#pragma unroll
+            for (int r = 0; r < R; ++r) key[tid * R + r] = v[r];
+        }
+        __syncthreads();
         // blocked ranges of sorted positions per thread
         const uint32_t C = (size + THREADS - 1) / THREADS;
         const uint32_t k0 = tid * C, k1 = k0 + C < size ? k0 + C : size;
@@ -661,10 +779,12 @@ __global__ void __launch_bounds__(256) k_medium_groups(const uint32_t *__restric
                 sheads += head;
             }
         }
-        uint32_t tot_s, tot_h, tot_l;
+        uint32_t tot_sh, tot_l;
         const uint32_t ex_last = block_exclusive_lastnz<THREADS>(lastv, wb[0], tot_l);
-        const uint32_t ex_surv = block_exclusive_sum<uint32_t, THREADS>(surv, wb[1], tot_s);
-        const uint32_t ex_head = block_exclusive_sum<uint32_t, THREADS>(sheads, wb[2], tot_h);
+        // survivors and survivor heads (each <= 4096) in the two halves of one word
+        const uint32_t ex_sh = block_exclusive_sum<uint32_t, THREADS>(surv | sheads << 16, wb[1], tot_sh);
+        const uint32_t ex_surv = ex_sh & 0xFFFFu, ex_head = ex_sh >> 16;
+        const uint32_t tot_s = tot_sh & 0xFFFFu, tot_h = tot_sh >> 16;
         if (tid == 0) s_base = tot_s ? atomicAdd(counter, ((unsigned long long)tot_h << 32) | tot_s) : 0ull;
         __syncthreads();
         const uint32_t base_e = (uint32_t)s_base, base_g = (uint32_t)(s_base >> 32);
@@ -1475,6 +1595,18 @@ static int stream_grid(uint64_t items, int threads)
     return (int)(want < 1 ? 1 : (want < cap ? want : cap));
 }
 
+// Grid of one full wave of resident CTAs, capped at `items`.
+template <typename Kernel>
+static unsigned resident_grid(Kernel kernel, int threads, uint64_t items)
+{
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, 0);
+    const uint64_t cap = (uint64_t)sms * (per > 0 ? per : 1);
+    return (unsigned)(items < cap ? (items ? items : 1) : cap);
+}
+
 template <int MODE>
 static cudaError_t run_assign(const TileArgs &a, SortWorkspace &ws, uint32_t *out_i, uint32_t *out_pos,
                               uint32_t *out_gid, uint32_t *gstart_out, const unsigned long long *base,
@@ -1604,14 +1736,16 @@ static cudaError_t run_rounds(SortWorkspace &ws, uint64_t nr, int K, uint32_t ke
         uint32_t *act_i = ws.vals[av], *act_pos = ws.pos[pg], *act_gid = ws.gid[pg];
         uint32_t *out_i = ws.vals[av ^ 1], *out_pos = ws.pos[pg ^ 1], *out_gid = ws.gid[pg ^ 1];
         uint32_t *r2 = reinterpret_cast<uint32_t *>(ws.keys[1]);   // consumed before the large sort reuses keys[1]
-        // counters: [0] small+medium output, [1] large list, [2] medium groups, [3] tied pairs,
-        // [4] next tied pair to compare
-        if ((e = cudaMemsetAsync(ws.counters, 0, 5 * sizeof(unsigned long long), st)) != cudaSuccess) return e;
+        // counters: [0] small+medium output, [1] large list, [2] medium groups (<= kMediumSmall),
+        // [3] tied pairs, [4] next tied pair to compare, [5] medium groups (> kMediumSmall)
+        if ((e = cudaMemsetAsync(ws.counters, 0, 6 * sizeof(unsigned long long), st)) != cudaSuccess) return e;
         uint32_t *pairs = ps.pack_bits ? r2 + N : nullptr;   // after r2 in keys[1]: N/2 slots at most
         if ((e = cudaMemsetAsync(ws.radix.hist, 0, (size_t)passes * 256 * 4, st)) != cudaSuccess) return e;
         uint32_t *mlist = ws.lvals[1];   // free until the large sort's first pass
+        uint32_t *mlist2 = ws.lvals[1] + N / 2;   // medium groups have > 32 members: N / 33 of each at most
         GSAIS_COUNTED((k_classify<<<stream_grid(G, 256), 256, 0, st>>>(ws.gstart[pg], G, N, ws.lid, ws.loff,
-                                                                      ws.counters + 1, mlist, ws.counters + 2)));
+                                                                      ws.counters + 1, mlist, ws.counters + 2, mlist2,
+                                                                      ws.counters + 5)));
         cudaEvent_t ev_rk = ws.radix.prof ? ws.radix.prof->begin(st) : nullptr;
         GSAIS_COUNTED((k_round_r2<<<stream_grid(N, 256), 256, 0, st>>>(
             act_i, act_pos, act_gid, ws.gstart[pg], ws.lid, ws.loff, ws.rank, h, N, nr, b2, r2, ws.keys[0],
@@ -1622,11 +1756,16 @@ static cudaError_t run_rounds(SortWorkspace &ws, uint64_t nr, int K, uint32_t ke
             act_i, act_pos, act_gid, r2, N, ws.rank, ws.sa, out_i, out_pos, out_gid, ws.gstart[pg ^ 1],
             ws.counters, pairs, ws.counters + 3)));
         if (ev_sm) ws.radix.prof->end(KK_SMALL, ev_sm, st, N * 32);
-        // one CTA per medium group (their count is on the device; CTAs past it exit)
-        const uint64_t mcap = (uint64_t)stream_grid(~0ull >> 8, 256) * 4;   // 32 CTAs per SM
-        const unsigned mgrid = (unsigned)(G < mcap ? (G ? G : 1) : mcap);
-        GSAIS_COUNTED((k_medium_groups<<<mgrid, 256, 0, st>>>(
+        // medium groups: one wave of resident CTAs, each looping over the
+        // groups (their count is on the device)
+        const uint64_t mg_max = G < N / (kSmallMax + 1) ? G : N / (kSmallMax + 1);
+        GSAIS_COUNTED((k_medium_groups<128, kMediumSmall>
+                       <<<resident_grid(k_medium_groups<128, kMediumSmall>, 128, mg_max), 128, 0, st>>>(
             mlist, ws.counters + 2, ws.gstart[pg], G, N, act_i, act_pos, r2, ws.rank, ws.sa, out_i, out_pos, out_gid,
+            ws.gstart[pg ^ 1], ws.counters)));
+        GSAIS_COUNTED((k_medium_groups<256, kMediumMax>
+                       <<<resident_grid(k_medium_groups<256, kMediumMax>, 256, mg_max), 256, 0, st>>>(
+            mlist2, ws.counters + 5, ws.gstart[pg], G, N, act_i, act_pos, r2, ws.rank, ws.sa, out_i, out_pos, out_gid,
             ws.gstart[pg ^ 1], ws.counters)));
         // members of a tied pair share 2h symbols: h by their group, h more by equal r2
         if (pairs && (e = run_pair_compare(ws, ps, pairs, N / 2, 2 * h, out_i, out_pos, out_gid, ws.gstart[pg ^ 1],
