@@ -133,6 +133,7 @@ extern "C" {
         int64_t workspace_bytes; /* device workspace held by the context */
         int64_t large_total;     /* sum over rounds of suffixes sorted by the global radix path */
         int64_t pairs_direct;    /* tied suffix pairs ordered by direct comparison of their text */
+        int64_t early_patch;     /* SA slots patched after SA left early for a pinned host buffer (0: no early copy) */
     } gsais_stats;
 
     int32_t gsais_last_stats(void * ctx, gsais_stats * out);

@@ -172,7 +172,7 @@ _lib = None
 class GsaisStats(ctypes.Structure):
     _fields_ = [("rounds", _i32), ("seed_symbols", _i32), ("seed_bits", _i32), ("radix_passes", _i32),
                 ("active_total", _i64), ("workspace_bytes", _i64), ("large_total", _i64),
-                ("pairs_direct", _i64)]
+                ("pairs_direct", _i64), ("early_patch", _i64)]
 
 
 class KernelProfile(ctypes.Structure):

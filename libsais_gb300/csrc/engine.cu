@@ -27,6 +27,7 @@ struct gsais_ctx {
     int device = -1;
     cudaStream_t stream = nullptr;
     cudaStream_t copy_stream = nullptr;   // device->host copies that overlap later kernels
+    cudaEvent_t early_ev = nullptr;       // SA may leave for the host (EarlySaCopy)
     void *arena = nullptr;
     size_t arena_bytes = 0;
     uint32_t *d_misc = nullptr;   // [0] error word, [1] validity flag
@@ -65,6 +66,7 @@ bool ctx_init(gsais_ctx *c)
     if (cudaGetDevice(&c->device) != cudaSuccess) return false;
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return false;
     if (cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess) return false;
+    if (cudaEventCreateWithFlags(&c->early_ev, cudaEventDisableTiming) != cudaSuccess) return false;
     if (cudaMalloc(&c->d_misc, 64) != cudaSuccess) return false;
     if (cudaMemset(c->d_misc, 0, 64) != cudaSuccess) return false;
     if (cudaMallocHost(&c->h_small, kSmallWords * sizeof(uint32_t)) != cudaSuccess) return false;
@@ -141,6 +143,43 @@ int64_t fail(cudaError_t)
         if (_e != cudaSuccess) return fail(_e);              \
     } while (0)
 
+// The device's address of a pinned (page-locked) host buffer, or nullptr.
+int32_t *pinned_view(void *p)
+{
+    cudaPointerAttributes a;
+    if (!p || cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? static_cast<int32_t *>(a.devicePointer) : nullptr;
+}
+
+// Slots an early SA copy may patch: at most n / 8 (more would make the
+// patch cost a sizable part of the copy it saves).
+inline uint64_t early_patch_cap(uint64_t n) { return n / 8; }
+
+// Sets up an early copy of the int32 SA into the caller's pinned buffer,
+// when it is one; the patch list comes from the arena (taken before the
+// sort workspace).
+bool early_setup(gsais_ctx *c, EarlySaCopy &ec, void *SA, int sa_bytes, uint64_t n, Carver &cv)
+{
+    if (sa_bytes != 4 || !SA) return false;
+    int32_t *dev = pinned_view(SA);
+    if (!dev) return false;
+    ec.host = static_cast<int32_t *>(SA);
+    ec.host_dev = dev;
+    ec.stream = c->copy_stream;
+    ec.ready = c->early_ev;
+    ec.patch_cap = early_patch_cap(n);
+    ec.patch = cv.take<uint32_t>(ec.patch_cap + 1);
+    return true;
+}
+
+inline size_t early_bytes(void *SA, int sa_bytes, uint64_t n)
+{
+    return sa_bytes == 4 && pinned_view(SA) ? align_up((early_patch_cap(n) + 1) * 4) : 0;
+}
+
 // Waits for a stream when it goes out of scope.
 struct StreamJoin {
     cudaStream_t s;
@@ -176,7 +215,7 @@ SortPlan plan_sort(uint64_t n, int symbytes, size_t extra)
 // Sort a device text already placed in the arena.  `sa_override` (nullable)
 // receives SA directly when the caller wants uint32 output in its own buffer.
 int64_t run_sort(gsais_ctx *c, const void *d_T, int symbytes, uint64_t n, bool gsa, SortWorkspace &ws,
-                 cudaStream_t st, uint32_t raw_max = 0)
+                 cudaStream_t st, uint32_t raw_max = 0, EarlySaCopy *early = nullptr)
 {
     if (gsa) {
         bool valid = true;
@@ -186,6 +225,7 @@ int64_t run_sort(gsais_ctx *c, const void *d_T, int symbytes, uint64_t n, bool g
     ws.radix.prof = &c->prof;
     SortOptions opt = c->opt;
     opt.raw_max = raw_max;
+    opt.early = early;
     GS_TRY(suffix_sort(d_T, symbytes, n, gsa, ws, opt, c->d_misc, st, &c->stats));
     return 0;
 }
@@ -214,6 +254,7 @@ void gsais_ctx_destroy(gsais_ctx *c)
         if (c->h_hist) cudaFreeHost(c->h_hist);
         if (c->stream) cudaStreamDestroy(c->stream);
         if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+        if (c->early_ev) cudaEventDestroy(c->early_ev);
     }
     delete c;
 }
@@ -236,16 +277,20 @@ int64_t gsais_run_sa(gsais_ctx *c, const void *T, int symbytes, int64_t n_, int 
     cudaStream_t st = c->stream;
     const size_t tb = align_up(n * symbytes);
     const size_t wide = sa_bytes == 8 ? align_up(n * 8) : 0;
-    const SortPlan plan = plan_sort(n, symbytes, tb + wide);
+    const SortPlan plan = plan_sort(n, symbytes, tb + wide + early_bytes(SA, sa_bytes, n));
     if (!ensure_arena(c, plan.total)) return -2;
     Carver cv(c->arena);
     uint8_t *d_T = cv.take<uint8_t>(n * symbytes);
     int64_t *d_wide = sa_bytes == 8 ? cv.take<int64_t>(n) : nullptr;
+    EarlySaCopy ec;
+    const bool early = early_setup(c, ec, SA, sa_bytes, n, cv);
     SortWorkspace ws;
     sort_workspace_carve(ws, cv.p, n, symbytes, c->h_small, c->h_hist);
     if (!clear_err(c, st)) return fail(cudaErrorUnknown);
+    cudaStream_t cs = c->copy_stream;
+    StreamJoin join{cs};   // no copy into the caller's buffer outlives the call, also on error returns
     GS_TRY(cudaMemcpyAsync(d_T, T, n * symbytes, cudaMemcpyHostToDevice, st));
-    const int64_t rc = run_sort(c, d_T, symbytes, n, gsa != 0, ws, st);
+    const int64_t rc = run_sort(c, d_T, symbytes, n, gsa != 0, ws, st, 0, early ? &ec : nullptr);
     if (rc == -1) {
         // libsais fills freq before rejecting a malformed GSA text (src/libsais.c:6883-6889)
         GS_TRY(symbol_histogram(d_T, symbytes, n, ws.hist, c->h_small + 16, st));
@@ -256,10 +301,14 @@ int64_t gsais_run_sa(gsais_ctx *c, const void *T, int symbytes, int64_t n_, int 
     if (sa_bytes == 8) {
         GS_TRY(widen_u32_to_i64(ws.sa, d_wide, n, st));
         GS_TRY(cudaMemcpyAsync(SA, d_wide, n * 8, cudaMemcpyDeviceToHost, st));
+    } else if (ec.started) {
+        GS_TRY(early_sa_patch(ec, ws.sa, n));   // the sort is done: run_sort synchronised st
     } else {
         GS_TRY(cudaMemcpyAsync(SA, ws.sa, n * 4, cudaMemcpyDeviceToHost, st));
     }
+    const cudaError_t ce = cudaStreamSynchronize(cs);
     GS_TRY(sync_checked(c, st));
+    GS_TRY(ce);
     emit_freq(c->h_small + 16, symbytes, freq, freq_bytes);
     return 0;
 }
@@ -328,7 +377,7 @@ int64_t gsais_run_bwt(gsais_ctx *c, const void *T, int symbytes, int64_t n_, voi
     cudaStream_t st = c->stream;
     const uint64_t icount = r > 0 ? (n - 1) / (uint64_t)r + 1 : 0;
     const size_t extra = align_up(n * symbytes) * 2 + (r > 0 ? align_up(icount * idx_bytes) : 0) +
-                         (SA && sa_bytes == 8 ? align_up(n * 8) : 0);
+                         (SA && sa_bytes == 8 ? align_up(n * 8) : 0) + early_bytes(SA, sa_bytes, n);
     const SortPlan plan = plan_sort(n, symbytes, extra);
     if (!ensure_arena(c, plan.total)) return -2;
     Carver cv(c->arena);
@@ -336,20 +385,25 @@ int64_t gsais_run_bwt(gsais_ctx *c, const void *T, int symbytes, int64_t n_, voi
     uint8_t *d_U = cv.take<uint8_t>(n * symbytes);
     void *d_I = r > 0 ? (void *)cv.take<uint8_t>(icount * idx_bytes) : nullptr;
     int64_t *d_wide = (SA && sa_bytes == 8) ? cv.take<int64_t>(n) : nullptr;
+    EarlySaCopy ec;
+    const bool early = early_setup(c, ec, SA, sa_bytes, n, cv);
     SortWorkspace ws;
     sort_workspace_carve(ws, cv.p, n, symbytes, c->h_small, c->h_hist);
     if (!clear_err(c, st)) return fail(cudaErrorUnknown);
-    GS_TRY(cudaMemcpyAsync(d_T, T, n * symbytes, cudaMemcpyHostToDevice, st));
-    const int64_t rc = run_sort(c, d_T, symbytes, n, false, ws, st);
-    if (rc != 0) return rc;
-    // the sort has completed (run_sort synchronises st): SA leaves on the copy
-    // stream while the BWT gather, which only reads SA, runs on st
     cudaStream_t cs = c->copy_stream;
     StreamJoin join{cs};   // no copy into the caller's buffer outlives the call, also on error returns
+    GS_TRY(cudaMemcpyAsync(d_T, T, n * symbytes, cudaMemcpyHostToDevice, st));
+    const int64_t rc = run_sort(c, d_T, symbytes, n, false, ws, st, 0, early ? &ec : nullptr);
+    if (rc != 0) return rc;
+    // the sort has completed (run_sort synchronises st): SA leaves on the copy
+    // stream (or, copied early, gets its late slots) while the BWT gather,
+    // which only reads SA, runs on st
     if (SA) {
         if (sa_bytes == 8) {
             GS_TRY(widen_u32_to_i64(ws.sa, d_wide, n, cs));
             GS_TRY(cudaMemcpyAsync(SA, d_wide, n * 8, cudaMemcpyDeviceToHost, cs));
+        } else if (ec.started) {
+            GS_TRY(early_sa_patch(ec, ws.sa, n));
         } else {
             GS_TRY(cudaMemcpyAsync(SA, ws.sa, n * 4, cudaMemcpyDeviceToHost, cs));
         }
@@ -683,6 +737,7 @@ int32_t gsais_last_stats(void *ctx, gsais_stats *out)
     out->workspace_bytes = (int64_t)c->arena_bytes;
     out->large_total = (int64_t)c->stats.large_total;
     out->pairs_direct = (int64_t)c->stats.pairs_direct;
+    out->early_patch = (int64_t)c->stats.early_patch;
     return 0;
 }
 

@@ -36,6 +36,12 @@ struct KernelProfiler {
     ~KernelProfiler();
 };
 
+// Small device-to-host read on stream st (a multiple of 4 bytes).  Into
+// pinned memory it is a one-block kernel storing over the host link, so it
+// does not queue behind a large copy that occupies the copy engine (an early
+// SA copy); into other host memory it is a cudaMemcpyAsync.
+cudaError_t read_back(void *h_dst, const void *d_src, size_t bytes, cudaStream_t st);
+
 // ---------------------------------------------------------------- radix sort
 // LSD radix sort of (key, value) pairs: 8-bit digits, one upsweep histogram
 // pass for all digits, then per digit a tile-count pass, a scan of the counts
@@ -76,6 +82,7 @@ struct SortStats {
     uint64_t active_total = 0;     // sum of active suffixes over rounds
     uint64_t large_total = 0;      // sum over rounds of suffixes in groups sorted by the radix path
     uint64_t pairs_direct = 0;     // tied pairs ordered by direct comparison
+    uint64_t early_patch = 0;      // SA slots written to the host after an early SA copy
     int radix_passes = 0;          // non-trivial digit passes over all sorts
 };
 

@@ -295,6 +295,12 @@ __global__ void __launch_bounds__(PassShape<K>::kThreads, PassShape<K>::kMinBloc
     if (bad) atomicOr(err, GSAIS_ERR_BOUNDS);
 }
 
+__global__ void __launch_bounds__(256) k_read_back(uint32_t *__restrict__ dst, const uint32_t *__restrict__ src,
+                                                   uint32_t words)
+{
+    for (uint32_t i = threadIdx.x; i < words; i += blockDim.x) dst[i] = src[i];
+}
+
 int sm_count()
 {
     int dev = 0, sms = 0;
@@ -336,9 +342,7 @@ cudaError_t sort_impl(K *keys[2], uint32_t *vals[2], uint64_t n, int begin_bit, 
         if (ev) rs.prof->end(KK_UPSWEEP, ev, st, n * sizeof(K));
     }
     GSAIS_COUNTED((k_bucket_bases<<<passes, 256, 0, st>>>(rs.hist, rs.bases)));
-    if ((e = cudaMemcpyAsync(rs.h_hist, rs.hist, (size_t)passes * 256 * sizeof(uint32_t), cudaMemcpyDeviceToHost,
-                             st)) != cudaSuccess)
-        return e;
+    if ((e = read_back(rs.h_hist, rs.hist, (size_t)passes * 256 * sizeof(uint32_t), st)) != cudaSuccess) return e;
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
     if ((e = pass_attr<K>()) != cudaSuccess) return e;
 
@@ -375,6 +379,21 @@ cudaError_t sort_impl(K *keys[2], uint32_t *vals[2], uint64_t n, int begin_bit, 
 }
 
 }  // namespace
+
+cudaError_t read_back(void *h_dst, const void *d_src, size_t bytes, cudaStream_t st)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, h_dst) != cudaSuccess) {
+        cudaGetLastError();
+        a.type = cudaMemoryTypeUnregistered;
+    }
+    if (a.type != cudaMemoryTypeHost || !a.devicePointer || (bytes & 3) ||
+        (reinterpret_cast<uintptr_t>(d_src) & 3) || (reinterpret_cast<uintptr_t>(h_dst) & 3))
+        return cudaMemcpyAsync(h_dst, d_src, bytes, cudaMemcpyDeviceToHost, st);
+    GSAIS_COUNTED((k_read_back<<<1, 256, 0, st>>>(static_cast<uint32_t *>(a.devicePointer),
+                                                 static_cast<const uint32_t *>(d_src), (uint32_t)(bytes / 4))));
+    return cudaGetLastError();
+}
 
 size_t radix_status_words(uint64_t n)
 {

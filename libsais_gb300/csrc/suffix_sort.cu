@@ -1262,6 +1262,8 @@ __global__ void __launch_bounds__(256) k_pair_compare(const uint32_t *__restrict
                                                       unsigned long long *__restrict__ cursor, PackedWords pw,
                                                       uint64_t n, uint64_t skip, uint32_t limit,
                                                       uint32_t *__restrict__ sa, uint32_t *__restrict__ rank,
+                                                      uint32_t *__restrict__ list_pos,
+                                                      uint32_t *__restrict__ list_rank,
                                                       uint32_t *__restrict__ out_i, uint32_t *__restrict__ out_pos,
                                                       uint32_t *__restrict__ out_gid,
                                                       uint32_t *__restrict__ gstart_out,
@@ -1357,8 +1359,14 @@ __global__ void __launch_bounds__(256) k_pair_compare(const uint32_t *__restrict
             const uint32_t lo = res < 0 ? a : b, hi = res < 0 ? b : a;
             sa[P] = lo;
             sa[P + 1] = hi;
-            rank[lo] = P + 1;
-            rank[hi] = P + 2;
+            if (list_rank) {   // seed ranks not scattered yet: order the pair in the SA-order list
+                list_pos[P] = lo;
+                list_pos[P + 1] = hi;
+                list_rank[P + 1] = P + 2;
+            } else {
+                rank[lo] = P + 1;
+                rank[hi] = P + 2;
+            }
         } else {
             const unsigned long long r = atomicAdd(counter, (1ull << 32) | 2ull);
             const uint32_t cc = (uint32_t)r, g = (uint32_t)(r >> 32);
@@ -1585,6 +1593,19 @@ static int grid_for(uint64_t items, int per_block)
     return (int)(g ? g : 1);
 }
 
+// host[slot] = sa[slot] for the recorded slots, written into pinned host
+// memory over the host link.  Bytes per slot: 4 + 4 read, 4 written.
+__global__ void __launch_bounds__(256) k_sa_patch(const uint32_t *__restrict__ patch, uint64_t m,
+                                                  const uint32_t *__restrict__ sa, uint64_t n,
+                                                  int32_t *__restrict__ host)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < m; j += stride) {
+        const uint32_t slot = patch[j];
+        if (slot < n) host[slot] = (int32_t)sa[slot];
+    }
+}
+
 static int stream_grid(uint64_t items, int threads)
 {
     int dev = 0, sms = 0;
@@ -1629,7 +1650,7 @@ static cudaError_t run_assign(const TileArgs &a, SortWorkspace &ws, uint32_t *ou
     // algorithmic bytes: key 8 + value 4 + slot 4 read, rank 4 scattered, and
     // 4 (SA) or 12 (survivor lists) written -- counted as 28 per entry
     if (ev) prof->end(KK_ASSIGN, ev, st, a.N * 28);
-    cudaError_t e = cudaMemcpyAsync(ws.h_small, ws.totals, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+    cudaError_t e = read_back(ws.h_small, ws.totals, 2 * sizeof(uint32_t), st);
     if (e != cudaSuccess) return e;
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
     *kept = ws.h_small[0];
@@ -1696,20 +1717,23 @@ constexpr uint32_t kPairLimit = 1u << 16;   // symbols compared beyond the share
 // Orders the pairs listed in `pairs` (count in counters[3], cursor
 // counters[4]); members share `skip` symbols.  Unresolved pairs are appended
 // to the out lists behind the reservation counter counters[0].
+// list_pos/list_rank (seed round with two-level ranks): the SA-order list of
+// (position, rank) not yet scattered into rank[]; the pair's order goes there.
 static cudaError_t run_pair_compare(SortWorkspace &ws, const PairSource &ps, const uint32_t *pairs, uint64_t max_pairs,
                                     uint64_t skip, uint32_t *out_i, uint32_t *out_pos, uint32_t *out_gid,
-                                    uint32_t *gstart_out, uint32_t *d_err, cudaStream_t st)
+                                    uint32_t *gstart_out, uint32_t *d_err, cudaStream_t st,
+                                    uint32_t *list_pos = nullptr, uint32_t *list_rank = nullptr)
 {
     cudaEvent_t ev_pc = ws.radix.prof ? ws.radix.prof->begin(st) : nullptr;
     const unsigned grid = (unsigned)stream_grid(max_pairs, 256);
     if (ps.pack_bits == 2)
         GSAIS_COUNTED((k_pair_compare<2><<<grid, 256, 0, st>>>(pairs, ws.counters + 3, ws.counters + 4, ps.words, ps.n,
-                                                              skip, kPairLimit, ws.sa, ws.rank, out_i, out_pos,
-                                                              out_gid, gstart_out, ws.counters, d_err)));
+                                                              skip, kPairLimit, ws.sa, ws.rank, list_pos, list_rank,
+                                                              out_i, out_pos, out_gid, gstart_out, ws.counters, d_err)));
     else
         GSAIS_COUNTED((k_pair_compare<4><<<grid, 256, 0, st>>>(pairs, ws.counters + 3, ws.counters + 4, ps.words, ps.n,
-                                                              skip, kPairLimit, ws.sa, ws.rank, out_i, out_pos,
-                                                              out_gid, gstart_out, ws.counters, d_err)));
+                                                              skip, kPairLimit, ws.sa, ws.rank, list_pos, list_rank,
+                                                              out_i, out_pos, out_gid, gstart_out, ws.counters, d_err)));
     if (ev_pc) ws.radix.prof->end(KK_PAIRS, ev_pc, st, 0);
     return cudaGetLastError();
 }
@@ -1771,9 +1795,7 @@ static cudaError_t run_rounds(SortWorkspace &ws, uint64_t nr, int K, uint32_t ke
         if (pairs && (e = run_pair_compare(ws, ps, pairs, N / 2, 2 * h, out_i, out_pos, out_gid, ws.gstart[pg ^ 1],
                                            d_err, st)) != cudaSuccess)
             return e;
-        if ((e = cudaMemcpyAsync(ws.h_small, ws.counters, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
-                                 st)) != cudaSuccess)
-            return e;
+        if ((e = read_back(ws.h_small, ws.counters, 4 * sizeof(unsigned long long), st)) != cudaSuccess) return e;
         if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
         const unsigned long long small_tot = reinterpret_cast<unsigned long long *>(ws.h_small)[0];
         const unsigned long long large_tot = reinterpret_cast<unsigned long long *>(ws.h_small)[1];
@@ -2008,17 +2030,18 @@ cudaError_t suffix_sort(const void *d_T, int symbytes, uint64_t n, bool gsa, Sor
         e = run_assign<MODE_INIT_PLAIN>(a, ws, ws.vals[av], ws.pos[pg], ws.gid[pg], ws.gstart[pg], nullptr, st,
                                         &kept, &groups);
     if (e != cudaSuccess) return e;
-    if (a.rank_out && (e = scatter_seed_ranks(ws, ws.vals[w], a.rank_out, n, n, d_err, st)) != cudaSuccess) return e;
     if (a.pairs) {
-        // after the seed ranks are in place: order the pairs (they share the K
-        // seed symbols); unresolved ones are appended behind the survivors
+        // order the pairs (they share the K seed symbols); unresolved ones are
+        // appended behind the survivors.  With two-level ranks the order goes
+        // into the SA-order list the rank scatter below reads.
         unsigned long long *h = reinterpret_cast<unsigned long long *>(ws.h_small + 8);
         h[0] = ((unsigned long long)groups << 32) | kept;
         if ((e = cudaMemcpyAsync(ws.counters, h, sizeof(unsigned long long), cudaMemcpyHostToDevice, st)) !=
             cudaSuccess)
             return e;
         if ((e = run_pair_compare(ws, ps, a.pairs, n / 2, (uint64_t)K, ws.vals[av], ws.pos[pg], ws.gid[pg],
-                                  ws.gstart[pg], d_err, st)) != cudaSuccess)
+                                  ws.gstart[pg], d_err, st, a.rank_out ? ws.vals[w] : nullptr, a.rank_out)) !=
+            cudaSuccess)
             return e;
         unsigned long long *hc = reinterpret_cast<unsigned long long *>(ws.h_small);
         if ((e = cudaMemcpyAsync(hc, ws.counters, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st)) !=
@@ -2030,14 +2053,39 @@ cudaError_t suffix_sort(const void *d_T, int symbytes, uint64_t n, bool gsa, Sor
         S.pairs_direct += hc[3];
     }
 
+    // ---- SA leaves for the host while the rank scatter and the rounds run
+    // (the slots the rounds write are patched afterwards)
+    if (opt.early && opt.early->host && kept > 0 && kept <= opt.early->patch_cap) {
+        EarlySaCopy &ec = *opt.early;
+        if ((e = cudaMemcpyAsync(ec.patch, ws.pos[pg], (size_t)kept * 4, cudaMemcpyDeviceToDevice, st)) !=
+            cudaSuccess)
+            return e;
+        if ((e = cudaEventRecord(ec.ready, st)) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(ec.stream, ec.ready, 0)) != cudaSuccess) return e;
+        if ((e = cudaMemcpyAsync(ec.host, ws.sa, n * 4, cudaMemcpyDeviceToHost, ec.stream)) != cudaSuccess)
+            return e;
+        ec.patch_n = kept;
+        ec.started = true;
+        S.early_patch = kept;
+    }
+    if (a.rank_out && (e = scatter_seed_ranks(ws, ws.vals[w], a.rank_out, n, n, d_err, st)) != cudaSuccess) return e;
+
     // ---- doubling rounds over the active suffixes
     if ((e = run_rounds(ws, n, K, kept, groups, av, pg, d_err, st, S, ps)) != cudaSuccess) return e;
     uint32_t herr = 0;
-    if ((e = cudaMemcpyAsync(ws.h_small, d_err, 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+    if ((e = read_back(ws.h_small, d_err, 4, st)) != cudaSuccess) return e;
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
     herr = ws.h_small[0];
     if (ws.radix.prof) ws.radix.prof->flush();
     return herr ? cudaErrorUnknown : cudaSuccess;
+}
+
+cudaError_t early_sa_patch(const EarlySaCopy &ec, const uint32_t *d_sa, uint64_t n)
+{
+    if (!ec.started || ec.patch_n == 0) return cudaSuccess;
+    GSAIS_COUNTED((k_sa_patch<<<stream_grid(ec.patch_n, 256), 256, 0, ec.stream>>>(ec.patch, ec.patch_n, d_sa, n,
+                                                                                  ec.host_dev)));
+    return cudaGetLastError();
 }
 
 cudaError_t symbol_histogram(const void *d_T, int symbytes, uint64_t n, uint32_t *d_hist, uint32_t *h_hist,

@@ -49,10 +49,34 @@ void sort_workspace_carve(SortWorkspace &ws, void *base, uint64_t n, int symbyte
 constexpr size_t kHostEdgeWords = 256;
 constexpr size_t kHostSmallWords = 16 + 65536 + 32768 + kHostEdgeWords;
 
+// Early device-to-host copy of an int32 suffix array into pinned host
+// memory.  When the seed round (with its tied pairs) leaves at most
+// patch_cap unresolved entries, the sort starts copying SA to `host` on
+// `stream` before the doubling rounds and records the SA slots of those
+// entries in `patch`; the rounds write only those slots, so once the sort is
+// done early_sa_patch() writes their final values through `host_dev` (the
+// device's address of the same buffer) and the copy of the whole array
+// overlaps the rounds.
+struct EarlySaCopy {
+    int32_t *host = nullptr;       // destination (the caller's pinned buffer)
+    int32_t *host_dev = nullptr;   // the same buffer as the device addresses it
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ready = nullptr;   // recorded on the sort's stream when the copy may start
+    uint32_t *patch = nullptr;     // device: room for patch_cap slots
+    uint64_t patch_cap = 0;
+    uint64_t patch_n = 0;          // out: slots recorded
+    bool started = false;          // out: the bulk copy is queued on `stream`
+};
+
 struct SortOptions {
     int seed_key_bits = 32;   // width of the packed seed prefix (32 or 64)
     uint32_t raw_max = 0;     // 32-bit integer symbols: the largest symbol value
+    EarlySaCopy *early = nullptr;
 };
+
+// Queues, on ec.stream behind the bulk copy, the writes of the recorded
+// slots' final values from d_sa to the host buffer.
+cudaError_t early_sa_patch(const EarlySaCopy &ec, const uint32_t *d_sa, uint64_t n);
 
 // Suffix array of the device text d_T (n symbols of `symbytes` bytes).  gsa
 // sorts as a generalized suffix array with 0 separators (the caller has

@@ -149,6 +149,43 @@ def test_copied_segments_pairs(oracle):
         assert st["pairs_direct"] > 0, st
 
 
+def test_pinned_host_buffers_early_copy(oracle):
+    """Host calls whose SA buffer is pinned: SA leaves for the host while the
+    doubling rounds run and the slots the rounds write are patched afterwards
+    (early_patch > 0 when that path ran).  SA, BWT and primary index must
+    equal the oracle's, for libsais and the combined SA + BWT call (and
+    libsais_bwt, which returns no SA); a periodic text leaves too many
+    unresolved suffixes and takes the plain copy."""
+    torch = pytest.importorskip("torch")
+    lib = G.load()
+    rng = np.random.default_rng(23)
+    cases = [(textgen.genome_like(1 << 20, seed=5), True),
+             (textgen.genome_like(300_001, seed=6), True),
+             ((rng.integers(0, 256, 200_000)).astype(np.uint8), None),
+             (np.frombuffer(b"abcab" * 40_000, dtype=np.uint8).copy(), False)]
+    for T, expect_early in cases:
+        n = T.size
+        _, oSA, _ = oracle.libsais(T)
+        p, oU, _, _ = oracle.libsais_bwt(T)
+        hT = torch.from_numpy(T).pin_memory()
+        for call in ("sa", "bwt", "sa_bwt"):
+            hSA = torch.full((n,), -7, dtype=torch.int32).pin_memory()
+            hU = torch.zeros(n, dtype=torch.uint8).pin_memory()
+            if call == "sa":
+                assert lib.libsais(hT.data_ptr(), hSA.data_ptr(), n, 0, None) == 0
+            elif call == "bwt":
+                assert lib.libsais_bwt(hT.data_ptr(), hU.data_ptr(), hSA.data_ptr(), n, 0, None) == p
+            else:
+                assert lib.gsais_sa_bwt(None, hT.data_ptr(), 1, n, hSA.data_ptr(), 4, hU.data_ptr(), None, 4) == p
+            early = G.last_stats()["early_patch"]   # libsais_bwt returns no SA: never early
+            if expect_early is not None:
+                assert (early > 0) == (expect_early and call != "bwt"), (call, n, early)
+            if call != "bwt":
+                assert np.array_equal(hSA.numpy().astype(np.int64), oSA), (call, n)
+            if call != "sa":
+                assert np.array_equal(hU.numpy(), oU), (call, n)
+
+
 def random_gsa(rng, count, maxlen, k):
     parts = []
     for _ in range(count):
