@@ -27,7 +27,10 @@ struct gsais_ctx {
     int device = -1;
     cudaStream_t stream = nullptr;
     cudaStream_t copy_stream = nullptr;   // device->host copies that overlap later kernels
+    cudaStream_t side_stream = nullptr;   // early BWT and SA patch, beside the sort and the copies
     cudaEvent_t early_ev = nullptr;       // SA may leave for the host (EarlySaCopy)
+    cudaEvent_t copied_ev = nullptr;      // the early SA copy has landed
+    cudaEvent_t bwt_ev = nullptr;         // the early BWT is done
     void *arena = nullptr;
     size_t arena_bytes = 0;
     uint32_t *d_misc = nullptr;   // [0] error word, [1] validity flag
@@ -66,7 +69,10 @@ bool ctx_init(gsais_ctx *c)
     if (cudaGetDevice(&c->device) != cudaSuccess) return false;
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return false;
     if (cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess) return false;
+    if (cudaStreamCreateWithFlags(&c->side_stream, cudaStreamNonBlocking) != cudaSuccess) return false;
     if (cudaEventCreateWithFlags(&c->early_ev, cudaEventDisableTiming) != cudaSuccess) return false;
+    if (cudaEventCreateWithFlags(&c->copied_ev, cudaEventDisableTiming) != cudaSuccess) return false;
+    if (cudaEventCreateWithFlags(&c->bwt_ev, cudaEventDisableTiming) != cudaSuccess) return false;
     if (cudaMalloc(&c->d_misc, 64) != cudaSuccess) return false;
     if (cudaMemset(c->d_misc, 0, 64) != cudaSuccess) return false;
     if (cudaMallocHost(&c->h_small, kSmallWords * sizeof(uint32_t)) != cudaSuccess) return false;
@@ -144,14 +150,14 @@ int64_t fail(cudaError_t)
     } while (0)
 
 // The device's address of a pinned (page-locked) host buffer, or nullptr.
-int32_t *pinned_view(void *p)
+void *pinned_view(void *p)
 {
     cudaPointerAttributes a;
     if (!p || cudaPointerGetAttributes(&a, p) != cudaSuccess) {
         cudaGetLastError();
         return nullptr;
     }
-    return a.type == cudaMemoryTypeHost ? static_cast<int32_t *>(a.devicePointer) : nullptr;
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
 }
 
 // Slots an early SA copy may patch: at most n / 8 (more would make the
@@ -164,20 +170,21 @@ inline uint64_t early_patch_cap(uint64_t n) { return n / 8; }
 bool early_setup(gsais_ctx *c, EarlySaCopy &ec, void *SA, int sa_bytes, uint64_t n, Carver &cv)
 {
     if (sa_bytes != 4 || !SA) return false;
-    int32_t *dev = pinned_view(SA);
+    void *dev = pinned_view(SA);
     if (!dev) return false;
     ec.host = static_cast<int32_t *>(SA);
-    ec.host_dev = dev;
+    ec.host_dev = static_cast<int32_t *>(dev);
     ec.stream = c->copy_stream;
     ec.ready = c->early_ev;
+    ec.copied = c->copied_ev;
     ec.patch_cap = early_patch_cap(n);
-    ec.patch = cv.take<uint32_t>(ec.patch_cap + 1);
+    ec.bits = cv.take<uint32_t>((n + 31) / 32);
     return true;
 }
 
 inline size_t early_bytes(void *SA, int sa_bytes, uint64_t n)
 {
-    return sa_bytes == 4 && pinned_view(SA) ? align_up((early_patch_cap(n) + 1) * 4) : 0;
+    return sa_bytes == 4 && pinned_view(SA) ? align_up((n + 31) / 32 * 4) : 0;
 }
 
 // Waits for a stream when it goes out of scope.
@@ -248,13 +255,17 @@ void gsais_ctx_destroy(gsais_ctx *c)
         DeviceGuard g(c->device);
         if (c->stream) cudaStreamSynchronize(c->stream);
         if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
+        if (c->side_stream) cudaStreamSynchronize(c->side_stream);
         if (c->arena) cudaFree(c->arena);
         if (c->d_misc) cudaFree(c->d_misc);
         if (c->h_small) cudaFreeHost(c->h_small);
         if (c->h_hist) cudaFreeHost(c->h_hist);
         if (c->stream) cudaStreamDestroy(c->stream);
         if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+        if (c->side_stream) cudaStreamDestroy(c->side_stream);
         if (c->early_ev) cudaEventDestroy(c->early_ev);
+        if (c->copied_ev) cudaEventDestroy(c->copied_ev);
+        if (c->bwt_ev) cudaEventDestroy(c->bwt_ev);
     }
     delete c;
 }
@@ -287,8 +298,8 @@ int64_t gsais_run_sa(gsais_ctx *c, const void *T, int symbytes, int64_t n_, int 
     SortWorkspace ws;
     sort_workspace_carve(ws, cv.p, n, symbytes, c->h_small, c->h_hist);
     if (!clear_err(c, st)) return fail(cudaErrorUnknown);
-    cudaStream_t cs = c->copy_stream;
-    StreamJoin join{cs};   // no copy into the caller's buffer outlives the call, also on error returns
+    cudaStream_t cs = c->copy_stream, xs = c->side_stream;
+    StreamJoin join{cs}, join_x{xs};   // no write into the caller's buffers outlives the call
     GS_TRY(cudaMemcpyAsync(d_T, T, n * symbytes, cudaMemcpyHostToDevice, st));
     const int64_t rc = run_sort(c, d_T, symbytes, n, gsa != 0, ws, st, 0, early ? &ec : nullptr);
     if (rc == -1) {
@@ -302,13 +313,14 @@ int64_t gsais_run_sa(gsais_ctx *c, const void *T, int symbytes, int64_t n_, int 
         GS_TRY(widen_u32_to_i64(ws.sa, d_wide, n, st));
         GS_TRY(cudaMemcpyAsync(SA, d_wide, n * 8, cudaMemcpyDeviceToHost, st));
     } else if (ec.started) {
-        GS_TRY(early_sa_patch(ec, ws.sa, n));   // the sort is done: run_sort synchronised st
+        GS_TRY(early_sa_patch(ec, ws.sa, n, xs));   // the sort is done: run_sort synchronised st
     } else {
         GS_TRY(cudaMemcpyAsync(SA, ws.sa, n * 4, cudaMemcpyDeviceToHost, st));
     }
-    const cudaError_t ce = cudaStreamSynchronize(cs);
+    const cudaError_t ce = cudaStreamSynchronize(cs), xe = cudaStreamSynchronize(xs);
     GS_TRY(sync_checked(c, st));
     GS_TRY(ce);
+    GS_TRY(xe);
     emit_freq(c->h_small + 16, symbytes, freq, freq_bytes);
     return 0;
 }
@@ -387,12 +399,30 @@ int64_t gsais_run_bwt(gsais_ctx *c, const void *T, int symbytes, int64_t n_, voi
     int64_t *d_wide = (SA && sa_bytes == 8) ? cv.take<int64_t>(n) : nullptr;
     EarlySaCopy ec;
     const bool early = early_setup(c, ec, SA, sa_bytes, n, cv);
+    void *U_dev = early ? pinned_view(U) : nullptr;   // an early BWT needs U pinned too
     SortWorkspace ws;
     sort_workspace_carve(ws, cv.p, n, symbytes, c->h_small, c->h_hist);
     if (!clear_err(c, st)) return fail(cudaErrorUnknown);
-    cudaStream_t cs = c->copy_stream;
-    StreamJoin join{cs};   // no copy into the caller's buffer outlives the call, also on error returns
+    cudaStream_t cs = c->copy_stream, xs = c->side_stream;
+    StreamJoin join{cs}, join_x{xs};   // no write into the caller's buffers outlives the call
     GS_TRY(cudaMemcpyAsync(d_T, T, n * symbytes, cudaMemcpyHostToDevice, st));
+    // With SA copied early and U pinned, the BWT is also taken early: at that
+    // point SA is final except the recorded slots, whose BWT rows are
+    // rewritten after the sort.  The gather runs on the side stream beside
+    // the rest of the sort; U leaves right behind SA on the copy stream.
+    bool early_u = false;
+    if (U_dev)
+        ec.on_start = [&](cudaStream_t) -> cudaError_t {
+            // unresolved slots may hold anything yet: no bounds error for them
+            cudaError_t e = cudaStreamWaitEvent(xs, ec.ready, 0);
+            if (e == cudaSuccess)
+                e = bwt_gather(d_T, symbytes, ws.sa, ws.slot0, n, d_U, packed_of(ws), nullptr, xs);
+            if (e == cudaSuccess) e = cudaEventRecord(c->bwt_ev, xs);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(cs, c->bwt_ev, 0);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(U, d_U, n * symbytes, cudaMemcpyDeviceToHost, cs);
+            early_u = e == cudaSuccess;
+            return e;
+        };
     const int64_t rc = run_sort(c, d_T, symbytes, n, false, ws, st, 0, early ? &ec : nullptr);
     if (rc != 0) return rc;
     // the sort has completed (run_sort synchronises st): SA leaves on the copy
@@ -403,19 +433,26 @@ int64_t gsais_run_bwt(gsais_ctx *c, const void *T, int symbytes, int64_t n_, voi
             GS_TRY(widen_u32_to_i64(ws.sa, d_wide, n, cs));
             GS_TRY(cudaMemcpyAsync(SA, d_wide, n * 8, cudaMemcpyDeviceToHost, cs));
         } else if (ec.started) {
-            GS_TRY(early_sa_patch(ec, ws.sa, n));
+            GS_TRY(early_sa_patch(ec, ws.sa, n, xs));
         } else {
             GS_TRY(cudaMemcpyAsync(SA, ws.sa, n * 4, cudaMemcpyDeviceToHost, cs));
         }
     }
-    GS_TRY(bwt_gather(d_T, symbytes, ws.sa, ws.rank, n, d_U, packed_of(ws), c->d_misc, st));
+    if (early_u) {
+        // the unresolved rows, written into the host copy behind it on the copy
+        // stream (the SA patch runs beside it on the side stream)
+        GS_TRY(bwt_patch(d_T, symbytes, ws.sa, ws.rank, n, ec.bits, U_dev, packed_of(ws), c->d_misc, cs));
+    } else {
+        GS_TRY(bwt_gather(d_T, symbytes, ws.sa, ws.rank, n, d_U, packed_of(ws), c->d_misc, st));
+        GS_TRY(cudaMemcpyAsync(U, d_U, n * symbytes, cudaMemcpyDeviceToHost, st));
+    }
     if (r > 0) GS_TRY(aux_sample(ws.rank, n, (uint64_t)r, d_I, idx_bytes, st));
     GS_TRY(cudaMemcpyAsync(c->h_small, ws.rank, 4, cudaMemcpyDeviceToHost, st));
-    GS_TRY(cudaMemcpyAsync(U, d_U, n * symbytes, cudaMemcpyDeviceToHost, st));
     if (r > 0) GS_TRY(cudaMemcpyAsync(I, d_I, icount * idx_bytes, cudaMemcpyDeviceToHost, st));
-    const cudaError_t ce = cudaStreamSynchronize(cs);
+    const cudaError_t ce = cudaStreamSynchronize(cs), xe = cudaStreamSynchronize(xs);
     GS_TRY(sync_checked(c, st));
     GS_TRY(ce);
+    GS_TRY(xe);
     const int64_t prim = (int64_t)c->h_small[0];   // ISA[0] + 1
     emit_freq(c->h_small + 16, symbytes, freq, freq_bytes);
     return r > 0 ? 0 : prim;

@@ -59,6 +59,53 @@ __global__ void __launch_bounds__(256) k_bwt(const Sym *__restrict__ T, const ui
             }
             const uint64_t q = p[j];
             if (q == 0 || q > n) {
+                if (err) atomicOr(err, GSAIS_ERR_BOUNDS);
+                continue;
+            }
+            if (pk.pack_bits == 2) {
+                const uint32_t w = reinterpret_cast<const uint16_t *>(pk.packed)[(q - 1) >> 3];
+                U[k] = dec[(w >> (2 * ((q - 1) & 7))) & 3u];
+            } else if (pk.pack_bits == 4) {
+                const uint32_t w = reinterpret_cast<const uint32_t *>(pk.packed)[(q - 1) >> 3];
+                U[k] = dec[(w >> (4 * ((q - 1) & 7))) & 15u];
+            } else {
+                U[k] = T[q - 1];
+            }
+        }
+    }
+}
+
+// BWT rows of the marked SA slots: the rows of slots still unresolved when
+// an early BWT was taken (their U positions are the same under the
+// provisional and the final primary row, as every row between the two lies
+// in suffix 0's group, which is marked).  Address order, a warp per bitmap
+// word, so runs of rows leave as coalesced writes when U is host memory.
+// Bytes: n / 8 read; per marked row SA 4 read, symbol gathered, 1-2 written.
+template <typename Sym>
+__global__ void __launch_bounds__(256) k_bwt_patch(const uint32_t *__restrict__ bits, uint64_t words,
+                                                   const Sym *__restrict__ T, const uint32_t *__restrict__ SA,
+                                                   uint64_t n, const uint32_t *__restrict__ isa1,
+                                                   Sym *__restrict__ U, PackedText pk, uint32_t *__restrict__ err)
+{
+    __shared__ Sym dec[16];
+    if (threadIdx.x < 16) dec[threadIdx.x] = (Sym)pk.decode[threadIdx.x];
+    __syncthreads();
+    const uint64_t i0 = (uint64_t)isa1[0] - 1;
+    const int lane = threadIdx.x & 31;
+    const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+    for (uint64_t base = ((uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; base < words;
+         base += warps * 32) {
+        const uint32_t m = base + lane < words ? bits[base + lane] : 0u;
+        uint32_t nz = __ballot_sync(GSAIS_FULL_MASK, m != 0);
+        while (nz) {
+            const int l = __ffs(nz) - 1;
+            nz &= nz - 1;
+            const uint32_t mw = __shfl_sync(GSAIS_FULL_MASK, m, l);
+            const uint64_t s = (base + (uint64_t)l) * 32 + (uint64_t)lane;
+            if (!((mw >> lane) & 1u) || s >= n || s == i0) continue;
+            const uint64_t k = s < i0 ? s + 1 : s;
+            const uint64_t q = SA[s];
+            if (q == 0 || q > n) {
                 atomicOr(err, GSAIS_ERR_BOUNDS);
                 continue;
             }
@@ -293,6 +340,22 @@ cudaError_t bwt_gather(const void *d_T, int symbytes, const uint32_t *d_SA, cons
     else
         GSAIS_COUNTED((k_bwt<uint16_t><<<grid_for((n + 7) / 8, 256), 256, 0, st>>>(
             static_cast<const uint16_t *>(d_T), d_SA, n, d_isa1, static_cast<uint16_t *>(d_U), pk, err)));
+    return cudaGetLastError();
+}
+
+cudaError_t bwt_patch(const void *d_T, int symbytes, const uint32_t *d_SA, const uint32_t *d_isa1, uint64_t n,
+                      const uint32_t *row_bits, void *U, const PackedText &pk, uint32_t *err, cudaStream_t st)
+{
+    const uint64_t words = (n + 31) / 32;
+    if (words == 0) return cudaSuccess;
+    if (symbytes == 1)
+        GSAIS_COUNTED((k_bwt_patch<uint8_t><<<grid_for(words, 256), 256, 0, st>>>(
+            row_bits, words, static_cast<const uint8_t *>(d_T), d_SA, n, d_isa1, static_cast<uint8_t *>(U), pk,
+            err)));
+    else
+        GSAIS_COUNTED((k_bwt_patch<uint16_t><<<grid_for(words, 256), 256, 0, st>>>(
+            row_bits, words, static_cast<const uint16_t *>(d_T), d_SA, n, d_isa1, static_cast<uint16_t *>(U), pk,
+            err)));
     return cudaGetLastError();
 }
 

@@ -9,6 +9,8 @@ namespace gsais {
 
 // U[0] = T[n-1]; U[k] = T[SA[row]-1] with the primary row skipped
 // (libsais src/libsais.c:7111-7118).  isa1 = rank array (ISA + 1).
+// err == nullptr: rows whose SA entry is out of range are skipped silently
+// (an early BWT, whose unresolved rows are rewritten later).
 // With pack_bits 2 or 4 the symbols are read from the packed code text
 // (positions p at bits [(p % per)*pack_bits, ...) of word p / per) and mapped
 // back through decode[], which keeps the gather inside L2 for DNA-like texts.
@@ -19,6 +21,13 @@ struct PackedText {
 };
 cudaError_t bwt_gather(const void *d_T, int symbytes, const uint32_t *d_SA, const uint32_t *d_isa1, uint64_t n,
                        void *d_U, const PackedText &pk, uint32_t *err, cudaStream_t st);
+
+// U[k] for the BWT rows whose SA slots are marked in row_bits ((n + 31) / 32
+// words), with the final primary row isa1[0] - 1: repairs a BWT taken while
+// those slots were unresolved.  U may be the device's address of pinned
+// host memory.
+cudaError_t bwt_patch(const void *d_T, int symbytes, const uint32_t *d_SA, const uint32_t *d_isa1, uint64_t n,
+                      const uint32_t *row_bits, void *U, const PackedText &pk, uint32_t *err, cudaStream_t st);
 
 // I[t] = ISA[t*r] + 1 for t = 0..(n-1)/r, as int32 (idx_bytes 4) or int64 (8).
 cudaError_t aux_sample(const uint32_t *d_isa1, uint64_t n, uint64_t r, void *d_I, int idx_bytes, cudaStream_t st);

@@ -261,6 +261,7 @@ struct TileArgs {
     uint32_t *rank_out;      // non-null: new ranks go here by list position (scattered later)
     uint32_t *pairs;         // non-null (seed round, plain texts): groups of exactly two leave
     unsigned long long *pair_count;   //   the list; their first slot is appended here
+    uint32_t *slot0;         // non-null (seed round): receives 1 + the slot of suffix 0
     uint64_t N;              // entries in this round
     uint64_t n;              // text length
     uint32_t K;              // seed symbols per key
@@ -537,6 +538,7 @@ __global__ void __launch_bounds__(kAssignThreads, 3)
         const uint32_t r = lastnz(wm, hv_inc[q]);
         if (a.rank_out) a.rank_out[base + x] = r;
         else rank[v] = r;
+        if (MODE != MODE_ROUND && v == 0 && a.slot0) *a.slot0 = (uint32_t)(base + x) + 1;
         const uint32_t bit = 1u << lane;
         if ((rf[q].single | rf[q].pair) & bit) {
             sa[pv[q]] = v;   // a single, or a pair's two members in either order until k_pair_compare
@@ -1264,6 +1266,7 @@ __global__ void __launch_bounds__(256) k_pair_compare(const uint32_t *__restrict
                                                       uint32_t *__restrict__ sa, uint32_t *__restrict__ rank,
                                                       uint32_t *__restrict__ list_pos,
                                                       uint32_t *__restrict__ list_rank,
+                                                      uint32_t *__restrict__ slot0,
                                                       uint32_t *__restrict__ out_i, uint32_t *__restrict__ out_pos,
                                                       uint32_t *__restrict__ out_gid,
                                                       uint32_t *__restrict__ gstart_out,
@@ -1359,6 +1362,7 @@ __global__ void __launch_bounds__(256) k_pair_compare(const uint32_t *__restrict
             const uint32_t lo = res < 0 ? a : b, hi = res < 0 ? b : a;
             sa[P] = lo;
             sa[P + 1] = hi;
+            if (slot0 && (lo == 0 || hi == 0)) *slot0 = P + (lo == 0 ? 1u : 2u);
             if (list_rank) {   // seed ranks not scattered yet: order the pair in the SA-order list
                 list_pos[P] = lo;
                 list_pos[P + 1] = hi;
@@ -1570,6 +1574,7 @@ void sort_workspace_carve(SortWorkspace &ws, void *base, uint64_t n, int symbyte
     for (int i = 0; i < 2; ++i) ws.lvals[i] = reinterpret_cast<uint32_t *>(take(n * 4));
     ws.lpos = reinterpret_cast<uint32_t *>(take(n * 4));
     ws.counters = reinterpret_cast<unsigned long long *>(take(8 * 8));
+    ws.slot0 = reinterpret_cast<uint32_t *>(ws.counters + 7);
     ws.tile_info = reinterpret_cast<uint32_t *>(take(tiles * 16));
     ws.tile_carry = reinterpret_cast<uint32_t *>(take(tiles * 16));
     ws.heads = reinterpret_cast<uint32_t *>(take((tiles * kAssignTile / 32 + 2) * 4));
@@ -1593,16 +1598,38 @@ static int grid_for(uint64_t items, int per_block)
     return (int)(g ? g : 1);
 }
 
-// host[slot] = sa[slot] for the recorded slots, written into pinned host
-// memory over the host link.  Bytes per slot: 4 + 4 read, 4 written.
-__global__ void __launch_bounds__(256) k_sa_patch(const uint32_t *__restrict__ patch, uint64_t m,
-                                                  const uint32_t *__restrict__ sa, uint64_t n,
-                                                  int32_t *__restrict__ host)
+// Sets the bit of every listed SA slot.  Bytes per slot: 4 read, one L2 atomic.
+__global__ void __launch_bounds__(256) k_mark_slots(const uint32_t *__restrict__ slots, uint64_t m, uint64_t n,
+                                                    uint32_t *__restrict__ bits)
 {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < m; j += stride) {
-        const uint32_t slot = patch[j];
-        if (slot < n) host[slot] = (int32_t)sa[slot];
+        const uint64_t s = slots[j];
+        if (s < n) atomicOr(&bits[s >> 5], 1u << (s & 31));
+    }
+}
+
+// host[slot] = sa[slot] for the marked slots, in address order: each warp
+// reads 32 bitmap words at once and takes the non-zero ones in turn, a lane
+// per slot of the word, so a run of marked slots leaves as one coalesced
+// write over the host link.  Bytes: n / 8 read, 8 per marked slot.
+__global__ void __launch_bounds__(256) k_sa_patch(const uint32_t *__restrict__ bits, uint64_t words,
+                                                  const uint32_t *__restrict__ sa, uint64_t n,
+                                                  int32_t *__restrict__ host)
+{
+    const int lane = threadIdx.x & 31;
+    const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+    for (uint64_t base = ((uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; base < words;
+         base += warps * 32) {
+        const uint32_t m = base + lane < words ? bits[base + lane] : 0u;
+        uint32_t nz = __ballot_sync(GSAIS_FULL_MASK, m != 0);
+        while (nz) {
+            const int l = __ffs(nz) - 1;
+            nz &= nz - 1;
+            const uint32_t mw = __shfl_sync(GSAIS_FULL_MASK, m, l);
+            const uint64_t slot = (base + (uint64_t)l) * 32 + (uint64_t)lane;
+            if (((mw >> lane) & 1u) && slot < n) host[slot] = (int32_t)sa[slot];
+        }
     }
 }
 
@@ -1722,18 +1749,19 @@ constexpr uint32_t kPairLimit = 1u << 16;   // symbols compared beyond the share
 static cudaError_t run_pair_compare(SortWorkspace &ws, const PairSource &ps, const uint32_t *pairs, uint64_t max_pairs,
                                     uint64_t skip, uint32_t *out_i, uint32_t *out_pos, uint32_t *out_gid,
                                     uint32_t *gstart_out, uint32_t *d_err, cudaStream_t st,
-                                    uint32_t *list_pos = nullptr, uint32_t *list_rank = nullptr)
+                                    uint32_t *list_pos = nullptr, uint32_t *list_rank = nullptr,
+                                    uint32_t *slot0 = nullptr)
 {
     cudaEvent_t ev_pc = ws.radix.prof ? ws.radix.prof->begin(st) : nullptr;
     const unsigned grid = (unsigned)stream_grid(max_pairs, 256);
     if (ps.pack_bits == 2)
         GSAIS_COUNTED((k_pair_compare<2><<<grid, 256, 0, st>>>(pairs, ws.counters + 3, ws.counters + 4, ps.words, ps.n,
                                                               skip, kPairLimit, ws.sa, ws.rank, list_pos, list_rank,
-                                                              out_i, out_pos, out_gid, gstart_out, ws.counters, d_err)));
+                                                              slot0, out_i, out_pos, out_gid, gstart_out, ws.counters, d_err)));
     else
         GSAIS_COUNTED((k_pair_compare<4><<<grid, 256, 0, st>>>(pairs, ws.counters + 3, ws.counters + 4, ps.words, ps.n,
                                                               skip, kPairLimit, ws.sa, ws.rank, list_pos, list_rank,
-                                                              out_i, out_pos, out_gid, gstart_out, ws.counters, d_err)));
+                                                              slot0, out_i, out_pos, out_gid, gstart_out, ws.counters, d_err)));
     if (ev_pc) ws.radix.prof->end(KK_PAIRS, ev_pc, st, 0);
     return cudaGetLastError();
 }
@@ -1820,6 +1848,7 @@ static cudaError_t run_rounds(SortWorkspace &ws, uint64_t nr, int K, uint32_t ke
             r.rank_out = nullptr;
             r.pairs = nullptr;
             r.pair_count = nullptr;
+            r.slot0 = nullptr;
             r.N = NL;
             r.n = nr;
             r.K = (uint32_t)K;
@@ -2000,6 +2029,7 @@ cudaError_t suffix_sort(const void *d_T, int symbytes, uint64_t n, bool gsa, Sor
     a.rank_out = nullptr;
     a.pairs = nullptr;
     a.pair_count = nullptr;
+    a.slot0 = ws.slot0;
     a.N = n;
     a.n = n;
     a.K = (uint32_t)K;
@@ -2040,7 +2070,8 @@ cudaError_t suffix_sort(const void *d_T, int symbytes, uint64_t n, bool gsa, Sor
             cudaSuccess)
             return e;
         if ((e = run_pair_compare(ws, ps, a.pairs, n / 2, (uint64_t)K, ws.vals[av], ws.pos[pg], ws.gid[pg],
-                                  ws.gstart[pg], d_err, st, a.rank_out ? ws.vals[w] : nullptr, a.rank_out)) !=
+                                  ws.gstart[pg], d_err, st, a.rank_out ? ws.vals[w] : nullptr, a.rank_out,
+                                  ws.slot0)) !=
             cudaSuccess)
             return e;
         unsigned long long *hc = reinterpret_cast<unsigned long long *>(ws.h_small);
@@ -2057,16 +2088,17 @@ cudaError_t suffix_sort(const void *d_T, int symbytes, uint64_t n, bool gsa, Sor
     // (the slots the rounds write are patched afterwards)
     if (opt.early && opt.early->host && kept > 0 && kept <= opt.early->patch_cap) {
         EarlySaCopy &ec = *opt.early;
-        if ((e = cudaMemcpyAsync(ec.patch, ws.pos[pg], (size_t)kept * 4, cudaMemcpyDeviceToDevice, st)) !=
-            cudaSuccess)
-            return e;
+        if ((e = cudaMemsetAsync(ec.bits, 0, (n + 31) / 32 * 4, st)) != cudaSuccess) return e;
+        GSAIS_COUNTED((k_mark_slots<<<stream_grid(kept, 256), 256, 0, st>>>(ws.pos[pg], kept, n, ec.bits)));
         if ((e = cudaEventRecord(ec.ready, st)) != cudaSuccess) return e;
         if ((e = cudaStreamWaitEvent(ec.stream, ec.ready, 0)) != cudaSuccess) return e;
         if ((e = cudaMemcpyAsync(ec.host, ws.sa, n * 4, cudaMemcpyDeviceToHost, ec.stream)) != cudaSuccess)
             return e;
+        if ((e = cudaEventRecord(ec.copied, ec.stream)) != cudaSuccess) return e;
         ec.patch_n = kept;
         ec.started = true;
         S.early_patch = kept;
+        if (ec.on_start && (e = ec.on_start(st)) != cudaSuccess) return e;
     }
     if (a.rank_out && (e = scatter_seed_ranks(ws, ws.vals[w], a.rank_out, n, n, d_err, st)) != cudaSuccess) return e;
 
@@ -2080,11 +2112,13 @@ cudaError_t suffix_sort(const void *d_T, int symbytes, uint64_t n, bool gsa, Sor
     return herr ? cudaErrorUnknown : cudaSuccess;
 }
 
-cudaError_t early_sa_patch(const EarlySaCopy &ec, const uint32_t *d_sa, uint64_t n)
+cudaError_t early_sa_patch(const EarlySaCopy &ec, const uint32_t *d_sa, uint64_t n, cudaStream_t st)
 {
     if (!ec.started || ec.patch_n == 0) return cudaSuccess;
-    GSAIS_COUNTED((k_sa_patch<<<stream_grid(ec.patch_n, 256), 256, 0, ec.stream>>>(ec.patch, ec.patch_n, d_sa, n,
-                                                                                  ec.host_dev)));
+    cudaError_t e = cudaStreamWaitEvent(st, ec.copied, 0);
+    if (e != cudaSuccess) return e;
+    const uint64_t words = (n + 31) / 32;
+    GSAIS_COUNTED((k_sa_patch<<<stream_grid(words, 256), 256, 0, st>>>(ec.bits, words, d_sa, n, ec.host_dev)));
     return cudaGetLastError();
 }
 
@@ -2178,6 +2212,7 @@ cudaError_t batch_suffix_sort(const uint8_t *d_T, uint64_t n, const uint64_t *d_
     a.rank_out = nullptr;
     a.pairs = nullptr;
     a.pair_count = nullptr;
+    a.slot0 = nullptr;
     a.N = n;
     a.n = nr;
     a.K = (uint32_t)K;

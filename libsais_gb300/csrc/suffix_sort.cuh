@@ -1,5 +1,6 @@
 // suffix_sort.cuh -- prefix-doubling suffix sorter (device side, internal).
 #pragma once
+#include <functional>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -23,6 +24,7 @@ struct SortWorkspace {
     uint32_t *heads = nullptr;               // head bit of every entry of an assign (summary -> assign)
     unsigned long long *counters = nullptr;  // 8 round counters: output reservation (groups<<32 | entries),
                                              // large list, medium groups, tied pairs, pair cursor
+    uint32_t *slot0 = nullptr;               // (in counters[7]) 1 + SA slot of suffix 0 after the seed round
     uint32_t *tile_info = nullptr;           // 3 words per assign tile
     uint32_t *tile_carry = nullptr;          // 3 words per assign tile
     uint32_t *totals = nullptr;              // [4] kept entries, kept groups, ...
@@ -52,20 +54,29 @@ constexpr size_t kHostSmallWords = 16 + 65536 + 32768 + kHostEdgeWords;
 // Early device-to-host copy of an int32 suffix array into pinned host
 // memory.  When the seed round (with its tied pairs) leaves at most
 // patch_cap unresolved entries, the sort starts copying SA to `host` on
-// `stream` before the doubling rounds and records the SA slots of those
-// entries in `patch`; the rounds write only those slots, so once the sort is
+// `stream` before the doubling rounds and sets the bits of those entries'
+// SA slots in `bits`; the rounds write only those slots, so once the sort is
 // done early_sa_patch() writes their final values through `host_dev` (the
 // device's address of the same buffer) and the copy of the whole array
-// overlaps the rounds.
+// overlaps the rounds.  The patches go in address order, a warp per 32
+// slots, so the unresolved slots' runs (their groups, adjacent groups
+// merged) leave as coalesced writes: the host link takes scattered 4-byte
+// writes at only a few billion a second.
 struct EarlySaCopy {
     int32_t *host = nullptr;       // destination (the caller's pinned buffer)
     int32_t *host_dev = nullptr;   // the same buffer as the device addresses it
     cudaStream_t stream = nullptr;
     cudaEvent_t ready = nullptr;   // recorded on the sort's stream when the copy may start
-    uint32_t *patch = nullptr;     // device: room for patch_cap slots
+    cudaEvent_t copied = nullptr;  // recorded on `stream` behind the bulk copy
+    uint32_t *bits = nullptr;      // device: (n + 31) / 32 words, one bit per SA slot
     uint64_t patch_cap = 0;
     uint64_t patch_n = 0;          // out: slots recorded
     bool started = false;          // out: the bulk copy is queued on `stream`
+    // Called once the bulk copy is queued (SA final except the recorded
+    // slots; ws.slot0 holds 1 + the slot of suffix 0, provisional when that
+    // slot is recorded); may queue more work on the sort's stream and on
+    // `stream` (an early BWT and its copy).
+    std::function<cudaError_t(cudaStream_t sort_stream)> on_start;
 };
 
 struct SortOptions {
@@ -74,9 +85,9 @@ struct SortOptions {
     EarlySaCopy *early = nullptr;
 };
 
-// Queues, on ec.stream behind the bulk copy, the writes of the recorded
-// slots' final values from d_sa to the host buffer.
-cudaError_t early_sa_patch(const EarlySaCopy &ec, const uint32_t *d_sa, uint64_t n);
+// Queues on `st`, behind the bulk copy (ec.copied), the writes of the
+// recorded slots' final values from d_sa into the host buffer.
+cudaError_t early_sa_patch(const EarlySaCopy &ec, const uint32_t *d_sa, uint64_t n, cudaStream_t st);
 
 // Suffix array of the device text d_T (n symbols of `symbytes` bytes).  gsa
 // sorts as a generalized suffix array with 0 separators (the caller has

@@ -155,12 +155,23 @@ def test_pinned_host_buffers_early_copy(oracle):
     (early_patch > 0 when that path ran).  SA, BWT and primary index must
     equal the oracle's, for libsais and the combined SA + BWT call (and
     libsais_bwt, which returns no SA); a periodic text leaves too many
-    unresolved suffixes and takes the plain copy."""
+    unresolved suffixes and takes the plain copy.  With U pinned too, the
+    BWT is taken at the same point and its unresolved rows rewritten later,
+    including texts whose suffix 0 is still unresolved then (a tied pair, a
+    group of three)."""
     torch = pytest.importorskip("torch")
     lib = G.load()
     rng = np.random.default_rng(23)
+    dna = lambda m: (rng.integers(0, 4, m) + 65).astype(np.uint8)
+    X = dna(5_000)
+    Y = dna(3_000)
+    # suffix 0 in a tied pair (X again at the end; Y three times keeps a
+    # group for the rounds) and in a group of three
+    pair0 = np.concatenate([X, dna(50_000), Y, dna(50_000), Y, dna(50_000), Y, dna(50_000), X])
+    group0 = np.concatenate([X, dna(100_000), X, dna(100_000), X[:4_000]])
     cases = [(textgen.genome_like(1 << 20, seed=5), True),
              (textgen.genome_like(300_001, seed=6), True),
+             (pair0, True), (group0, True),
              ((rng.integers(0, 256, 200_000)).astype(np.uint8), None),
              (np.frombuffer(b"abcab" * 40_000, dtype=np.uint8).copy(), False)]
     for T, expect_early in cases:
