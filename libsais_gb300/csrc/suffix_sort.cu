@@ -291,9 +291,10 @@ __device__ __forceinline__ uint64_t list_key(const TileArgs &a, uint64_t j)
     return a.keys32 ? (uint64_t)a.keys32[j] : a.keys[j];
 }
 
-// One warp per word: keys (and values) of 32 entries, the previous entry's
-// through a shuffle; each warp takes four words per step with all loads
-// issued first.  Bytes per entry: key 4 or 8 (+ value 4 in the plain seed round).
+// One warp per word: keys of 32 entries, the previous entry's through a
+// shuffle; each warp takes four words per step with all loads issued first.
+// (Suffixes shorter than K, whose padded keys may tie with longer ones, get
+// their heads from k_tail_heads.)  Bytes per entry: key 4 or 8.
 template <int MODE>
 __global__ void __launch_bounds__(256) k_heads(TileArgs a, uint32_t *__restrict__ heads)
 {
@@ -303,16 +304,13 @@ __global__ void __launch_bounds__(256) k_heads(TileArgs a, uint32_t *__restrict_
     const uint64_t nw = (uint64_t)gridDim.x * (blockDim.x / 32) * WPS;
     for (uint64_t w0 = ((uint64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5)) * WPS; w0 < words; w0 += nw) {
         uint64_t k[WPS], kp0[WPS];
-        uint32_t v[WPS], vp0[WPS];
 #pragma unroll
         for (int u = 0; u < WPS; ++u) {
             const uint64_t j = (w0 + u) * 32 + lane;
             const bool in = j < a.N;
             k[u] = in ? list_key<MODE>(a, j) : 0ull;
-            v[u] = (MODE == MODE_INIT_PLAIN && in) ? a.vals[j] : 0u;
             const bool first = lane == 0 && j > 0 && in;   // lane 0 loads its predecessor
             kp0[u] = first ? list_key<MODE>(a, j - 1) : 0ull;
-            vp0[u] = (MODE == MODE_INIT_PLAIN && first) ? a.vals[j - 1] : 0u;
         }
 #pragma unroll
         for (int u = 0; u < WPS; ++u) {
@@ -320,18 +318,9 @@ __global__ void __launch_bounds__(256) k_heads(TileArgs a, uint32_t *__restrict_
             const uint64_t j = w * 32 + lane;
             const bool in = j < a.N;
             uint64_t kp = __shfl_up_sync(GSAIS_FULL_MASK, k[u], 1);
-            uint32_t vp = __shfl_up_sync(GSAIS_FULL_MASK, v[u], 1);
-            if (lane == 0) {
-                kp = kp0[u];
-                vp = vp0[u];
-            }
+            if (lane == 0) kp = kp0[u];
             bool head = !in || j == 0 || k[u] != kp;
-            if (!head && MODE == MODE_INIT_PLAIN) {
-                // equal padded keys: suffixes shorter than K differ in length class
-                const uint64_t lc = a.n - v[u] < a.K ? a.n - v[u] : a.K;
-                const uint64_t lcp = a.n - vp < a.K ? a.n - vp : a.K;
-                head = lc != lcp;
-            } else if (!head && MODE == MODE_INIT_GSA) {
+            if (!head && MODE == MODE_INIT_GSA) {
                 head = has_zero_field(k[u], a.zlo, a.zhi);
             }
             const uint32_t bits = __ballot_sync(GSAIS_FULL_MASK, head);
@@ -339,6 +328,54 @@ __global__ void __launch_bounds__(256) k_heads(TileArgs a, uint32_t *__restrict_
         }
     }
 }
+
+// Seed round of a plain text: a suffix shorter than K (position n - K + 1
+// .. n - 1) pads its key with code 0, so the key can tie with a longer
+// suffix's.  Such a suffix is its own group (lengths differ) and its entry
+// comes first among its key's (the seed list is in reverse text order and
+// the sort is stable), shortest first: the head bits of its entry and of the
+// entry after it are set.  One thread per short suffix: its key from the
+// text, the first entry of that key by binary search over the sorted keys,
+// plus the shorter suffixes with the same key.
+template <typename Sym>
+__global__ void __launch_bounds__(64) k_tail_heads(const Sym *__restrict__ T, uint64_t n,
+                                                   const uint16_t *__restrict__ codes, int bits, TileArgs a,
+                                                   uint32_t *__restrict__ heads)
+{
+    __shared__ uint64_t sk[64];
+    const int t = threadIdx.x;   // suffix length t + 1
+    const int K = (int)a.K;
+    const bool act = t < K - 1 && (uint64_t)t < n;
+    uint64_t key = 0;
+    if (act) {
+        const uint64_t p = n - 1 - t;
+        for (int q = 0; q < K; ++q) {
+            const uint64_t c = p + q < n ? (sizeof(Sym) == 4 ? (uint64_t)T[p + q] : (uint64_t)codes[T[p + q]]) : 0ull;
+            key = (key << bits) | c;
+        }
+    }
+    sk[t] = key;
+    __syncthreads();
+    if (!act) return;
+    uint64_t e = 0;
+    for (int u = 0; u < t; ++u) e += sk[u] == key;
+    uint64_t lo = 0, hi = a.N;
+    while (lo < hi) {
+        const uint64_t mid = lo + (hi - lo) / 2;
+        if (list_key<MODE_INIT_PLAIN>(a, mid) < key) lo = mid + 1;
+        else hi = mid;
+    }
+    e += lo;
+    if (e < a.N) atomicOr(&heads[e >> 5], 1u << (e & 31));
+    if (e + 1 < a.N) atomicOr(&heads[(e + 1) >> 5], 1u << ((e + 1) & 31));
+}
+
+struct TailSource {   // the text of a plain seed round, for k_tail_heads
+    const void *T = nullptr;
+    int symbytes = 1;
+    const uint16_t *codes = nullptr;
+    int bits = 0;
+};
 
 struct RowFlags {
     uint32_t head, single, pair, first, kept, kh;   // bit l: entry 32 r + l of the row
@@ -1658,7 +1695,7 @@ static unsigned resident_grid(Kernel kernel, int threads, uint64_t items)
 template <int MODE>
 static cudaError_t run_assign(const TileArgs &a, SortWorkspace &ws, uint32_t *out_i, uint32_t *out_pos,
                               uint32_t *out_gid, uint32_t *gstart_out, const unsigned long long *base,
-                              cudaStream_t st, uint32_t *kept, uint32_t *groups)
+                              cudaStream_t st, uint32_t *kept, uint32_t *groups, const TailSource *tails = nullptr)
 {
     const uint64_t tiles = (a.N + kAssignTile - 1) / kAssignTile;
     KernelProfiler *prof = ws.radix.prof;
@@ -1667,6 +1704,17 @@ static cudaError_t run_assign(const TileArgs &a, SortWorkspace &ws, uint32_t *ou
     const uint64_t hsteps = (words + 31) / 32;   // 8 warps x 4 words per block step
     GSAIS_COUNTED((k_heads<MODE><<<(unsigned)(hsteps < (1u << 16) ? (hsteps ? hsteps : 1) : (1u << 16)), 256, 0, st>>>(
         a, ws.heads)));
+    if (MODE == MODE_INIT_PLAIN && tails && tails->T && a.K > 1) {
+        if (tails->symbytes == 1)
+            GSAIS_COUNTED((k_tail_heads<uint8_t><<<1, 64, 0, st>>>(static_cast<const uint8_t *>(tails->T), a.n,
+                                                                 tails->codes, tails->bits, a, ws.heads)));
+        else if (tails->symbytes == 2)
+            GSAIS_COUNTED((k_tail_heads<uint16_t><<<1, 64, 0, st>>>(static_cast<const uint16_t *>(tails->T), a.n,
+                                                                  tails->codes, tails->bits, a, ws.heads)));
+        else
+            GSAIS_COUNTED((k_tail_heads<uint32_t><<<1, 64, 0, st>>>(static_cast<const uint32_t *>(tails->T), a.n,
+                                                                  tails->codes, tails->bits, a, ws.heads)));
+    }
     GSAIS_COUNTED((k_tile_summary<MODE><<<(unsigned)((tiles + 7) / 8), 256, 0, st>>>(a, ws.heads, ws.tile_info)));
     if (ev) prof->end(KK_SUMMARY, ev, st, a.N * (MODE == MODE_ROUND ? 12 : 16));
     GSAIS_COUNTED((k_tile_scan<<<1, 1024, 0, st>>>(ws.tile_info, ws.tile_carry, tiles, ws.totals, base,
@@ -2056,9 +2104,15 @@ cudaError_t suffix_sort(const void *d_T, int symbytes, uint64_t n, bool gsa, Sor
     if (gsa)
         e = run_assign<MODE_INIT_GSA>(a, ws, ws.vals[av], ws.pos[pg], ws.gid[pg], ws.gstart[pg], nullptr, st, &kept,
                                       &groups);
-    else
+    else {
+        TailSource tails;   // suffixes shorter than K get their heads from the text
+        tails.T = d_T;
+        tails.symbytes = symbytes;
+        tails.codes = ws.codes;
+        tails.bits = bits;
         e = run_assign<MODE_INIT_PLAIN>(a, ws, ws.vals[av], ws.pos[pg], ws.gid[pg], ws.gstart[pg], nullptr, st,
-                                        &kept, &groups);
+                                        &kept, &groups, &tails);
+    }
     if (e != cudaSuccess) return e;
     if (a.pairs) {
         // order the pairs (they share the K seed symbols); unresolved ones are
