@@ -1431,7 +1431,9 @@ __global__ void __launch_bounds__(256) k_pair_compare(const uint32_t *__restrict
 // Each level reads and writes 8 bytes per entry; the window pass reads 8 and
 // writes 4.  No random access reaches DRAM or L2.
 constexpr int kPermItems = 16;
-constexpr int kPermTile = 256 * kPermItems;
+constexpr int kPermThreads = 512;
+constexpr int kPermTile = kPermThreads * kPermItems;   // 8192: runs of ~32 entries per digit
+constexpr size_t kPermSmem = (size_t)2 * kPermTile * sizeof(uint32_t);
 
 __global__ void k_perm_cursors(uint32_t *__restrict__ cursor, uint32_t count, int shift, uint64_t N)
 {
@@ -1448,21 +1450,24 @@ __global__ void k_perm_cursors(uint32_t *__restrict__ cursor, uint32_t count, in
 // cursor[digit]++ (order inside a digit is not kept: the scatter after the
 // last level does not need it).
 template <int RANGE>
-__global__ void __launch_bounds__(256) k_perm_partition(const uint32_t *__restrict__ in_pos,
-                                                        const uint32_t *__restrict__ in_r, uint64_t N, int shift,
-                                                        int lshift, uint32_t *__restrict__ cursor,
-                                                        uint32_t *__restrict__ out_pos, uint32_t *__restrict__ out_r,
-                                                        uint32_t *__restrict__ err)
+__global__ void __launch_bounds__(kPermThreads) k_perm_partition(const uint32_t *__restrict__ in_pos,
+                                                                 const uint32_t *__restrict__ in_r, uint64_t N,
+                                                                 int shift, int lshift,
+                                                                 uint32_t *__restrict__ cursor,
+                                                                 uint32_t *__restrict__ out_pos,
+                                                                 uint32_t *__restrict__ out_r,
+                                                                 uint32_t *__restrict__ err)
 {
-    static_assert(RANGE % 256 == 0, "whole digits per thread");
-    constexpr int PER = RANGE / 256;
-    __shared__ uint32_t s_pos[kPermTile], s_r[kPermTile];
+    constexpr int THREADS = kPermThreads;
+    constexpr int PER = (RANGE + THREADS - 1) / THREADS;   // digits per thread in the scan
+    extern __shared__ uint32_t s_dyn[];
+    uint32_t *s_pos = s_dyn, *s_r = s_dyn + kPermTile;
     __shared__ uint32_t s_cnt[RANGE], s_lstart[RANGE], s_g[RANGE];
-    __shared__ uint32_t s_scan[9];
+    __shared__ uint32_t s_scan[THREADS / 32 + 1];
     const int tid = threadIdx.x;
     const uint64_t t0 = (uint64_t)blockIdx.x * kPermTile;
     const uint32_t valid = (uint32_t)(N - t0 < (uint64_t)kPermTile ? N - t0 : (uint64_t)kPermTile);
-    for (int i = tid; i < RANGE; i += 256) s_cnt[i] = 0;
+    for (int i = tid; i < RANGE; i += THREADS) s_cnt[i] = 0;
     const uint32_t lbase = lshift ? ((in_pos[t0] >> lshift) << (lshift - shift)) : 0u;
     __syncthreads();
     uint32_t p[kPermItems], r[kPermItems];
@@ -1471,7 +1476,7 @@ __global__ void __launch_bounds__(256) k_perm_partition(const uint32_t *__restri
     // all loads of the tile first, then the shared-memory slot counters
 #pragma unroll
     for (int k = 0; k < kPermItems; ++k) {
-        const uint32_t i = k * 256 + tid;
+        const uint32_t i = k * THREADS + tid;
         p[k] = i < valid ? in_pos[t0 + i] : 0xFFFFFFFFu;
         r[k] = i < valid ? in_r[t0 + i] : 0u;
     }
@@ -1492,16 +1497,19 @@ __global__ void __launch_bounds__(256) k_perm_partition(const uint32_t *__restri
     uint32_t c[PER], sum = 0;
 #pragma unroll
     for (int q = 0; q < PER; ++q) {
-        c[q] = s_cnt[tid * PER + q];
+        const uint32_t ld = tid * PER + q;
+        c[q] = ld < RANGE ? s_cnt[ld] : 0u;
         sum += c[q];
     }
     uint32_t total;
-    uint32_t a = block_exclusive_sum<uint32_t, 256>(sum, s_scan, total);
+    uint32_t a = block_exclusive_sum<uint32_t, THREADS>(sum, s_scan, total);
 #pragma unroll
     for (int q = 0; q < PER; ++q) {
         const uint32_t ld = tid * PER + q;
-        s_lstart[ld] = a;
-        s_g[ld] = c[q] ? atomicAdd(&cursor[lbase + ld], c[q]) : 0u;
+        if (ld < RANGE) {
+            s_lstart[ld] = a;
+            s_g[ld] = c[q] ? atomicAdd(&cursor[lbase + ld], c[q]) : 0u;
+        }
         a += c[q];
     }
     __syncthreads();
@@ -1516,7 +1524,7 @@ __global__ void __launch_bounds__(256) k_perm_partition(const uint32_t *__restri
     }
     __syncthreads();
     const uint32_t kept = total;
-    for (uint32_t i = tid; i < kept; i += 256) {
+    for (uint32_t i = tid; i < kept; i += THREADS) {
         const uint32_t q = s_pos[i];
         const uint32_t ld = (q >> shift) - lbase;
         const uint64_t o = (uint64_t)s_g[ld] + (i - s_lstart[ld]);
@@ -1755,9 +1763,20 @@ static cudaError_t scatter_seed_ranks(SortWorkspace &ws, uint32_t *sorted_pos, u
         if ((uint64_t)n1 + n2 > ws.radix.status_words * 2) return cudaErrorInvalidValue;
         GSAIS_COUNTED((k_perm_cursors<<<(n1 + 255) / 256, 256, 0, st>>>(cur, n1, shift1, N)));
         GSAIS_COUNTED((k_perm_cursors<<<(n2 + 255) / 256, 256, 0, st>>>(cur + n1, n2, shift2, N)));
-        GSAIS_COUNTED((k_perm_partition<256><<<(unsigned)tiles, 256, 0, st>>>(sorted_pos, ranks, N, shift1, 0, cur,
-                                                                              ws.lvals[0], ws.lvals[1], d_err)));
-        GSAIS_COUNTED((k_perm_partition<512><<<(unsigned)tiles, 256, 0, st>>>(
+        static bool attr_done[64] = {false};   // dynamic shared memory above 48 KB, per device
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (dev < 0 || dev >= 64 || !attr_done[dev]) {
+            if ((e = cudaFuncSetAttribute(k_perm_partition<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)kPermSmem)) != cudaSuccess ||
+                (e = cudaFuncSetAttribute(k_perm_partition<512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)kPermSmem)) != cudaSuccess)
+                return e;
+            if (dev >= 0 && dev < 64) attr_done[dev] = true;
+        }
+        GSAIS_COUNTED((k_perm_partition<256><<<(unsigned)tiles, kPermThreads, kPermSmem, st>>>(
+            sorted_pos, ranks, N, shift1, 0, cur, ws.lvals[0], ws.lvals[1], d_err)));
+        GSAIS_COUNTED((k_perm_partition<512><<<(unsigned)tiles, kPermThreads, kPermSmem, st>>>(
             ws.lvals[0], ws.lvals[1], N, shift2, shift1, cur + n1, sorted_pos, ranks, d_err)));
         const size_t smem = (size_t)4 << shift2;
         if (smem > 48 * 1024 &&
