@@ -31,6 +31,7 @@ struct gsais_ctx {
     cudaEvent_t early_ev = nullptr;       // SA may leave for the host (EarlySaCopy)
     cudaEvent_t copied_ev = nullptr;      // the early SA copy has landed
     cudaEvent_t bwt_ev = nullptr;         // the early BWT is done
+    cudaEvent_t upload_ev = nullptr;      // a chunk of the text has arrived
     void *arena = nullptr;
     size_t arena_bytes = 0;
     uint32_t *d_misc = nullptr;   // [0] error word, [1] validity flag
@@ -73,6 +74,7 @@ bool ctx_init(gsais_ctx *c)
     if (cudaEventCreateWithFlags(&c->early_ev, cudaEventDisableTiming) != cudaSuccess) return false;
     if (cudaEventCreateWithFlags(&c->copied_ev, cudaEventDisableTiming) != cudaSuccess) return false;
     if (cudaEventCreateWithFlags(&c->bwt_ev, cudaEventDisableTiming) != cudaSuccess) return false;
+    if (cudaEventCreateWithFlags(&c->upload_ev, cudaEventDisableTiming) != cudaSuccess) return false;
     if (cudaMalloc(&c->d_misc, 64) != cudaSuccess) return false;
     if (cudaMemset(c->d_misc, 0, 64) != cudaSuccess) return false;
     if (cudaMallocHost(&c->h_small, kSmallWords * sizeof(uint32_t)) != cudaSuccess) return false;
@@ -221,8 +223,38 @@ SortPlan plan_sort(uint64_t n, int symbytes, size_t extra)
 
 // Sort a device text already placed in the arena.  `sa_override` (nullable)
 // receives SA directly when the caller wants uint32 output in its own buffer.
+// Uploads the text on st in chunks, the symbol histogram following each
+// chunk on xs, so the histogram costs no time of its own; small texts (and
+// other symbol widths) go in one copy and the sort counts them itself.
+// *hist_ready: ws.hist holds the histogram (pass it to run_sort).
+cudaError_t upload_text(gsais_ctx *c, void *d_T, const void *T, int symbytes, uint64_t n, SortWorkspace &ws,
+                        cudaStream_t st, cudaStream_t xs, bool *hist_ready)
+{
+    *hist_ready = false;
+    if (n < (1ull << 24) || (symbytes != 1 && symbytes != 2))
+        return cudaMemcpyAsync(d_T, T, n * symbytes, cudaMemcpyHostToDevice, st);
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(ws.hist, 0, (size_t)(symbytes == 1 ? 256 : 65536) * 4, xs)) != cudaSuccess) return e;
+    const uint64_t chunk = 1ull << 25;   // symbols per copy
+    for (uint64_t off = 0; off < n; off += chunk) {
+        const uint64_t len = n - off < chunk ? n - off : chunk;
+        char *dst = static_cast<char *>(d_T) + off * symbytes;
+        if ((e = cudaMemcpyAsync(dst, static_cast<const char *>(T) + off * symbytes, len * symbytes,
+                                 cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+            (e = cudaEventRecord(c->upload_ev, st)) != cudaSuccess ||
+            (e = cudaStreamWaitEvent(xs, c->upload_ev, 0)) != cudaSuccess ||
+            (e = symbol_histogram_part(dst, symbytes, len, ws.hist, xs)) != cudaSuccess)
+            return e;
+    }
+    if ((e = cudaEventRecord(c->upload_ev, xs)) != cudaSuccess || (e = cudaStreamWaitEvent(st, c->upload_ev, 0)) !=
+                                                                       cudaSuccess)
+        return e;
+    *hist_ready = true;
+    return cudaSuccess;
+}
+
 int64_t run_sort(gsais_ctx *c, const void *d_T, int symbytes, uint64_t n, bool gsa, SortWorkspace &ws,
-                 cudaStream_t st, uint32_t raw_max = 0, EarlySaCopy *early = nullptr)
+                 cudaStream_t st, uint32_t raw_max = 0, EarlySaCopy *early = nullptr, bool hist_ready = false)
 {
     if (gsa) {
         bool valid = true;
@@ -233,6 +265,7 @@ int64_t run_sort(gsais_ctx *c, const void *d_T, int symbytes, uint64_t n, bool g
     SortOptions opt = c->opt;
     opt.raw_max = raw_max;
     opt.early = early;
+    opt.hist_ready = hist_ready;
     GS_TRY(suffix_sort(d_T, symbytes, n, gsa, ws, opt, c->d_misc, st, &c->stats));
     return 0;
 }
@@ -266,6 +299,7 @@ void gsais_ctx_destroy(gsais_ctx *c)
         if (c->early_ev) cudaEventDestroy(c->early_ev);
         if (c->copied_ev) cudaEventDestroy(c->copied_ev);
         if (c->bwt_ev) cudaEventDestroy(c->bwt_ev);
+        if (c->upload_ev) cudaEventDestroy(c->upload_ev);
     }
     delete c;
 }
@@ -300,8 +334,9 @@ int64_t gsais_run_sa(gsais_ctx *c, const void *T, int symbytes, int64_t n_, int 
     if (!clear_err(c, st)) return fail(cudaErrorUnknown);
     cudaStream_t cs = c->copy_stream, xs = c->side_stream;
     StreamJoin join{cs}, join_x{xs};   // no write into the caller's buffers outlives the call
-    GS_TRY(cudaMemcpyAsync(d_T, T, n * symbytes, cudaMemcpyHostToDevice, st));
-    const int64_t rc = run_sort(c, d_T, symbytes, n, gsa != 0, ws, st, 0, early ? &ec : nullptr);
+    bool hist_ready = false;
+    GS_TRY(upload_text(c, d_T, T, symbytes, n, ws, st, xs, &hist_ready));
+    const int64_t rc = run_sort(c, d_T, symbytes, n, gsa != 0, ws, st, 0, early ? &ec : nullptr, hist_ready);
     if (rc == -1) {
         // libsais fills freq before rejecting a malformed GSA text (src/libsais.c:6883-6889)
         GS_TRY(symbol_histogram(d_T, symbytes, n, ws.hist, c->h_small + 16, st));
@@ -405,7 +440,8 @@ int64_t gsais_run_bwt(gsais_ctx *c, const void *T, int symbytes, int64_t n_, voi
     if (!clear_err(c, st)) return fail(cudaErrorUnknown);
     cudaStream_t cs = c->copy_stream, xs = c->side_stream;
     StreamJoin join{cs}, join_x{xs};   // no write into the caller's buffers outlives the call
-    GS_TRY(cudaMemcpyAsync(d_T, T, n * symbytes, cudaMemcpyHostToDevice, st));
+    bool hist_ready = false;
+    GS_TRY(upload_text(c, d_T, T, symbytes, n, ws, st, xs, &hist_ready));
     // With SA copied early and U pinned, the BWT is also taken early: at that
     // point SA is final except the recorded slots, whose BWT rows are
     // rewritten after the sort.  The gather runs on the side stream beside
@@ -423,7 +459,7 @@ int64_t gsais_run_bwt(gsais_ctx *c, const void *T, int symbytes, int64_t n_, voi
             early_u = e == cudaSuccess;
             return e;
         };
-    const int64_t rc = run_sort(c, d_T, symbytes, n, false, ws, st, 0, early ? &ec : nullptr);
+    const int64_t rc = run_sort(c, d_T, symbytes, n, false, ws, st, 0, early ? &ec : nullptr, hist_ready);
     if (rc != 0) return rc;
     // the sort has completed (run_sort synchronises st): SA leaves on the copy
     // stream (or, copied early, gets its late slots) while the BWT gather,

@@ -1977,7 +1977,13 @@ cudaError_t suffix_sort(const void *d_T, int symbytes, uint64_t n, bool gsa, Sor
     if (raw) {
         bits = gsais_bits_for(opt.raw_max > 1 ? opt.raw_max : 1);
     } else {
-        if ((e = symbol_histogram(d_T, symbytes, n, ws.hist, h_hist, st)) != cudaSuccess) return e;
+        if (opt.hist_ready) {
+            if ((e = cudaMemcpyAsync(h_hist, ws.hist, (size_t)nsym * 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+                (e = cudaStreamSynchronize(st)) != cudaSuccess)
+                return e;
+        } else if ((e = symbol_histogram(d_T, symbytes, n, ws.hist, h_hist, st)) != cudaSuccess) {
+            return e;
+        }
         uint32_t sigma = 0;
         for (int c = 0; c < nsym; ++c) {
             h_codes[c] = (uint16_t)sigma;
@@ -2192,6 +2198,18 @@ cudaError_t early_sa_patch(const EarlySaCopy &ec, const uint32_t *d_sa, uint64_t
     if (e != cudaSuccess) return e;
     const uint64_t words = (n + 31) / 32;
     GSAIS_COUNTED((k_sa_patch<<<stream_grid(words, 256), 256, 0, st>>>(ec.bits, words, d_sa, n, ec.host_dev)));
+    return cudaGetLastError();
+}
+
+cudaError_t symbol_histogram_part(const void *d_part, int symbytes, uint64_t len, uint32_t *d_hist, cudaStream_t st)
+{
+    if (len == 0) return cudaSuccess;
+    if (symbytes == 1)
+        GSAIS_COUNTED((k_hist_u8<<<stream_grid(len / 4 + 1, 256), 256, 0, st>>>(static_cast<const uint8_t *>(d_part),
+                                                                                len, d_hist)));
+    else
+        GSAIS_COUNTED((k_hist_u16<<<stream_grid(len, 256), 256, 0, st>>>(static_cast<const uint16_t *>(d_part), len,
+                                                                          d_hist)));
     return cudaGetLastError();
 }
 

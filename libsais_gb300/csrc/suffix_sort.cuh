@@ -83,6 +83,7 @@ struct SortOptions {
     int seed_key_bits = 32;   // width of the packed seed prefix (32 or 64)
     uint32_t raw_max = 0;     // 32-bit integer symbols: the largest symbol value
     EarlySaCopy *early = nullptr;
+    bool hist_ready = false;  // ws.hist already holds the symbol histogram (symbol_histogram_part)
 };
 
 // Queues on `st`, behind the bulk copy (ec.copied), the writes of the
@@ -112,6 +113,9 @@ cudaError_t batch_outputs(const SortWorkspace &ws, const uint8_t *d_T, uint64_t 
 
 // Symbol histogram of a device text into d_hist and the pinned h_hist
 // (256 or 65536 counts); synchronises the stream.
+// Adds the symbols of a stretch of the text to d_hist (no zeroing, no
+// read-back): lets the histogram follow the text's upload chunk by chunk.
+cudaError_t symbol_histogram_part(const void *d_part, int symbytes, uint64_t len, uint32_t *d_hist, cudaStream_t st);
 cudaError_t symbol_histogram(const void *d_T, int symbytes, uint64_t n, uint32_t *d_hist, uint32_t *h_hist,
                              cudaStream_t st);
 
