@@ -171,3 +171,28 @@ def test_new_families_host_checks(lib):
     S16 = np.full(1, 3, np.int64)
     F = np.zeros(65536, np.int64)
     assert lib.libsais16x64(p(U16), p(S16), 1, 0, p(F)) == 0 and S16[0] == 0 and F[500] == 1
+
+
+def test_python_structs_match_the_header(tmp_path):
+    """The ctypes mirrors of the header's structs have the C layout: every
+    field's offset and the struct size, as gcc lays them out."""
+    import libsais_gb300 as G
+    mirrors = {"gsais_stats": G.GsaisStats, "gsais_kernel_profile": G.KernelProfile,
+               "gsais_server_stats": G.ServerStats}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", "#include <libsais_gb300.h>", "int main(void){"]
+    for cname, py in mirrors.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines.append("return 0;}")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    r = subprocess.run(["gcc", "-std=c99", "-I", INCLUDE, str(src), "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l}
+    for cname, py in mirrors.items():
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
