@@ -11,7 +11,8 @@ synthetic data standing in for the genome corpora of libsais's benchmarks.
            HBM by gsais_sa_bwt_device; CUDA events on the launching stream.
   e2e      the same step through the host C-ABI (gsais_sa_bwt) from pinned
            host buffers: H2D of the text and D2H of SA and BWT are inside the
-           timed region.
+           timed region (SA and the BWT leave while the last doubling rounds
+           run; their late slots are rewritten before the call returns).
   roofline the radix-sort digit pass kernel k_radix_pass (the dominant
            kernel): its algorithmic bytes (every key/value pair read and
            written once) over its CUDA-event time inside the timed region,
