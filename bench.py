@@ -8,22 +8,27 @@ substitutions, tandem repeats of period 2-64 x 10-500 copies), seeded
 synthetic data standing in for the genome corpora of libsais's benchmarks.
 
   value    device-resident: text already in HBM, SA (int32) and BWT written to
-           HBM by gsais_sa_bwt_device; CUDA events on the launching stream.
-  e2e      the same step through the host C-ABI (gsais_sa_bwt) from pinned
-           host buffers: H2D of the text and D2H of SA and BWT are inside the
-           timed region (SA and the BWT leave while the last doubling rounds
-           run; their late slots are rewritten before the call returns).
+           HBM by one sort (gsais_sa_bwt_device); CUDA events on the launching
+           stream.
+  e2e      the same metric through the drop-in libsais API from pinned host
+           buffers: libsais() for SA, then libsais_bwt() for the BWT (two
+           sorts, exactly the two calls a libsais user makes); the text goes
+           up in each call and SA and BWT come back inside the timed region.
+           The one-sort host call gsais_sa_bwt is reported beside it.
   roofline the radix-sort digit pass kernel k_radix_pass (the dominant
            kernel): its algorithmic bytes (every key/value pair read and
            written once) over its CUDA-event time inside the timed region,
            against the measured HBM copy bandwidth; traffic = the DRAM bytes
            per algorithmic byte of an ncu capture of the same kernel
            (profiles/radix_pass_traffic.json) times the launch's bytes.
-  cpu_baseline  the CPU oracle port (SA-IS + BWT, 1 thread) on a bounded
-           prefix of the same text.
+  cpu_baseline  the reference libsais built with OpenMP (oracle/_ref), run by
+           this script's reference arm in a child process on the whole
+           workload text with every host thread: libsais_omp + libsais_bwt_omp.
 
---impl reference times the reference's CPU implementation of the step on the
-host cores (the compiled reference where available, else the oracle port).
+--impl reference times that reference step (libsais_omp then libsais_bwt_omp
+on the whole text, all host threads; the oracle port on a prefix only when the
+reference library could not be built).  Its input comes from the oracle's
+build of the text generators, so that arm loads no library of this package.
 """
 from __future__ import annotations
 
@@ -157,66 +162,172 @@ def barrier(dist):
         dist.barrier()
 
 
-def cpu_step(T: np.ndarray):
-    """SA + BWT on the host with the best CPU implementation available here."""
-    from oracle.oracle import REF_SO, Oracle
-    if os.path.exists(REF_SO):
-        try:
-            from oracle.oracle import Reference
-            R = Reference()
-            threads = os.cpu_count() or 1
-            t0 = time.perf_counter()
-            rc, SA, _ = R.libsais(T, threads=threads)
-            i0 = int(np.flatnonzero(SA == 0)[0])
-            U = np.empty_like(T)
-            U[0] = T[-1]
-            rows = np.concatenate([SA[:i0], SA[i0 + 1:]])
-            U[1:] = T[rows - 1]
-            dt = time.perf_counter() - t0
-            return dt, "reference", threads
-        except OSError:
-            pass
+def host_threads() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def bench_config(name: str, n: int) -> dict:
+    """The workload description shared by both arms (identical dicts)."""
+    return {"workload": name, "n": n, "description": WORKLOADS[name][2], "sa": "int32",
+            "outputs": "SA + BWT + primary index", "l2": "inputs larger than L2 (text and SA > 129 MB)"}
+
+
+def reference_text(name: str, n: int) -> np.ndarray:
+    """The workload text from the oracle library's build of the generators
+    (the same C source, so the same bytes as make_text)."""
+    from libsais_gb300 import textgen
+    from oracle.oracle import ORACLE_SO, build
+    if not os.path.exists(ORACLE_SO):
+        build(with_reference=False)
+    textgen.set_library(ORACLE_SO)
+    try:
+        return make_text(name, n)
+    finally:
+        textgen.set_library(None)
+
+
+class ReferenceStep:
+    """One SA+BWT step of the reference libsais: libsais_omp for the suffix array,
+    then libsais_bwt_omp for the BWT and primary index (include/libsais.h:144,
+    :238), on `threads` OpenMP threads.  Output and temporary buffers are
+    allocated and touched once, outside the timed calls."""
+
+    def __init__(self, T: np.ndarray, threads: int):
+        from oracle.oracle import Reference
+        self.lib = Reference().lib
+        self.T = np.ascontiguousarray(T)
+        n = self.T.size
+        self.n, self.threads = n, threads
+        self.SA = np.zeros(n, dtype=np.int32)
+        self.A = np.zeros(n, dtype=np.int32)
+        self.U = np.zeros(n, dtype=np.uint8)
+        self.freq = np.zeros(256, dtype=np.int32)
+
+    def __call__(self):
+        p = lambda a: a.ctypes.data
+        t0 = time.perf_counter()
+        rc = self.lib.libsais_omp(p(self.T), p(self.SA), self.n, 0, p(self.freq), self.threads)
+        t1 = time.perf_counter()
+        prim = self.lib.libsais_bwt_omp(p(self.T), p(self.U), p(self.A), self.n, 0, p(self.freq), self.threads)
+        t2 = time.perf_counter()
+        if rc != 0 or prim < 0:
+            raise SystemExit(f"reference libsais failed: {rc} {prim}")
+        return t2 - t0, t1 - t0, t2 - t1, int(prim)
+
+
+def port_step(T: np.ndarray):
+    """SA-IS + BWT by the oracle port (1 thread), when the reference is absent."""
+    from oracle.oracle import Oracle
     O = Oracle()
     t0 = time.perf_counter()
-    rc, SA = O.sa(T)
+    _, SA = O.sa(T)
     O.bwt_from_sa(T, SA)
-    return time.perf_counter() - t0, "port", 1
+    return time.perf_counter() - t0
 
 
-def run_reference(args, rank, dist):
+def run_reference(args, rank):
+    """The reference arm: libsais built with OpenMP, on the host cores."""
     if rank != 0:
         return
     name = args.workload
     n = args.n or WORKLOADS[name][1]
-    sample = min(n, args.ref_sample)
-    T = make_text(name, n)[:sample].copy()
-    for _ in range(args.warmup):
-        cpu_step(T)
-    times = []
-    kind, cores = "port", 1
-    for _ in range(args.steps):
-        dt, kind, cores = cpu_step(T)
-        times.append(dt)
+    os.environ.setdefault("OMP_PROC_BIND", "close")   # read when the OpenMP runtime loads
+    os.environ.setdefault("OMP_DYNAMIC", "false")
+    from oracle.oracle import REF_SO
+    T = reference_text(name, n)
+    threads = host_threads()
+    detail = {}
+    if os.path.exists(REF_SO):
+        step = ReferenceStep(T, threads)
+        for _ in range(args.warmup):
+            step()
+        times, sa_t, bwt_t = [], [], []
+        for _ in range(args.steps):
+            dt, ds, db, _ = step()
+            times.append(dt)
+            sa_t.append(ds)
+            bwt_t.append(db)
+        kind, cores, sample_n = "reference", threads, n
+        sample = (f"whole workload text (n={n}): libsais_omp + libsais_bwt_omp, {threads} OpenMP threads, "
+                  f"reference libsais {_ref_version()} built with gcc -O3 -fopenmp")
+        detail = {"sa_ms": round(1e3 * statistics.median(sa_t), 1), "bwt_ms": round(1e3 * statistics.median(bwt_t), 1),
+                  "threads": threads, "omp_proc_bind": os.environ.get("OMP_PROC_BIND"),
+                  "step_ms_min_max": [round(1e3 * min(times), 1), round(1e3 * max(times), 1)]}
+    else:
+        sample_n = min(n, args.ref_sample)
+        Ts = T[:sample_n].copy()
+        for _ in range(args.warmup):
+            port_step(Ts)
+        times = [port_step(Ts) for _ in range(args.steps)]
+        kind, cores = "port", 1
+        sample = f"first {sample_n} symbols of the {WORKLOADS[name][2]} (reference library not built here)"
     mean = sum(times) / len(times)
-    value = sample / 1e6 / mean
+    value = sample_n / 1e6 / mean
     line = {
         "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(mean * 1e3, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-        "config": {"workload": name, "n": n, "sample_n": sample, "parallelism": "host CPU"},
-        "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": cores, "kind": kind,
-                         "sample": f"first {sample} symbols of the {WORKLOADS[name][2]}"},
+        "config": bench_config(name, n), "placement": f"host CPU, {cores} threads",
+        "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": cores, "kind": kind, "sample": sample},
         "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "gpu_launches": 0,
     }
+    if detail:
+        line["reference_detail"] = detail
     print(json.dumps(line), flush=True)
 
 
-def run_batched(G, torch, count: int = 4096, steps: int = 3, warmup: int = 1, cpu_strings: int = 32):
+def _ref_version() -> str:
+    from oracle.oracle import reference_dir
+    try:
+        with open(os.path.join(reference_dir(), "VERSION")) as f:
+            return f.read().strip()
+    except OSError:
+        return "?"
+
+
+def cpu_baseline_child(name: str, n: int):
+    """Runs this script's reference arm (1 warm-up + 1 timed step) in a child
+    process and returns its cpu_baseline block: the OpenMP runtime and the
+    reference library stay out of this (CUDA) process."""
+    env = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK")}
+    cmd = [sys.executable, os.path.abspath(__file__), "--impl", "reference", "--baseline-child", "--workload", name,
+           "--n", str(n)]
+    r = subprocess.run(cmd, capture_output=True, text=True, env=env)
+    for ln in reversed(r.stdout.splitlines()):
+        if ln.startswith("{"):
+            line = json.loads(ln)
+            out = dict(line["cpu_baseline"])
+            if "reference_detail" in line:
+                out["detail"] = line["reference_detail"]
+            return out
+    return {"value": None, "unit": UNIT, "cores": 0, "kind": "reference",
+            "sample": "child failed: " + (r.stderr.strip().splitlines() or ["?"])[-1][:160]}
+
+
+def oracle_check_sa_bwt(O, T: np.ndarray, SA: np.ndarray, U: np.ndarray, primary: int) -> bool:
+    """SA passes the oracle's linear-time suffix-array check and the BWT and
+    primary index equal the ones the oracle derives from it."""
+    SA = np.ascontiguousarray(SA, dtype=np.int64)
+    if not O.check_sa(T, SA):
+        return False
+    p, oU, _ = O.bwt_from_sa(T, SA)
+    return p == int(primary) and np.array_equal(oU, U)
+
+
+def run_batched(G, torch, count: int = 4096, steps: int = 3, warmup: int = 1, cpu_strings: int = 32,
+                checked: int = 256):
     """The batched workload: `count` uint8 strings, lengths log-uniform over
     256 B - 4 MiB, i.i.d. ACGT with 1% 'N' (seeded).  Times the batched sort
     (all strings in the same launches) against one GPU call per string on the
-    same device buffers, and checks that both give identical SA/BWT/primary."""
+    same device buffers.  A seeded sample of `checked` strings is checked
+    against the oracle (SA check, BWT and primary index); the batched and
+    per-string outputs are also compared in full."""
     from libsais_gb300 import textgen
+    from oracle.oracle import Oracle
     T, offs = textgen.batch_strings(count, seed=3)
     n = int(offs[-1])
     dT = torch.from_numpy(T).cuda()
@@ -251,9 +362,15 @@ def run_batched(G, torch, count: int = 4096, steps: int = 3, warmup: int = 1, cp
     torch.cuda.synchronize()
     per_string_s = time.perf_counter() - t0
     per_string_launches = G.launch_count() - launches0
-    identical = bool(torch.equal(pSA, dSA) and torch.equal(pU, dU) and np.array_equal(prim, dP.cpu().numpy()))
-    from oracle.oracle import Oracle
+    hSA, hU, hP = dSA.cpu().numpy(), dU.cpu().numpy(), dP.cpu().numpy()
+    identical = bool(torch.equal(pSA, dSA) and torch.equal(pU, dU) and np.array_equal(prim, hP))
     O = Oracle()
+    rng = np.random.default_rng(7)
+    sample = np.unique(np.concatenate([[0, count - 1], rng.choice(count, size=min(checked, count), replace=False)]))
+    ok = True
+    for s in sample:
+        a, b = int(offs[s]), int(offs[s + 1])
+        ok &= oracle_check_sa_bwt(O, T[a:b], hSA[a:b], hU[a:b], int(hP[s]))
     cpu_n = int(offs[cpu_strings])
     t0 = time.perf_counter()
     for s in range(cpu_strings):
@@ -265,7 +382,10 @@ def run_batched(G, torch, count: int = 4096, steps: int = 3, warmup: int = 1, cp
             "batched_ms": round(batched_ms, 2), "batched_launches": batched_launches,
             "per_string_mb_s": round(n / 1e6 / per_string_s, 1), "per_string_ms": round(per_string_s * 1e3, 1),
             "per_string_launches": per_string_launches,
-            "speedup_vs_per_string": round(per_string_s * 1e3 / batched_ms, 2), "identical": identical,
+            "speedup_vs_per_string": round(per_string_s * 1e3 / batched_ms, 2),
+            "batched_equals_per_string": identical, "oracle_checked_strings": int(sample.size),
+            "oracle_sample": "strings 0, count-1 and a seeded (seed 7) sample: SA check + BWT + primary",
+            "oracle_ok": bool(ok),
             "cpu_port_mb_s": round(cpu_n / 1e6 / cpu_s, 2), "cpu_sample": f"first {cpu_strings} strings, 1 thread"}
 
 
@@ -304,8 +424,12 @@ def make_serving_jobs(count: int, seed: int = 6):
 
 
 def run_serving(G, rates=(100, 1000, 5000), max_jobs: int = 600, seconds: float = 4.0, seed: int = 6,
-                budget: int = 120 << 30, workers: int = 3):
-    """Continuous-batching server vs the plain one-job-at-a-time GPU path."""
+                budget: int = 120 << 30, workers: int = 3, oracle_jobs: int = 12):
+    """Continuous-batching server vs the plain one-job-at-a-time GPU path.  The
+    first `oracle_jobs` jobs of at most 8 Mi symbols of each rate are checked
+    against the oracle; every job is compared with the single-job path."""
+    from oracle.oracle import Oracle
+    O = Oracle()
     jobs_all = make_serving_jobs(max_jobs, seed)
     out = {"budget_bytes": budget, "workers": workers, "rates": []}
     from libsais_gb300 import textgen
@@ -315,17 +439,21 @@ def run_serving(G, rates=(100, 1000, 5000), max_jobs: int = 600, seconds: float 
         arrivals = textgen.poisson_arrivals(count, float(rate), seed + 10 + rate)
         srv = G.Server(hbm_budget_bytes=budget, workers=workers, small_job_symbols=1 << 20, max_batch=256)
         ids, hashes, lat, queued = [], [], [], []
+        check = set(int(k) for k in np.flatnonzero([t.size <= (8 << 20) for t in jobs])[:oracle_jobs])
+        checked = []
         t0 = time.perf_counter()
         for k, t in enumerate(jobs):
             delay = arrivals[k] - (time.perf_counter() - t0)
             if delay > 0:
                 time.sleep(delay)
             ids.append(srv.submit(t))
-        for jid in ids:
+        for k, jid in enumerate(ids):
             res, SA, U, q, total, b = srv.wait(jid)
             hashes.append(_job_hash(res, SA, U))
             lat.append(total)
             queued.append(q)
+            if k in check:
+                checked.append((k, res, SA, U))
         st = srv.stats()
         srv.close()
         sym = int(sum(t.size for t in jobs))
@@ -341,6 +469,7 @@ def run_serving(G, rates=(100, 1000, 5000), max_jobs: int = 600, seconds: float 
                                    None, 4)
             same &= _job_hash(res, SA, U) == hashes[k]
         plain_s = time.perf_counter() - t1
+        oracle_ok = all(oracle_check_sa_bwt(O, jobs[k], SA, U, res) for k, res, SA, U in checked)
         out["rates"].append({
             "rate_per_s": rate, "jobs": count, "input_mb": round(sym / 1e6, 1),
             "p50_ms": round(float(np.percentile(lat_ms, 50)), 2), "p95_ms": round(float(np.percentile(lat_ms, 95)), 2),
@@ -349,7 +478,8 @@ def run_serving(G, rates=(100, 1000, 5000), max_jobs: int = 600, seconds: float 
             "plain_one_job_at_a_time_mb_s": round(sym / 1e6 / plain_s, 1),
             "coalesced_batches": st["batches"], "coalesced_jobs": st["batched_jobs"],
             "hbm_high_water_gb": round(st["hbm_high_water_bytes"] / 1e9, 2), "rejected": st["rejected"],
-            "identical_to_single_job_path": bool(same)})
+            "identical_to_single_job_path": bool(same), "oracle_checked_jobs": len(checked),
+            "oracle_ok": bool(oracle_ok)})
     out["footprint_bytes_per_symbol"] = 80.0
     return out
 
@@ -369,15 +499,63 @@ def _timed(torch, fn, steps: int = 3, warmup: int = 1):
     return e0.elapsed_time(e1) / steps
 
 
-def run_plcp_lcp(G, torch, dT, dSA, n: int):
-    """PLCP (Phi + chunked Kasai) and LCP of the resident text and SA."""
+# Algorithmic bytes per symbol: PLCP = Phi (SA read 4, Phi written 4) + the
+# Kasai pass (Phi read 4, PLCP written 4, ~2 text bytes amortised); LCP = SA
+# read 4, PLCP gathered 4, LCP written 4.
+PLCP_BYTES_PER_SYMBOL = 18
+LCP_BYTES_PER_SYMBOL = 12
+
+
+def run_plcp_lcp(G, torch, dT, dSA, n: int, T=None, O=None, gsa: bool = False):
+    """PLCP and LCP of the resident text and SA, with their HBM rooflines
+    (algorithmic bytes / time / measured copy bandwidth); checked against the
+    oracle when T and O are given."""
+    peak, kind = peaks()
     dP = torch.empty_like(dSA)
     dL = torch.empty_like(dSA)
     stream = torch.cuda.current_stream()
-    plcp_ms = _timed(torch, lambda: G.plcp_device(dT, dSA, dP, stream=stream))
+    plcp_ms = _timed(torch, lambda: G.plcp_device(dT, dSA, dP, gsa=gsa, stream=stream))
     lcp_ms = _timed(torch, lambda: G.lcp_device(dP, dSA, dL, stream=stream))
-    return {"plcp_mb_s": round(n / 1e6 / (plcp_ms / 1e3), 1), "plcp_ms": round(plcp_ms, 3),
-            "lcp_mb_s": round(n / 1e6 / (lcp_ms / 1e3), 1), "lcp_ms": round(lcp_ms, 3)}
+    out = {"plcp_mb_s": round(n / 1e6 / (plcp_ms / 1e3), 1), "plcp_ms": round(plcp_ms, 3),
+           "lcp_mb_s": round(n / 1e6 / (lcp_ms / 1e3), 1), "lcp_ms": round(lcp_ms, 3),
+           "roofline": {"plcp": round(PLCP_BYTES_PER_SYMBOL * n / (plcp_ms / 1e3) / 1e9 / peak, 4),
+                        "lcp": round(LCP_BYTES_PER_SYMBOL * n / (lcp_ms / 1e3) / 1e9 / peak, 4),
+                        "unit": f"fraction of {peak} GB/s ({kind})",
+                        "bytes_per_symbol": {"plcp": PLCP_BYTES_PER_SYMBOL, "lcp": LCP_BYTES_PER_SYMBOL}}}
+    if T is not None and O is not None:
+        SA = dSA.cpu().numpy().astype(np.int64)
+        oP = O.plcp(T, SA, gsa=gsa)
+        out["plcp_equals_oracle"] = bool(np.array_equal(dP.cpu().numpy().astype(np.int64), oP))
+        out["lcp_equals_oracle"] = bool(np.array_equal(dL.cpu().numpy().astype(np.int64), O.lcp(oP, SA)))
+    return out
+
+
+def run_stress(G, torch, names=("all_A_2^26", "period7_2^26"), steps: int = 3):
+    """The degenerate texts at n = 2^26: SA+BWT device-resident, checked against
+    the oracle (SA check, BWT and primary index, PLCP and LCP)."""
+    from oracle.oracle import Oracle
+    O = Oracle()
+    out = {}
+    for name in names:
+        n = WORKLOADS[name][1]
+        T = make_text(name, n)
+        dT = torch.from_numpy(T).cuda()
+        dSA = torch.empty(n, dtype=torch.int32, device="cuda")
+        dU = torch.empty(n, dtype=torch.uint8, device="cuda")
+        stream = torch.cuda.current_stream()
+        prim = G.sa_bwt_device(dT, dSA, dU, stream=stream)
+        ms = _timed(torch, lambda: G.sa_bwt_device(dT, dSA, dU, stream=stream), steps=steps)
+        st = G.last_stats()
+        ok = oracle_check_sa_bwt(O, T, dSA.cpu().numpy(), dU.cpu().numpy(), prim)
+        pl = run_plcp_lcp(G, torch, dT, dSA, n, T, O)
+        out[name] = {"n": n, "sa_bwt_mb_s": round(n / 1e6 / (ms / 1e3), 1), "sa_bwt_ms": round(ms, 3),
+                     "rounds": st["rounds"], "radix_passes": st["radix_passes"], "sa_bwt_equals_oracle": bool(ok),
+                     "plcp_ms": pl["plcp_ms"], "lcp_ms": pl["lcp_ms"],
+                     "plcp_lcp_equal_oracle": bool(pl["plcp_equals_oracle"] and pl["lcp_equals_oracle"])}
+        del dT, dSA, dU
+        G.release_workspace()
+        torch.cuda.empty_cache()
+    return out
 
 
 def run_unbwt(G, U: np.ndarray, primary: int, T: np.ndarray, steps: int = 3, cpu_sample: int = 1 << 24):
@@ -432,17 +610,12 @@ def run_gsa(G, torch, reads: int = 1 << 20):
     dSA = torch.empty(n, dtype=torch.int32, device="cuda")
     stream = torch.cuda.current_stream()
     sa_ms = _timed(torch, lambda: G.sa_device(dT, dSA, gsa=True, stream=stream))
-    dP = torch.empty_like(dSA)
-    dL = torch.empty_like(dSA)
-    plcp_ms = _timed(torch, lambda: G.plcp_device(dT, dSA, dP, gsa=True, stream=stream))
-    lcp_ms = _timed(torch, lambda: G.lcp_device(dP, dSA, dL, stream=stream))
     O = Oracle()
-    SA = dSA.cpu().numpy().astype(np.int64)
-    ok_sa = O.check_sa(T, SA, gsa=True)
-    ok_plcp = bool(np.array_equal(dP.cpu().numpy().astype(np.int64), O.plcp(T, SA, gsa=True)))
+    pl = run_plcp_lcp(G, torch, dT, dSA, n, T, O, gsa=True)
+    ok_sa = O.check_sa(T, dSA.cpu().numpy().astype(np.int64), gsa=True)
     return {"reads": reads, "n": n, "gsa_mb_s": round(n / 1e6 / (sa_ms / 1e3), 1), "gsa_ms": round(sa_ms, 3),
-            "plcp_gsa_mb_s": round(n / 1e6 / (plcp_ms / 1e3), 1), "lcp_mb_s": round(n / 1e6 / (lcp_ms / 1e3), 1),
-            "sa_valid": bool(ok_sa), "plcp_matches_oracle": ok_plcp}
+            "plcp_gsa_mb_s": pl["plcp_mb_s"], "lcp_mb_s": pl["lcp_mb_s"], "sa_valid": bool(ok_sa),
+            "plcp_matches_oracle": pl["plcp_equals_oracle"], "lcp_matches_oracle": pl["lcp_equals_oracle"]}
 
 
 def main():
@@ -454,17 +627,22 @@ def main():
     ap.add_argument("--workload", default="genome_like_2^28", choices=sorted(WORKLOADS))
     ap.add_argument("--n", type=int, default=0, help="override the workload length")
     ap.add_argument("--ref-sample", type=int, default=REF_SAMPLE)
+    ap.add_argument("--baseline-child", action="store_true",
+                    help="reference arm as the cpu_baseline of the other arm: 1 warm-up, 1 timed step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--seed-key-bits", type=int, default=0)
-    ap.add_argument("--no-extras", action="store_true", help="skip the batched and serving measurements")
+    ap.add_argument("--no-extras", action="store_true", help="skip the measurements beside the headline")
     ap.add_argument("--batch-strings", type=int, default=4096)
     args = ap.parse_args()
-    args.warmup = max(args.warmup, 3)
+    if args.baseline_child:
+        args.steps, args.warmup = 1, 1
+    else:
+        args.warmup = max(args.warmup, 3)
 
     world, rank, local, dist = dist_setup()
     if args.impl == "reference":
-        run_reference(args, rank, dist)
+        run_reference(args, rank)
         return
 
     import torch
@@ -533,49 +711,84 @@ def main():
                 "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
                 "kernel": "k_radix_pass", "launches_per_step": ks["launches"] / args.steps,
                 "algorithmic_bytes_per_launch": int(per_launch_bytes), "ms_per_launch": round(per_launch_ms, 4)}
-    kernels = {k: {"launches_per_step": v["launches"] / args.steps,
-                   "ms_per_step": round(v["total_ms"] / args.steps, 3)} for k, v in prof.items() if v["launches"]}
+    kernels = {}
+    step_bytes = 0
+    for k, v in prof.items():
+        if not v["launches"]:
+            continue
+        kms = v["total_ms"] / args.steps
+        kb = v["bytes"] / args.steps
+        step_bytes += kb
+        kernels[k] = {"launches_per_step": v["launches"] / args.steps, "ms_per_step": round(kms, 3),
+                      "algorithmic_bytes_per_step": int(kb),
+                      "hbm_frac": round(kb / (kms / 1e3) / 1e9 / peak, 4) if kms > 0 and kb else None}
+    step_roof = {"algorithmic_bytes_per_step": int(step_bytes),
+                 "achieved_gbs": round(step_bytes / (ms / 1e3) / 1e9, 1),
+                 "frac": round(step_bytes / (ms / 1e3) / 1e9 / peak, 4), "peak": peak, "peak_source": peak_kind,
+                 "compulsory_bytes_per_step": 6 * n,
+                 "note": "sum of the algorithmic bytes of the timed kernels per step over ms_per_step"}
 
-    # ---- end to end through the host C-ABI from pinned buffers
-    e2e = None
+    # ---- end to end through the drop-in libsais API from pinned host buffers
+    e2e, e2e_one_sort = None, None
     if not args.no_e2e:
         hT = torch.from_numpy(T).pin_memory()
         hSA = torch.empty(n, dtype=torch.int32).pin_memory()
         hU = torch.empty(n, dtype=torch.uint8).pin_memory()
+        hA = np.empty(n, dtype=np.int32)   # libsais_bwt's temporary array (not written by this library)
+        hF = np.zeros(256, dtype=np.int32)
         lib = G.load()
-        call = lambda: lib.gsais_sa_bwt(None, hT.data_ptr(), 1, n, hSA.data_ptr(), 4, hU.data_ptr(), None, 4)
-        if call() != prim:
-            raise SystemExit("host-path primary index differs from the device path")
-        if not (torch.equal(hSA, dSA.cpu()) and torch.equal(hU, dU.cpu())):
-            raise SystemExit("host-path SA/BWT differ from the device path")
-        for _ in range(max(args.warmup - 1, 1)):   # untimed: the first DMAs map the pinned pages
-            call()
-        barrier(dist)
-        t0 = time.perf_counter()
-        step_ms = []
-        for _ in range(args.steps):
-            t1 = time.perf_counter()
-            call()
-            step_ms.append((time.perf_counter() - t1) * 1e3)
-        e2e_s = (time.perf_counter() - t0) / args.steps
-        e2e_s = reduce_max(dist, e2e_s)
-        e2e = {"value": round(world * n / 1e6 / e2e_s, 3), "unit": UNIT, "h2d_bytes_per_step": n,
-               "d2h_bytes_per_step": n * 4 + n, "ms_per_step": round(e2e_s * 1e3, 3),
-               "step_ms_min_max": [round(min(step_ms), 3), round(max(step_ms), 3)]}
+
+        def dropin():
+            rc = lib.libsais(hT.data_ptr(), hSA.data_ptr(), n, 0, hF.ctypes.data)
+            p = lib.libsais_bwt(hT.data_ptr(), hU.data_ptr(), hA.ctypes.data, n, 0, hF.ctypes.data)
+            return p if rc == 0 else rc
+
+        one_sort = lambda: lib.gsais_sa_bwt(None, hT.data_ptr(), 1, n, hSA.data_ptr(), 4, hU.data_ptr(), None, 4)
+        for fn, label in ((dropin, "libsais + libsais_bwt"), (one_sort, "gsais_sa_bwt")):
+            hSA.fill_(-1)
+            hU.fill_(0)
+            if fn() != prim:
+                raise SystemExit(f"host path ({label}): primary index differs from the device path")
+            if not (torch.equal(hSA, dSA.cpu()) and torch.equal(hU, dU.cpu())):
+                raise SystemExit(f"host path ({label}): SA/BWT differ from the device path")
+        res = {}
+        for fn, key in ((dropin, "dropin"), (one_sort, "one_sort")):
+            for _ in range(max(args.warmup - 1, 1)):   # untimed: the first DMAs map the pinned pages
+                fn()
+            barrier(dist)
+            t0 = time.perf_counter()
+            step_ms = []
+            for _ in range(args.steps):
+                t1 = time.perf_counter()
+                fn()
+                step_ms.append((time.perf_counter() - t1) * 1e3)
+            dt = reduce_max(dist, (time.perf_counter() - t0) / args.steps)
+            res[key] = (dt, step_ms)
+        dt, step_ms = res["dropin"]
+        e2e = {"value": round(world * n / 1e6 / dt, 3), "unit": UNIT, "h2d_bytes_per_step": 2 * n,
+               "d2h_bytes_per_step": n * 4 + n, "ms_per_step": round(dt * 1e3, 3),
+               "step_ms_min_max": [round(min(step_ms), 3), round(max(step_ms), 3)],
+               "api": "libsais() then libsais_bwt() on pinned host buffers (two sorts; the text goes up twice)"}
+        dt, step_ms = res["one_sort"]
+        e2e_one_sort = {"value": round(world * n / 1e6 / dt, 3), "unit": UNIT, "h2d_bytes_per_step": n,
+                        "d2h_bytes_per_step": n * 4 + n, "ms_per_step": round(dt * 1e3, 3),
+                        "step_ms_min_max": [round(min(step_ms), 3), round(max(step_ms), 3)],
+                        "api": "gsais_sa_bwt (SA and BWT from one sort) on pinned host buffers"}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        sample = min(n, args.ref_sample)
-        Ts = T[:sample].copy()
-        dt, kind, cores = cpu_step(Ts)
-        cpu = {"value": round(sample / 1e6 / dt, 3), "unit": UNIT, "cores": cores, "kind": kind,
-               "sample": f"first {sample} symbols of the {WORKLOADS[name][2]}, SA-IS + BWT"}
+        cpu = cpu_baseline_child(name, n)
 
     extras = {}
     if rank == 0 and world == 1 and not args.no_extras:
-        extras["plcp_lcp"] = run_plcp_lcp(G, torch, dT, dSA, n)
+        from oracle.oracle import Oracle
+        O = Oracle()
+        extras["plcp_lcp"] = run_plcp_lcp(G, torch, dT, dSA, n, T, O)
         extras["unbwt"] = run_unbwt(G, dU.cpu().numpy(), prim, T)
+        del dT, dSA, dU
         G.release_workspace()
+        torch.cuda.empty_cache()
+        extras["stress"] = run_stress(G, torch)
         extras["gsa"] = run_gsa(G, torch)
         G.release_workspace()
         extras["batched"] = run_batched(G, torch, count=args.batch_strings)
@@ -588,14 +801,13 @@ def main():
             "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-            "config": {"workload": name, "n": n, "description": WORKLOADS[name][2], "sa": "int32",
-                       "outputs": "SA + BWT + primary index", "l2": "inputs larger than L2 (text and SA > 129 MB)",
-                       "parallelism": "replicas" if world > 1 else "single GPU",
-                       "rounds": stats["rounds"], "seed_symbols": stats["seed_symbols"],
-                       "radix_passes": stats["radix_passes"], "active_total": stats["active_total"],
-                       "pairs_direct": stats["pairs_direct"], "large_total": stats["large_total"]},
-            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-            "kernels": kernels, "clocks": clocks,
+            "config": bench_config(name, n),
+            "placement": "replicas" if world > 1 else "single GPU",
+            "sort_stats": {"rounds": stats["rounds"], "seed_symbols": stats["seed_symbols"],
+                           "radix_passes": stats["radix_passes"], "active_total": stats["active_total"],
+                           "pairs_direct": stats["pairs_direct"], "large_total": stats["large_total"]},
+            "roofline": roof, "step_roofline": step_roof, "cpu_baseline": cpu, "e2e": e2e,
+            "e2e_one_sort": e2e_one_sort, "gpu_launches": launches, "kernels": kernels, "clocks": clocks,
         }
         line.update(extras)
         print(json.dumps(line), flush=True)

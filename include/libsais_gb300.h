@@ -166,14 +166,38 @@ extern "C" {
     void gsais_release_workspace(void * ctx);
 
     /**
+    * Test hook for the bounded device waits (no counterpart in the reference).  With
+    * limit_ns > 0, every full tile of the radix digit pass, after its staging copies
+    * have landed, also waits on a barrier that nothing arrives on and gives up after
+    * limit_ns nanoseconds: the wait's error bit is raised, the tile is staged again
+    * with plain loads, and the sort returns -2 (src/libsais.c:6930-6932 uses -2 for
+    * internal failures).  0 switches it off.  Applies to the current device.
+    * @return 0, -1 for a limit outside [0, 1e9], -2 on a CUDA failure.
+    */
+    int32_t gsais_test_stall_radix_wait(int64_t limit_ns);
+
+    /**
+    * Test hook (no counterpart in the reference): the next `count` device workspace
+    * allocations of any context fail as if the device were out of memory, so the
+    * calls that need them return -2 as the reference does on a failed allocation
+    * (src/libsais.c:6930-6932).  0 switches it off.
+    * @return 0, or -1 for a negative count.
+    */
+    int32_t gsais_test_fail_allocations(int32_t count);
+
+    /**
     * Suffix array of a device-resident text, allocating nothing.  No counterpart in
-    * the reference libsais: it exists for callers that cannot call cudaMalloc (code
-    * running under CUDA graph capture, inside a framework whose allocator owns all
-    * device memory, or on paths where an allocation may block).  All scratch comes
-    * from one fixed 6 MiB __device__ array that every GPU loading this library
-    * reserves until the library is unloaded; calls share it, so calls that overlap
-    * on the GPU race.  The first call on each device looks up the array's address
-    * (cudaGetSymbolAddress); make it before any stream capture.
+    * the reference libsais.  It serves callers that cannot call cudaMalloc: a plugin
+    * running inside an application whose caching allocator owns the device's memory
+    * (cudaMalloc there can fail on memory the allocator holds, and can synchronise
+    * the device under the host's other streams), and latency-critical paths.  All
+    * scratch comes from one fixed 6 MiB __device__ array that every GPU loading this
+    * library reserves until the library is unloaded.  Calls share the array, which
+    * keeps the previous call's contents (the sort clears what must start at zero),
+    * and calls whose work overlaps on one GPU race on it; a host mutex admits one call
+    * at a time and the call returns only after its work on `stream` has finished
+    * (error returns drain `stream` first).  The first call on each device looks up
+    * the array's device address (cudaGetSymbolAddress, that device current).
     * @param T [0..n-1] Device pointer to the text (symbytes 1 or 2).
     * @param n The text length, at most 65536 symbols (longer texts return -1).
     * @param gsa Non-zero for the generalized suffix array (0 separators, T[n-1] == 0).

@@ -155,6 +155,8 @@ _SIGS = {
     "gsais_profile_reset": (None, [_p]),
     "gsais_launch_count": (_i64, []),
     "gsais_sa_device_noalloc": (_i64, [_p, _i32, _i64, _i32, _p, _p]),
+    "gsais_test_stall_radix_wait": (_i32, [_i64]),
+    "gsais_test_fail_allocations": (_i32, [_i32]),
     "gsais_batch_sa_bwt": (_i64, [_p, _p, _p, _i32, _p, _p, _p]),
     "gsais_batch_sa_bwt_device": (_i64, [_p, _p, _i64, _p, _i32, _p, _p, _p, _p]),
     "gsais_server_create": (_p, [_i64, _i32, _i64, _i32]),

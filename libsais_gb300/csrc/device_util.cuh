@@ -84,16 +84,23 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
 }
 
 // Bounded wait on an mbarrier phase.  Returns false (and raises the error
-// bit) if the phase did not complete within the limit.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, uint32_t *err)
+// bit) if the phase did not complete within limit_ns nanoseconds (or
+// GSAIS_SPIN_LIMIT polls).
+__device__ __forceinline__ bool mbar_wait_bounded_ns(uint64_t *bar, uint32_t parity, uint32_t *err,
+                                                     uint64_t limit_ns)
 {
     const uint64_t t0 = global_ns();
     for (uint32_t it = 0; it < GSAIS_SPIN_LIMIT; ++it) {
         if (mbar_try_wait(bar, parity)) return true;
-        if ((it & 255) == 255 && global_ns() - t0 > GSAIS_SPIN_NS) break;
+        if ((it & 255) == 255 && global_ns() - t0 > limit_ns) break;
     }
     atomicOr(err, GSAIS_ERR_MBARRIER_SPIN);
     return false;
+}
+
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, uint32_t *err)
+{
+    return mbar_wait_bounded_ns(bar, parity, err, GSAIS_SPIN_NS);
 }
 
 __device__ __forceinline__ uint32_t lanemask_lt()

@@ -83,9 +83,15 @@ bool ctx_init(gsais_ctx *c)
     return true;
 }
 
+// Test hook: the next g_fail_allocs workspace allocations fail as if the
+// device were out of memory (gsais_test_fail_allocations).
+std::atomic<int32_t> g_fail_allocs{0};
+
 bool ensure_arena(gsais_ctx *c, size_t bytes)
 {
     if (c->arena_bytes >= bytes) return true;
+    for (int32_t k = g_fail_allocs.load(); k > 0;)
+        if (g_fail_allocs.compare_exchange_weak(k, k - 1)) return false;
     if (c->arena) {
         cudaFree(c->arena);
         c->arena = nullptr;
@@ -861,6 +867,23 @@ void gsais_profile_reset(void *ctx)
 }
 
 int64_t gsais_launch_count(void) { return (int64_t)g_launches.load(); }
+
+int32_t gsais_test_stall_radix_wait(int64_t limit_ns)
+{
+    if (limit_ns < 0 || limit_ns > 1000000000ll) return -1;
+    if (set_test_stall_wait((uint64_t)limit_ns) != cudaSuccess) {
+        cudaGetLastError();
+        return -2;
+    }
+    return 0;
+}
+
+int32_t gsais_test_fail_allocations(int32_t count)
+{
+    if (count < 0) return -1;
+    g_fail_allocs.store(count);
+    return 0;
+}
 
 void gsais_release_workspace(void *ctx)
 {

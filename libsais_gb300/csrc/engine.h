@@ -74,6 +74,10 @@ cudaError_t radix_sort_pairs32(uint32_t *keys[2], uint32_t *vals[2], uint64_t n,
 cudaError_t radix_partition32(uint32_t *keys[2], uint32_t *vals[2], uint64_t n, int begin_bit, int end_bit,
                               RadixScratch &rs, uint32_t *d_err, cudaStream_t st, int *which);
 
+// Test hook: limit (ns) of an extra bounded wait that every full radix tile
+// makes on a barrier nothing arrives on (0 = off); set on the current device.
+cudaError_t set_test_stall_wait(uint64_t limit_ns);
+
 // --------------------------------------------------------------- statistics
 struct SortStats {
     int rounds = 0;                // doubling rounds after the seed sort

@@ -1,13 +1,17 @@
 // noalloc.cu -- suffix array of a device-resident text without allocating
 // any memory.
 //
-// Some callers cannot call cudaMalloc: code that runs while a CUDA graph is
-// being captured, code inside a framework whose caching allocator owns all
-// device memory, and real-time paths where an allocation may block.  For
-// them this file provides gsais_sa_device_noalloc, which runs the same
-// prefix-doubling suffix sort as gsais_sa_device but takes all of its
-// scratch from one file-scope __device__ array of fixed size, so the call
-// itself allocates nothing (no cudaMalloc/cudaFree, no pinned host memory).
+// Some callers cannot call cudaMalloc.  A plugin that runs inside a host
+// application whose caching allocator owns all of the device's memory (a
+// deep-learning framework, a database engine) must not allocate behind that
+// allocator's back: cudaMalloc can fail for want of free memory the
+// allocator is holding, and it can synchronise the whole device, stalling
+// the host's other streams.  Latency-critical callers avoid it for the same
+// reason.  For them this file provides gsais_sa_device_noalloc, which runs
+// the same prefix-doubling suffix sort as gsais_sa_device but takes all of
+// its device scratch from one file-scope __device__ array of fixed size, so
+// the call itself allocates nothing (no cudaMalloc/cudaFree, no pinned host
+// memory, no library routine that allocates).
 //
 // Limits and sharing rules:
 //   * texts of at most kNoAllocMaxN = 65,536 symbols; longer texts get -1;
@@ -15,11 +19,14 @@
 //     GPU that loads this library, for as long as the library stays loaded;
 //   * every call uses the same array and the array keeps the previous call's
 //     contents; the sort clears everything that must start at zero;
-//   * calls are serialised on the host by a mutex, but calls that overlap on
-//     the GPU (for example from two processes sharing the module, or a
-//     caller that replays captured work concurrently) race on the array;
+//   * calls whose work overlaps on one GPU race on the array.  Each CUDA
+//     context has its own copy of it, so separate processes never share it;
+//     within one process a host mutex admits one call at a time and every
+//     call returns only after the work it queued on `stream` has finished
+//     (an error return first drains `stream`), so calls made one after
+//     another, from any thread, do not overlap;
 //   * the first call on each device looks up the array's device address with
-//     cudaGetSymbolAddress; make that first call before any stream capture.
+//     cudaGetSymbolAddress (with that device current) and keeps it.
 #include <cstring>
 #include <mutex>
 
@@ -62,6 +69,17 @@ void *scratch_for(int dev)
     return g_scratch_addr[dev];
 }
 
+// Error return: no kernel of this call may still use the shared array once
+// the mutex is released, so the stream is drained first (its own error, if
+// any, is cleared; the call fails either way).
+int64_t fail_drained(cudaStream_t st)
+{
+    cudaGetLastError();
+    cudaStreamSynchronize(st);
+    cudaGetLastError();
+    return -2;
+}
+
 }  // namespace
 
 extern "C" int64_t gsais_sa_device_noalloc(const void *T, int32_t symbytes, int64_t n, int32_t gsa, void *SA,
@@ -87,22 +105,15 @@ extern "C" int64_t gsais_sa_device_noalloc(const void *T, int32_t symbytes, int6
     SortWorkspace ws;
     sort_workspace_carve(ws, base + 256, (uint64_t)n, symbytes, g_host_small, g_host_hist);
     ws.sa = static_cast<uint32_t *>(SA);
-    if (cudaMemsetAsync(d_err, 0, 8, st) != cudaSuccess) {
-        cudaGetLastError();
-        return -2;
-    }
+    if (cudaMemsetAsync(d_err, 0, 8, st) != cudaSuccess) return fail_drained(st);
     if (gsa) {
         bool valid = true;
-        if (gsa_validate(T, symbytes, (uint64_t)n, d_err + 1, g_host_flag, st, &valid) != cudaSuccess) {
-            cudaGetLastError();
-            return -2;
-        }
+        if (gsa_validate(T, symbytes, (uint64_t)n, d_err + 1, g_host_flag, st, &valid) != cudaSuccess)
+            return fail_drained(st);
         if (!valid) return -1;
     }
     SortOptions opt;
-    if (suffix_sort(T, symbytes, (uint64_t)n, gsa != 0, ws, opt, d_err, st, nullptr) != cudaSuccess) {
-        cudaGetLastError();
-        return -2;
-    }
+    if (suffix_sort(T, symbytes, (uint64_t)n, gsa != 0, ws, opt, d_err, st, nullptr) != cudaSuccess)
+        return fail_drained(st);
     return 0;
 }

@@ -28,6 +28,17 @@ namespace {
 
 constexpr int kHistCopies = 4;
 
+}  // namespace
+
+// Test hook (gsais_test_stall_radix_wait): when non-zero, every full tile of
+// k_radix_pass, after its staging copies have landed, also waits on a second
+// mbarrier that nothing arrives on, giving up after this many nanoseconds.
+// The give-up path is the one a real staging timeout takes: the error bit is
+// raised (the call returns -2) and the tile is staged again with plain loads.
+__device__ uint64_t g_test_stall_wait_ns = 0;
+
+namespace {
+
 // Histograms of every digit pass in one read of the keys (used when the
 // producer of the keys did not accumulate them).  Counters are replicated
 // kHistCopies times (by warp) to spread shared-atomic traffic.
@@ -175,14 +186,17 @@ __global__ void __launch_bounds__(PassShape<K>::kThreads, PassShape<K>::kMinBloc
     __shared__ uint32_t s_gbase[256];
     __shared__ uint32_t s_scan[WARPS + 1];
     __shared__ __align__(8) uint64_t s_bar;
+    __shared__ __align__(8) uint64_t s_never;   // test hook only: no thread arrives on it
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint32_t tile = blockIdx.x;
     const uint64_t base = (uint64_t)tile * TILE;
     const uint32_t valid = (uint32_t)((n - base) < (uint64_t)TILE ? (n - base) : (uint64_t)TILE);
     const bool full = valid == TILE;
+    const uint64_t stall_ns = full ? g_test_stall_wait_ns : 0;
     if (tid == 0 && full) {
         mbar_init(&s_bar, 1);
+        if (stall_ns) mbar_init(&s_never, 1);
         mbar_arrive_expect_tx(&s_bar, TILE * (uint32_t)(sizeof(K) + sizeof(uint32_t)));
         bulk_copy_g2s(s_keys, kin + base, TILE * sizeof(K), &s_bar);
         bulk_copy_g2s(s_vals, vin + base, TILE * sizeof(uint32_t), &s_bar);
@@ -190,9 +204,20 @@ __global__ void __launch_bounds__(PassShape<K>::kThreads, PassShape<K>::kMinBloc
     for (int i = tid; i < WARPS * 256; i += THREADS) (&s_whist[0][0])[i] = 0;
     const uint32_t gofs = offs[(uint64_t)tid * tiles + tile];
     __syncthreads();
+    bool staged = true;
     if (full) {
-        mbar_wait_bounded(&s_bar, 0, err);
-    } else {
+        bool landed = mbar_wait_bounded(&s_bar, 0, err);
+        staged = landed;
+        if (landed && stall_ns) staged = mbar_wait_bounded_ns(&s_never, 0, err, stall_ns);
+        // A wait that gave up has raised the error bit (the call will return
+        // -2).  The tile is then staged again with plain loads, so the pass
+        // still writes a permutation of its input and no later kernel reads
+        // stale entries as indexes; copies still in flight get one more
+        // bounded wait first (they write the same bytes).
+        staged = __syncthreads_and(staged);
+        if (!staged && !landed) mbar_wait_bounded(&s_bar, 0, err);
+    }
+    if (!full || !staged) {
         for (uint32_t i = tid; i < valid; i += THREADS) {
             s_keys[i] = kin[base + i];
             s_vals[i] = vin[base + i];
@@ -379,6 +404,11 @@ cudaError_t sort_impl(K *keys[2], uint32_t *vals[2], uint64_t n, int begin_bit, 
 }
 
 }  // namespace
+
+cudaError_t set_test_stall_wait(uint64_t limit_ns)
+{
+    return cudaMemcpyToSymbol(g_test_stall_wait_ns, &limit_ns, sizeof(limit_ns));
+}
 
 cudaError_t read_back(void *h_dst, const void *d_src, size_t bytes, cudaStream_t st)
 {

@@ -19,6 +19,15 @@ _u64 = ctypes.c_uint64
 _p = ctypes.c_void_p
 _d = ctypes.c_double
 _tg = None
+_tg_path = None   # None: lib/libtextgen.so
+
+
+def set_library(path=None) -> None:
+    """Load the generators from another build of textgen.c (None: the package's
+    lib/libtextgen.so).  The CPU-only reference timing uses the oracle's copy, so
+    that it loads no library of this package."""
+    global _tg, _tg_path
+    _tg, _tg_path = None, path
 
 ACGT = np.frombuffer(b"ACGT", dtype=np.uint8)
 
@@ -26,9 +35,10 @@ ACGT = np.frombuffer(b"ACGT", dtype=np.uint8)
 def _lib():
     global _tg
     if _tg is None:
-        if not os.path.exists(TEXTGEN_SO):
+        path = _tg_path or TEXTGEN_SO
+        if _tg_path is None and not os.path.exists(TEXTGEN_SO):
             build()
-        lib = ctypes.CDLL(TEXTGEN_SO)
+        lib = ctypes.CDLL(path)
         lib.tg_iid_u8.argtypes = [_p, _u64, _p, ctypes.c_int, _u64]
         lib.tg_dna_with_n.argtypes = [_p, _u64, _d, _u64]
         lib.tg_constant.argtypes = [_p, _u64, ctypes.c_uint8]

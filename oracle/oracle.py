@@ -33,13 +33,31 @@ _i64 = ctypes.c_int64
 _i32 = ctypes.c_int32
 
 
+ROOT = os.path.dirname(HERE)
+STAGED_REF = os.path.join(ROOT, "baseline", "_ref")
+
+
+def reference_dir() -> str:
+    """Source tree the reference is compiled from: $LIBSAIS_REFERENCE_DIR, else
+    the staged copy under baseline/_ref (made by ``make -C oracle stage``)."""
+    return os.environ.get("LIBSAIS_REFERENCE_DIR") or STAGED_REF
+
+
 def build(with_reference: bool = True) -> None:
-    """Compile liboracle.so (and the reference, when its sources are present)."""
+    """Compile liboracle.so (and the reference, when its sources are present).
+
+    Without $LIBSAIS_REFERENCE_DIR and without a staged copy, the Makefile's
+    ``stage`` recipe is tried first; where no reference source tree exists it
+    fails quietly and only liboracle.so is built."""
     targets = ["all"]
-    ref_dir = os.environ.get("LIBSAIS_REFERENCE_DIR", "/root/reference")
+    ref_dir = reference_dir()
+    if with_reference and not os.environ.get("LIBSAIS_REFERENCE_DIR") and \
+            not os.path.isdir(os.path.join(ref_dir, "src")):
+        subprocess.run(["make", "-s", "-C", HERE, "stage"], stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
     if with_reference and os.path.isdir(os.path.join(ref_dir, "src")):
         targets.append("ref")
-    subprocess.run(["make", "-s", "-C", HERE, "-j4", f"REF={ref_dir}"] + targets, check=True)
+    jobs = str(max(4, min(8, os.cpu_count() or 4)))
+    subprocess.run(["make", "-s", "-C", HERE, "-j" + jobs, f"REF={ref_dir}"] + targets, check=True)
 
 
 def _ptr(a: np.ndarray) -> int:
