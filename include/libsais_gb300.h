@@ -141,6 +141,43 @@ extern "C" {
     /** Seed key width in bits (32 or 64) used by later sorts on ctx; returns the previous width. */
     int32_t gsais_set_seed_key_bits(void * ctx, int32_t bits);
 
+    /**
+    * Tuning parameters of the suffix sort (no counterpart in the reference, which
+    * has no tunables on this path).  digit_bits: radix digit width (8);
+    * radix_items32 / radix_items64: keys per thread of a radix digit pass over 32-bit
+    * (16, 20, 24, 28) and 64-bit (12, 16, 20) keys, the tile being 256 threads times
+    * that; medium_small (64..512) and medium_max (medium_small..4096): unsorted groups
+    * of up to medium_small members are split by a 128-thread CTA, up to medium_max by
+    * a 256-thread CTA, larger ones by the global segmented radix sort.
+    */
+    typedef struct gsais_tuning
+    {
+        int32_t digit_bits;
+        int32_t radix_items32;
+        int32_t radix_items64;
+        int32_t medium_small;
+        int32_t medium_max;
+    } gsais_tuning;
+
+    /**
+    * Fixes the tuning of later sorts on ctx (NULL: the process-wide context).  t == NULL
+    * goes back to the autotuner cache (its entry for the GPU, the alphabet's code bits
+    * and the nearest n bucket) or the built-in defaults.
+    * @return 0, or -1 for values outside the ranges above.
+    */
+    int32_t gsais_set_tuning(void * ctx, const gsais_tuning * t);
+
+    /** The tuning the last sort on ctx ran with. */
+    int32_t gsais_last_tuning(void * ctx, gsais_tuning * out);
+
+    /**
+    * Loads the autotuner cache (the JSON file libsais_gb300.autotune writes; path NULL:
+    * $GSAIS_TUNING_CACHE, which is also read on first use).  Sorts without a tuning of
+    * their own take its entry for their GPU, code bits and nearest n bucket.
+    * @return the number of entries loaded, or -1 if the file is missing or malformed.
+    */
+    int32_t gsais_load_tuning_cache(const char * path);
+
     /** Per-kernel timing record (CUDA events on the launching stream). */
     typedef struct gsais_kernel_profile
     {

@@ -155,6 +155,9 @@ _SIGS = {
     "gsais_profile_reset": (None, [_p]),
     "gsais_launch_count": (_i64, []),
     "gsais_sa_device_noalloc": (_i64, [_p, _i32, _i64, _i32, _p, _p]),
+    "gsais_set_tuning": (_i32, [_p, _p]),
+    "gsais_last_tuning": (_i32, [_p, _p]),
+    "gsais_load_tuning_cache": (_i32, [ctypes.c_char_p]),
     "gsais_test_stall_radix_wait": (_i32, [_i64]),
     "gsais_test_fail_allocations": (_i32, [_i32]),
     "gsais_batch_sa_bwt": (_i64, [_p, _p, _p, _i32, _p, _p, _p]),
@@ -175,6 +178,37 @@ class GsaisStats(ctypes.Structure):
     _fields_ = [("rounds", _i32), ("seed_symbols", _i32), ("seed_bits", _i32), ("radix_passes", _i32),
                 ("active_total", _i64), ("workspace_bytes", _i64), ("large_total", _i64),
                 ("pairs_direct", _i64), ("early_patch", _i64)]
+
+
+class GsaisTuning(ctypes.Structure):
+    _fields_ = [("digit_bits", _i32), ("radix_items32", _i32), ("radix_items64", _i32), ("medium_small", _i32),
+                ("medium_max", _i32)]
+
+
+TUNING_DEFAULTS = {"digit_bits": 8, "radix_items32": 24, "radix_items64": 16, "medium_small": 512,
+                   "medium_max": 4096}
+
+
+def set_tuning(tuning=None, ctx=None) -> int:
+    """gsais_set_tuning: fix the sort's tuning on ctx (a dict of GsaisTuning
+    fields, missing ones from TUNING_DEFAULTS), or None for cache/defaults."""
+    lib = load()
+    h = ctx.handle if ctx else None
+    if tuning is None:
+        return int(lib.gsais_set_tuning(h, None))
+    t = GsaisTuning(**{**TUNING_DEFAULTS, **tuning})
+    return int(lib.gsais_set_tuning(h, ctypes.byref(t)))
+
+
+def last_tuning(ctx=None) -> dict:
+    lib = load()
+    t = GsaisTuning()
+    lib.gsais_last_tuning(ctx.handle if ctx else None, ctypes.byref(t))
+    return {k: getattr(t, k) for k, _ in GsaisTuning._fields_}
+
+
+def load_tuning_cache(path=None) -> int:
+    return int(load().gsais_load_tuning_cache(path.encode() if path else None))
 
 
 class KernelProfile(ctypes.Structure):

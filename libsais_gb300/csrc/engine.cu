@@ -747,7 +747,8 @@ static int64_t batch_run(gsais_ctx *c, const uint8_t *d_T, int64_t n_, const uin
     sort_workspace_carve(ws, cv.p, n + (uint64_t)count, 1, c->h_small, c->h_hist);
     ws.radix.prof = &c->prof;
     if (!clear_err(c, st)) return fail(cudaErrorUnknown);
-    GS_TRY(batch_suffix_sort(d_T, n, d_offs, (uint32_t)count, ws, c->d_misc, st, &c->stats));
+    GS_TRY(batch_suffix_sort(d_T, n, d_offs, (uint32_t)count, ws, c->d_misc, st, &c->stats,
+                             c->opt.tuning_set ? &c->opt.tuning : nullptr));
     GS_TRY(batch_outputs(ws, d_T, n, d_offs, (uint32_t)count, d_SA, d_U, d_primary, c->d_misc, st));
     GS_TRY(sync_checked(c, st));
     return 0;
@@ -829,6 +830,44 @@ int32_t gsais_set_seed_key_bits(void *ctx, int32_t bits)
     c->opt.seed_key_bits = bits;
     return prev;
 }
+
+int32_t gsais_set_tuning(void *ctx, const gsais_tuning *t)
+{
+    gsais_ctx *c = resolve(ctx);
+    if (!c) return -1;
+    std::lock_guard<std::mutex> lock(c->mu);
+    if (!t) {
+        c->opt.tuning_set = false;
+        c->opt.tuning = Tuning();
+        return 0;
+    }
+    Tuning tn;
+    tn.digit_bits = t->digit_bits;
+    tn.radix_items32 = t->radix_items32;
+    tn.radix_items64 = t->radix_items64;
+    tn.medium_small = t->medium_small;
+    tn.medium_max = t->medium_max;
+    if (!tuning_valid(tn)) return -1;
+    c->opt.tuning = tn;
+    c->opt.tuning_set = true;
+    return 0;
+}
+
+int32_t gsais_last_tuning(void *ctx, gsais_tuning *out)
+{
+    gsais_ctx *c = resolve(ctx);
+    if (!c || !out) return -1;
+    std::lock_guard<std::mutex> lock(c->mu);
+    const Tuning &tn = c->stats.tuning;
+    out->digit_bits = tn.digit_bits;
+    out->radix_items32 = tn.radix_items32;
+    out->radix_items64 = tn.radix_items64;
+    out->medium_small = tn.medium_small;
+    out->medium_max = tn.medium_max;
+    return 0;
+}
+
+int32_t gsais_load_tuning_cache(const char *path) { return tuning_load_cache(path); }
 
 int32_t gsais_profile_enable(void *ctx, int32_t on)
 {

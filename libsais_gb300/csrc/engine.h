@@ -7,6 +7,8 @@
 #include <atomic>
 #include <vector>
 
+#include "tuning.h"
+
 namespace gsais {
 
 // Number of kernels this library has launched (all contexts).
@@ -55,9 +57,14 @@ struct RadixScratch {
     size_t status_words = 0;
     uint32_t *h_hist = nullptr;    // pinned host copy of hist
     KernelProfiler *prof = nullptr;
+    int items32 = 24;              // keys per thread of a digit pass, 32-bit keys (16, 20, 24, 28)
+    int items64 = 16;              // the same for 64-bit keys (12, 16, 20)
 };
 
 size_t radix_status_words(uint64_t n);
+// Whether a digit-pass instance with `items` keys per thread is compiled for
+// keys of key_bytes (4 or 8) bytes.
+bool radix_items_supported(int key_bytes, int items);
 
 // Sorts keys[0]/vals[0] by key bits [0, end_bit).  keys[1]/vals[1] are the
 // alternate buffers.  On success returns 0 and sets *which to the buffer
@@ -67,9 +74,11 @@ size_t radix_status_words(uint64_t n);
 cudaError_t radix_sort_pairs(uint64_t *keys[2], uint32_t *vals[2], uint64_t n, int end_bit,
                              RadixScratch &rs, uint32_t *d_err, cudaStream_t st, int *which,
                              int *passes_run, bool hist_ready = false);
+// implicit_vals: vals[0] is not read; value i is n - 1 - i (seed keys written
+// in reverse text order carry their suffix index implicitly).
 cudaError_t radix_sort_pairs32(uint32_t *keys[2], uint32_t *vals[2], uint64_t n, int end_bit,
                                RadixScratch &rs, uint32_t *d_err, cudaStream_t st, int *which,
-                               int *passes_run, bool hist_ready = false);
+                               int *passes_run, bool hist_ready = false, bool implicit_vals = false);
 // Stable partition of (uint32 key, value) pairs by key bits [begin_bit, end_bit).
 cudaError_t radix_partition32(uint32_t *keys[2], uint32_t *vals[2], uint64_t n, int begin_bit, int end_bit,
                               RadixScratch &rs, uint32_t *d_err, cudaStream_t st, int *which);
@@ -88,6 +97,7 @@ struct SortStats {
     uint64_t pairs_direct = 0;     // tied pairs ordered by direct comparison
     uint64_t early_patch = 0;      // SA slots written to the host after an early SA copy
     int radix_passes = 0;          // non-trivial digit passes over all sorts
+    Tuning tuning;                 // the tuning the sort ran with
 };
 
 }  // namespace gsais

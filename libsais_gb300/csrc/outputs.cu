@@ -5,9 +5,12 @@
 // n before it is used as an address; a bad index raises GSAIS_ERR_BOUNDS in
 // the context's error word and the access is skipped, so a malformed caller
 // array becomes a -2 return instead of a device fault.
+#include <type_traits>
+
 #include "device_util.cuh"
 #include "engine.h"
 #include "outputs.cuh"
+#include "suffix_sort.cuh"
 
 namespace gsais {
 
@@ -73,6 +76,90 @@ __global__ void __launch_bounds__(256) k_bwt(const Sym *__restrict__ T, const ui
             }
         }
     }
+}
+
+// The same gather with four consecutive output symbols per thread, stored
+// as one 4-byte (8-bit symbols) or 8-byte (16-bit symbols) word: U must be
+// aligned to that word.  Rows per thread per step: 4 x B, all SA loads first,
+// then all gathers.
+template <typename Sym>
+__device__ __forceinline__ Sym bwt_symbol(const Sym *__restrict__ T, uint64_t q, const uint8_t *packed,
+                                          int pack_bits, const Sym *dec)
+{
+    if (pack_bits == 2) {
+        const uint32_t w = __ldg(reinterpret_cast<const uint16_t *>(packed) + ((q - 1) >> 3));
+        return dec[(w >> (2 * ((q - 1) & 7))) & 3u];
+    }
+    if (pack_bits == 4) {
+        const uint32_t w = __ldg(reinterpret_cast<const uint32_t *>(packed) + ((q - 1) >> 3));
+        return dec[(w >> (4 * ((q - 1) & 7))) & 15u];
+    }
+    return T[q - 1];
+}
+
+template <typename Sym>
+__global__ void __launch_bounds__(256, 4) k_bwt_words(const Sym *__restrict__ T, const uint32_t *__restrict__ SA,
+                                                      uint64_t n, const uint32_t *__restrict__ isa1,
+                                                      Sym *__restrict__ U, PackedText pk, uint32_t *__restrict__ err)
+{
+    constexpr int B = 2;
+    using Word = typename std::conditional<sizeof(Sym) == 1, uint32_t, uint2>::type;
+    __shared__ Sym dec[16];
+    if (threadIdx.x < 16) dec[threadIdx.x] = (Sym)pk.decode[threadIdx.x];
+    __syncthreads();
+    const uint8_t *packed = pk.packed;
+    const int pack_bits = pk.pack_bits;
+    const uint64_t i0 = (uint64_t)isa1[0] - 1;   // SA row of suffix 0
+    const uint64_t words = (n + 3) / 4;
+    const uint64_t span = (uint64_t)gridDim.x * blockDim.x * B;
+    bool bad = false;
+    for (uint64_t w0 = (uint64_t)blockIdx.x * blockDim.x * B + threadIdx.x; w0 < words; w0 += span) {
+        uint32_t p[B][4];
+#pragma unroll
+        for (int j = 0; j < B; ++j)
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const uint64_t k = (w0 + (uint64_t)j * blockDim.x) * 4 + r;
+                const uint64_t row = k <= i0 ? k - 1 : k;
+                p[j][r] = (k > 0 && k < n && row < n) ? SA[row] : 0u;
+            }
+#pragma unroll
+        for (int j = 0; j < B; ++j) {
+            const uint64_t w = w0 + (uint64_t)j * blockDim.x;
+            if (w >= words) break;
+            Sym v[4];
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const uint64_t k = w * 4 + r;
+                const uint64_t q = p[j][r];
+                v[r] = 0;
+                if (k == 0) {
+                    v[r] = T[n - 1];
+                } else if (k < n) {
+                    if (q == 0 || q > n) bad = true;
+                    else v[r] = bwt_symbol(T, q, packed, pack_bits, dec);
+                }
+            }
+            if (w * 4 + 4 <= n) {
+                Word out;
+                if (sizeof(Sym) == 1) {
+                    reinterpret_cast<uint32_t &>(out) = (uint32_t)v[0] | ((uint32_t)v[1] << 8) |
+                                                         ((uint32_t)v[2] << 16) | ((uint32_t)v[3] << 24);
+                } else {
+                    uint2 o2;
+                    o2.x = (uint32_t)v[0] | ((uint32_t)v[1] << 16);
+                    o2.y = (uint32_t)v[2] | ((uint32_t)v[3] << 16);
+                    reinterpret_cast<uint2 &>(out) = o2;
+                }
+                reinterpret_cast<Word *>(U)[w] = out;
+            } else {
+#pragma unroll
+                for (int r = 0; r < 4; ++r)
+                    if (w * 4 + r < n) U[w * 4 + r] = v[r];
+            }
+        }
+    }
+    if (bad && err) atomicOr(err, GSAIS_ERR_BOUNDS);
 }
 
 // BWT rows of the marked SA slots: the rows of slots still unresolved when
@@ -181,7 +268,8 @@ __global__ void __launch_bounds__(256) k_int_narrow(const I *__restrict__ T, uin
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) out[i] = (O)T[i];
 }
 
-// Phi[SA[j]] = SA[j-1], Phi[SA[0]] = n (src/libsais.c:8116 compute_phi).
+// Phi[SA[j]] = SA[j-1], Phi[SA[0]] = n (src/libsais.c:8116 compute_phi), by
+// a direct scatter (texts too small for the position partitions).
 // Bytes per row: SA 4 + 4 read, Phi 4 scattered.
 __global__ void __launch_bounds__(256) k_phi(const uint32_t *__restrict__ SA, uint64_t n, uint32_t *__restrict__ phi,
                                              uint32_t *__restrict__ err)
@@ -197,41 +285,163 @@ __global__ void __launch_bounds__(256) k_phi(const uint32_t *__restrict__ SA, ui
     }
 }
 
-// Length of the common prefix of suffixes a and b, known to be >= l0,
-// extended by one warp 32 symbols per step.  Plain texts stop at the text
-// end (src/libsais.c:8177: m = n - max(i, k)); GSA stops at a separator.
-template <typename Sym, bool GSA>
-__device__ __forceinline__ uint64_t warp_extend(const Sym *__restrict__ T, uint64_t n, uint64_t a, uint64_t b,
-                                                uint64_t l0)
+// ---- symbol comparison on 8-byte windows of the text.  The text is read as
+// aligned 64-bit words (a window at any byte offset is two words and a
+// funnel shift); a word not wholly inside the text is assembled byte by byte,
+// bytes past the end reading as 0 (every caller clamps lengths to the text).
+struct TextWords {
+    const uint8_t *T;   // the text
+    uint64_t nbytes;    // its length in bytes
+    uint32_t mis;       // T's offset past the previous 8-byte boundary
+};
+
+__device__ __forceinline__ uint64_t load8(const TextWords &tw, uint64_t off)
 {
+    const uint64_t a = off + tw.mis;
+    const uint64_t w = a >> 3;
+    const uint32_t sh = (uint32_t)(a & 7) * 8;
+    const uint64_t end = tw.mis + tw.nbytes;   // in aligned coordinates
+    if (w * 8 >= tw.mis && (w + 2) * 8 <= end) {
+        const uint64_t *W = reinterpret_cast<const uint64_t *>(tw.T - tw.mis);
+        const uint64_t lo = __ldg(W + w);
+        if (sh == 0) return lo;
+        const uint64_t hi = __ldg(W + w + 1);
+        return (lo >> sh) | (hi << (64 - sh));
+    }
+    uint64_t v = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+        if (off + k < tw.nbytes) v |= (uint64_t)tw.T[off + k] << (8 * k);
+    return v;
+}
+
+// Equal leading symbols of two 8-byte windows (S-byte symbols, little
+// endian); GSA also stops at a 0 symbol of x (a separator ends a suffix).
+template <int S, bool GSA>
+__device__ __forceinline__ uint32_t eq_symbols(uint64_t x, uint64_t y)
+{
+    uint64_t stop = x ^ y;
+    if (GSA) {
+        // lowest flagged symbol = the first 0 symbol (borrows only run upwards)
+        if (S == 1) stop |= (x - 0x0101010101010101ull) & ~x & 0x8080808080808080ull;
+        if (S == 2) stop |= (x - 0x0001000100010001ull) & ~x & 0x8000800080008000ull;
+    }
+    const uint32_t bit = stop ? (uint32_t)(__ffsll((long long)stop) - 1) : 64u;
+    return bit / (8 * S);
+}
+
+// First mismatch offset >= l of the suffixes at p and q, at most m (one
+// thread, 8 bytes per step).  Plain texts: m = n - max(p, q) (src/libsais.c:8177);
+// GSA also stops at a separator (:8215-8238).
+template <typename Sym, bool GSA>
+__device__ __forceinline__ uint64_t extend_thread(const TextWords &tw, uint64_t p, uint64_t q, uint64_t l, uint64_t m)
+{
+    constexpr int S = sizeof(Sym), PER = 8 / S;
+    while (l < m) {
+        const uint32_t c = eq_symbols<S, GSA>(load8(tw, (p + l) * S), load8(tw, (q + l) * S));
+        l += c;
+        if (c < PER) break;
+    }
+    return l < m ? l : m;
+}
+
+// Equal leading symbols of the 16-byte windows at symbol offset o (capped at
+// m - o; 0 if o >= m).
+template <typename Sym, bool GSA>
+__device__ __forceinline__ uint32_t lane_window(const TextWords &tw, uint64_t p, uint64_t q, uint64_t o, uint64_t m)
+{
+    constexpr int S = sizeof(Sym), HALF = 8 / S;
+    if (o >= m) return 0;
+    uint32_t c = eq_symbols<S, GSA>(load8(tw, (p + o) * S), load8(tw, (q + o) * S));
+    if (c == HALF) c += eq_symbols<S, GSA>(load8(tw, (p + o + HALF) * S), load8(tw, (q + o + HALF) * S));
+    return (uint64_t)c > m - o ? (uint32_t)(m - o) : c;
+}
+
+// One warp extends from l, 16 bytes per lane per step, for at most `iters`
+// steps.  Returns the first mismatch offset (<= m) with *done, or the offset
+// reached with !*done.
+template <typename Sym, bool GSA>
+__device__ __forceinline__ uint64_t extend_warp(const TextWords &tw, uint64_t p, uint64_t q, uint64_t l, uint64_t m,
+                                                int iters, bool *done)
+{
+    constexpr int PER = 16 / sizeof(Sym);
     const int lane = threadIdx.x & 31;
-    const uint64_t m = n - (a > b ? a : b);
-    if (l0 > m) l0 = m;
-    for (;;) {
-        const uint64_t x = l0 + lane;
-        bool match;
-        if (!GSA) {
-            match = x < m && T[a + x] == T[b + x];
-        } else {
-            match = x < m && T[a + x] != 0 && T[a + x] == T[b + x];
+    for (int it = 0; it < iters; ++it) {
+        if (l >= m) {
+            *done = true;
+            return m;
         }
-        const uint32_t bad = __ballot_sync(GSAIS_FULL_MASK, !match);
-        if (bad) return l0 + (uint64_t)(__ffs(bad) - 1);
-        l0 += 32;
+        const uint64_t o = l + (uint64_t)lane * PER;
+        const uint32_t c = lane_window<Sym, GSA>(tw, p, q, o, m);
+        const uint32_t ball = __ballot_sync(GSAIS_FULL_MASK, c < (uint32_t)PER);
+        if (ball) {
+            const int f = __ffs(ball) - 1;
+            const uint64_t r = l + (uint64_t)f * PER + __shfl_sync(GSAIS_FULL_MASK, c, f);
+            *done = true;
+            return r < m ? r : m;
+        }
+        l += 32 * PER;
+    }
+    *done = false;
+    return l;
+}
+
+// PLCP of the first chunk start (position 0) from scratch, by every CTA of the
+// grid: CTA g compares blocks g, g + grid, ... of 16 bytes per thread and
+// lowers sparse[0] to the first mismatch it finds; a block that starts at or
+// beyond the value already found is skipped.  sparse[0] holds m (or 0) on entry.
+template <typename Sym, bool GSA>
+__global__ void __launch_bounds__(256) k_plcp_first(TextWords tw, uint64_t n, const uint32_t *__restrict__ phi,
+                                                    uint32_t *sparse)
+{
+    constexpr int PER = 16 / sizeof(Sym);
+    constexpr uint64_t BLK = 256 * PER;
+    const uint64_t b = phi[0];
+    if (b >= n) return;   // suffix 0 is first in SA (or a bad entry): PLCP 0
+    const uint64_t m = n - b;   // a = 0 < b
+    __shared__ unsigned long long s_min;
+    __shared__ uint32_t s_cur;
+    for (uint64_t g = blockIdx.x;; g += gridDim.x) {
+        const uint64_t o0 = g * BLK;
+        if (threadIdx.x == 0) {
+            s_cur = *reinterpret_cast<volatile uint32_t *>(sparse);
+            s_min = ~0ull;
+        }
+        __syncthreads();
+        if (o0 >= m || o0 >= s_cur) break;   // the same decision in every thread
+        const uint64_t o = o0 + (uint64_t)threadIdx.x * PER;
+        const uint32_t c = lane_window<Sym, GSA>(tw, 0, b, o, m);
+        if (c < (uint32_t)PER) atomicMin(&s_min, (unsigned long long)(o + c));
+        __syncthreads();
+        if (threadIdx.x == 0 && s_min != ~0ull) atomicMin(sparse, (uint32_t)(s_min < m ? s_min : m));
+        __syncthreads();
     }
 }
 
-// One level of exact PLCP values at chunk starts: chunk k = (2w+1)*half
-// takes its lower bound from chunk k - half (PLCP[i+d] >= PLCP[i] - d).
+__global__ void k_plcp_first_init(const uint32_t *__restrict__ phi, uint64_t n, uint32_t *__restrict__ sparse,
+                                  uint32_t *__restrict__ level_counts, int levels, uint32_t *__restrict__ err)
+{
+    const uint64_t b = phi[0];
+    if (b > n) atomicOr(err, GSAIS_ERR_BOUNDS);
+    sparse[0] = b >= n ? 0u : (uint32_t)(n - b);
+    for (int k = 0; k < levels; ++k) level_counts[k] = 0;
+}
+
+// One level of exact PLCP values at chunk starts: chunk k = (2w+1)*half takes
+// its lower bound from chunk k - half (PLCP[i+d] >= PLCP[i] - d).  A warp per
+// chunk start extends for at most kLevelIters steps; starts still matching
+// go to the long list for k_plcp_long.
+constexpr int kLevelIters = 8;
+
 template <typename Sym, bool GSA>
-__global__ void __launch_bounds__(256) k_plcp_level(const Sym *__restrict__ T, uint64_t n,
-                                                    const uint32_t *__restrict__ phi, uint32_t chunk,
-                                                    uint64_t nchunks, uint64_t half, uint32_t *__restrict__ sparse,
-                                                    uint32_t *__restrict__ err)
+__global__ void __launch_bounds__(256) k_plcp_level(TextWords tw, uint64_t n, const uint32_t *__restrict__ phi,
+                                                    uint32_t chunk, uint64_t nchunks, uint64_t half,
+                                                    uint32_t *__restrict__ sparse, uint2 *__restrict__ long_list,
+                                                    uint32_t *__restrict__ long_count, uint32_t *__restrict__ err)
 {
     const uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint64_t k = half == 0 ? w : (2 * w + 1) * half;
-    if (k >= nchunks || (half == 0 && k > 0)) return;
+    const uint64_t k = (2 * w + 1) * half;
+    if (k >= nchunks) return;
     const uint64_t a = k * chunk;
     uint64_t b = phi[a];
     if (b > n) {
@@ -239,92 +449,212 @@ __global__ void __launch_bounds__(256) k_plcp_level(const Sym *__restrict__ T, u
         b = n;
     }
     uint64_t l = 0;
+    bool done = true;
     if (b != n) {
-        uint64_t lb = 0;
-        if (half != 0) {
-            const uint64_t kp = k - half;
-            const uint64_t d = a - kp * chunk;
-            const uint64_t lp = sparse[kp];
-            lb = lp > d ? lp - d : 0;
-        }
-        l = warp_extend<Sym, GSA>(T, n, a, b, lb);
+        const uint64_t kp = k - half;
+        const uint64_t d = a - kp * chunk;
+        const uint64_t lp = sparse[kp];
+        const uint64_t m = n - (a > b ? a : b);
+        l = lp > d ? lp - d : 0;
+        if (l > m) l = m;
+        l = extend_warp<Sym, GSA>(tw, a, b, l, m, kLevelIters, &done);
     }
-    if ((threadIdx.x & 31) == 0) sparse[k] = (uint32_t)l;
+    if ((threadIdx.x & 31) == 0) {
+        if (done) {
+            sparse[k] = (uint32_t)l;
+        } else {
+            const uint32_t slot = atomicAdd(long_count, 1u);
+            long_list[slot] = make_uint2((uint32_t)k, (uint32_t)l);
+        }
+    }
 }
 
-// Kasai's carried length inside each chunk, starting from the exact value at
-// the chunk start (src/libsais.c:8167 compute_plcp restarts at block starts
-// too).  Phi is read and overwritten by PLCP in place.
+// The long extensions of one level: a CTA per listed start, 256 threads x 16
+// bytes per step.
 template <typename Sym, bool GSA>
-__global__ void __launch_bounds__(256) k_plcp_chunks(const Sym *__restrict__ T, uint64_t n, uint32_t chunk,
-                                                     uint64_t nchunks, const uint32_t *__restrict__ sparse,
-                                                     uint32_t *__restrict__ plcp, uint32_t *__restrict__ err)
+__global__ void __launch_bounds__(256) k_plcp_long(TextWords tw, uint64_t n, const uint32_t *__restrict__ phi,
+                                                   uint32_t chunk, uint32_t *__restrict__ sparse,
+                                                   const uint2 *__restrict__ long_list,
+                                                   const uint32_t *__restrict__ long_count)
 {
-    const uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nchunks) return;
-    const uint64_t a = k * chunk;
-    const uint64_t e = a + chunk < n ? a + chunk : n;
-    uint64_t l = sparse[k];
-    plcp[a] = (uint32_t)l;
-    for (uint64_t x = a + 1; x < e; ++x) {
-        uint64_t b = plcp[x];
-        if (b > n) {
-            atomicOr(err, GSAIS_ERR_BOUNDS);
-            b = n;
-        }
-        if (b == n) {
-            l = 0;
-        } else {
-            l = l ? l - 1 : 0;
-            const uint64_t m = n - (x > b ? x : b);
-            if (l > m) l = m;
-            if (!GSA) {
-                while (l < m && T[x + l] == T[b + l]) ++l;
-            } else {
-                while (l < m && T[x + l] != 0 && T[x + l] == T[b + l]) ++l;
+    constexpr int PER = 16 / sizeof(Sym);
+    __shared__ unsigned long long s_min;
+    const uint32_t count = *long_count;
+    for (uint32_t j = blockIdx.x; j < count; j += gridDim.x) {
+        const uint2 e = long_list[j];
+        const uint64_t a = (uint64_t)e.x * chunk;
+        const uint64_t b = phi[a];   // listed by k_plcp_level only when b < n
+        const uint64_t m = b < n ? n - (a > b ? a : b) : 0;
+        uint64_t l = e.y < m ? e.y : m;
+        while (l < m) {
+            if (threadIdx.x == 0) s_min = ~0ull;
+            __syncthreads();
+            const uint64_t o = l + (uint64_t)threadIdx.x * PER;
+            const uint32_t c = lane_window<Sym, GSA>(tw, a, b, o, m);
+            if (c < (uint32_t)PER) atomicMin(&s_min, (unsigned long long)(o + c));
+            __syncthreads();
+            const unsigned long long r = s_min;
+            __syncthreads();
+            if (r != ~0ull) {
+                l = r < m ? r : m;
+                break;
             }
+            l += 256 * PER;
         }
-        plcp[x] = (uint32_t)l;
+        if (threadIdx.x == 0) sparse[e.x] = (uint32_t)(l < m ? l : m);
+    }
+}
+
+// Kasai's carried length inside each chunk of kPlcpChunk positions, starting
+// from the exact value at the chunk start (src/libsais.c:8167 compute_plcp
+// restarts at block starts too).  A CTA stages the Phi values of 128 chunks
+// in shared memory (coalesced), each thread walks its chunk, and the PLCP
+// values go back over Phi, coalesced.
+constexpr uint32_t kPlcpChunk = 64;
+constexpr int kKasaiThreads = 128;
+constexpr int kKasaiStride = kPlcpChunk + 1;   // padded rows: no bank conflicts
+
+template <typename Sym, bool GSA>
+__global__ void __launch_bounds__(kKasaiThreads) k_plcp_kasai(TextWords tw, uint64_t n, uint64_t nchunks,
+                                                              const uint32_t *__restrict__ sparse,
+                                                              uint32_t *__restrict__ plcp, uint32_t *__restrict__ err)
+{
+    __shared__ uint32_t s[kKasaiThreads * kKasaiStride];
+    const uint64_t tile0 = (uint64_t)blockIdx.x * kKasaiThreads * kPlcpChunk;
+    for (uint32_t e = threadIdx.x; e < kKasaiThreads * kPlcpChunk; e += kKasaiThreads) {
+        const uint64_t x = tile0 + e;
+        if (x < n) s[(e / kPlcpChunk) * kKasaiStride + (e % kPlcpChunk)] = plcp[x];
+    }
+    __syncthreads();
+    const uint64_t k = (uint64_t)blockIdx.x * kKasaiThreads + threadIdx.x;
+    bool bad = false;
+    if (k < nchunks) {
+        uint32_t *row = s + threadIdx.x * kKasaiStride;
+        const uint64_t a = k * kPlcpChunk;
+        const uint64_t e = a + kPlcpChunk < n ? a + kPlcpChunk : n;
+        uint64_t l = sparse[k];
+        row[0] = (uint32_t)l;
+        for (uint64_t x = a + 1; x < e; ++x) {
+            uint64_t b = row[x - a];
+            if (b > n) {
+                bad = true;
+                b = n;
+            }
+            if (b == n) {
+                l = 0;
+            } else {
+                l = l ? l - 1 : 0;
+                const uint64_t m = n - (x > b ? x : b);
+                if (l > m) l = m;
+                l = extend_thread<Sym, GSA>(tw, x, b, l, m);
+            }
+            row[x - a] = (uint32_t)l;
+        }
+    }
+    if (bad) atomicOr(err, GSAIS_ERR_BOUNDS);
+    __syncthreads();
+    for (uint32_t e = threadIdx.x; e < kKasaiThreads * kPlcpChunk; e += kKasaiThreads) {
+        const uint64_t x = tile0 + e;
+        if (x < n) plcp[x] = s[(e / kPlcpChunk) * kKasaiStride + (e % kPlcpChunk)];
     }
 }
 
 // LCP[i] = PLCP[SA[i]] (src/libsais.c:8311 compute_lcp).  Bytes: 12 per row.
+// Eight rows per thread per step: all SA loads, then all eight gathers in
+// flight, then the stores.
 __global__ void __launch_bounds__(256) k_lcp(const uint32_t *__restrict__ plcp, const uint32_t *__restrict__ SA,
                                              uint32_t *__restrict__ lcp, uint64_t n, uint32_t *__restrict__ err)
 {
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const uint64_t s = SA[i];
-        if (s >= n) {
-            atomicOr(err, GSAIS_ERR_BOUNDS);
-            continue;
+    constexpr int B = 8;
+    const uint64_t span = (uint64_t)gridDim.x * blockDim.x * B;
+    bool bad = false;
+    for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x * B + threadIdx.x; i0 < n; i0 += span) {
+        uint32_t s[B], v[B];
+#pragma unroll
+        for (int j = 0; j < B; ++j) {
+            const uint64_t i = i0 + (uint64_t)j * blockDim.x;
+            s[j] = i < n ? SA[i] : 0u;
         }
-        lcp[i] = plcp[s];
+#pragma unroll
+        for (int j = 0; j < B; ++j) {
+            const uint64_t i = i0 + (uint64_t)j * blockDim.x;
+            const bool ok = i < n && s[j] < n;
+            bad |= i < n && !ok;
+            v[j] = ok ? __ldg(plcp + s[j]) : 0u;
+        }
+#pragma unroll
+        for (int j = 0; j < B; ++j) {
+            const uint64_t i = i0 + (uint64_t)j * blockDim.x;
+            if (i < n) lcp[i] = v[j];
+        }
     }
+    if (bad) atomicOr(err, GSAIS_ERR_BOUNDS);
 }
 
-constexpr uint32_t kPlcpChunk = 64;
+// Scratch of plcp_run, in words: chunk-start values, the long list (two words
+// per entry, at most one entry per chunk start of a level), per-level long
+// counts, and the Phi partitions' scratch.
+constexpr int kMaxLevels = 40;
+
+uint64_t plcp_chunks(uint64_t n) { return (n + kPlcpChunk - 1) / kPlcpChunk; }
+
+size_t plcp_scratch_layout(uint64_t n, size_t *o_long, size_t *o_counts, size_t *o_phi)
+{
+    const uint64_t nc = plcp_chunks(n);
+    size_t w = (nc + 2 + 63) / 64 * 64;   // sparse
+    *o_long = w;
+    w += 2 * ((nc / 2 + 2 + 31) / 32 * 32);
+    *o_counts = w;
+    w += 64;
+    *o_phi = w;
+    w += phi_scratch_words(n);
+    return w;
+}
 
 template <typename Sym, bool GSA>
-cudaError_t plcp_run(const Sym *T, const uint32_t *SA, uint64_t n, uint32_t *plcp, uint32_t *sparse, uint32_t *err,
+cudaError_t plcp_run(const Sym *T, const uint32_t *SA, uint64_t n, uint32_t *plcp, uint32_t *scratch, uint32_t *err,
                      cudaStream_t st)
 {
-    GSAIS_COUNTED((k_phi<<<grid_for(n, 256), 256, 0, st>>>(SA, n, plcp, err)));
-    const uint64_t nchunks = (n + kPlcpChunk - 1) / kPlcpChunk;
-    // level 0: chunk 0 from scratch
-    GSAIS_COUNTED((k_plcp_level<Sym, GSA><<<1, 32, 0, st>>>(T, n, plcp, kPlcpChunk, nchunks, 0, sparse, err)));
+    size_t o_long, o_counts, o_phi;
+    plcp_scratch_layout(n, &o_long, &o_counts, &o_phi);
+    uint32_t *sparse = scratch;
+    uint2 *long_list = reinterpret_cast<uint2 *>(scratch + o_long);
+    uint32_t *counts = scratch + o_counts;
+    if (phi_partitioned(n)) {
+        cudaError_t e = phi_permute(SA, n, plcp, scratch + o_phi, err, st);
+        if (e != cudaSuccess) return e;
+    } else {
+        GSAIS_COUNTED((k_phi<<<grid_for(n, 256), 256, 0, st>>>(SA, n, plcp, err)));
+    }
+    TextWords tw;
+    tw.T = reinterpret_cast<const uint8_t *>(T);
+    tw.nbytes = n * sizeof(Sym);
+    tw.mis = (uint32_t)(reinterpret_cast<uintptr_t>(T) & 7);
+    const uint64_t nchunks = plcp_chunks(n);
     uint64_t top = 1;
-    while (top < nchunks) top <<= 1;
-    for (uint64_t half = top >> 1; half >= 1; half >>= 1) {
+    int levels = 0;
+    while (top < nchunks) {
+        top <<= 1;
+        ++levels;
+    }
+    if (levels > kMaxLevels) return cudaErrorInvalidValue;
+    // level 0: chunk 0 from scratch, by the whole grid
+    GSAIS_COUNTED((k_plcp_first_init<<<1, 1, 0, st>>>(plcp, n, sparse, counts, levels, err)));
+    GSAIS_COUNTED((k_plcp_first<Sym, GSA><<<sm_count() * 4, 256, 0, st>>>(tw, n, plcp, sparse)));
+    int level = 0;
+    for (uint64_t half = top >> 1; half >= 1; half >>= 1, ++level) {
         const uint64_t count = nchunks > half ? (nchunks - half + 2 * half - 1) / (2 * half) : 0;
         if (count == 0) continue;
         const uint64_t threads = count * 32;
         const unsigned blocks = (unsigned)((threads + 255) / 256);
-        GSAIS_COUNTED(
-            (k_plcp_level<Sym, GSA><<<blocks, 256, 0, st>>>(T, n, plcp, kPlcpChunk, nchunks, half, sparse, err)));
+        GSAIS_COUNTED((k_plcp_level<Sym, GSA><<<blocks, 256, 0, st>>>(tw, n, plcp, kPlcpChunk, nchunks, half,
+                                                                       sparse, long_list, counts + level, err)));
+        const unsigned lg = (unsigned)(count < (uint64_t)sm_count() * 2 ? count : (uint64_t)sm_count() * 2);
+        GSAIS_COUNTED((k_plcp_long<Sym, GSA><<<lg, 256, 0, st>>>(tw, n, plcp, kPlcpChunk, sparse, long_list,
+                                                                 counts + level)));
     }
-    GSAIS_COUNTED((k_plcp_chunks<Sym, GSA><<<(unsigned)((nchunks + 255) / 256), 256, 0, st>>>(
-        T, n, kPlcpChunk, nchunks, sparse, plcp, err)));
+    GSAIS_COUNTED((k_plcp_kasai<Sym, GSA><<<(unsigned)((nchunks + kKasaiThreads - 1) / kKasaiThreads), kKasaiThreads,
+                                            0, st>>>(tw, n, nchunks, sparse, plcp, err)));
     return cudaGetLastError();
 }
 
@@ -334,6 +664,17 @@ cudaError_t bwt_gather(const void *d_T, int symbytes, const uint32_t *d_SA, cons
                        void *d_U, const PackedText &pk, uint32_t *err, cudaStream_t st)
 {
     if (n == 0) return cudaSuccess;
+    const uintptr_t ua = reinterpret_cast<uintptr_t>(d_U);
+    if (symbytes == 1 && (ua & 3) == 0) {
+        GSAIS_COUNTED((k_bwt_words<uint8_t><<<grid_for((n + 7) / 8, 256), 256, 0, st>>>(
+            static_cast<const uint8_t *>(d_T), d_SA, n, d_isa1, static_cast<uint8_t *>(d_U), pk, err)));
+        return cudaGetLastError();
+    }
+    if (symbytes == 2 && (ua & 7) == 0) {
+        GSAIS_COUNTED((k_bwt_words<uint16_t><<<grid_for((n + 7) / 8, 256), 256, 0, st>>>(
+            static_cast<const uint16_t *>(d_T), d_SA, n, d_isa1, static_cast<uint16_t *>(d_U), pk, err)));
+        return cudaGetLastError();
+    }
     if (symbytes == 1)
         GSAIS_COUNTED((k_bwt<uint8_t><<<grid_for((n + 7) / 8, 256), 256, 0, st>>>(
             static_cast<const uint8_t *>(d_T), d_SA, n, d_isa1, static_cast<uint8_t *>(d_U), pk, err)));
@@ -384,7 +725,11 @@ cudaError_t narrow_i64_to_u32(const int64_t *src, uint32_t *dst, uint64_t n, uin
     return cudaGetLastError();
 }
 
-size_t plcp_sparse_words(uint64_t n) { return (size_t)((n + kPlcpChunk - 1) / kPlcpChunk + 1); }
+size_t plcp_sparse_words(uint64_t n)
+{
+    size_t a, b, c;
+    return plcp_scratch_layout(n, &a, &b, &c);
+}
 
 cudaError_t plcp_build(const void *d_T, int symbytes, const uint32_t *d_SA, uint64_t n, bool gsa, uint32_t *d_PLCP,
                        uint32_t *d_sparse, uint32_t *err, cudaStream_t st)

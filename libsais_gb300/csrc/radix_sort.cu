@@ -75,38 +75,37 @@ __global__ void __launch_bounds__(256) k_bucket_bases(const uint32_t *__restrict
     bases[p * 256 + threadIdx.x] = e;
 }
 
-template <typename K>
-struct PassShape;
-template <>
-struct PassShape<uint64_t> {
-    static constexpr int kThreads = 256, kItems = 16, kMinBlocks = 3;
-};
-template <>
-struct PassShape<uint32_t> {
-    static constexpr int kThreads = 256, kItems = 24, kMinBlocks = 3;
+// Tile shape of a digit pass: 256 threads (one per digit in the scans) x
+// ITEMS keys.  The items per thread are a tuning parameter (RadixScratch);
+// the instances compiled here are the candidates the autotuner searches.
+template <typename K, int ITEMS>
+struct PassShape {
+    static constexpr int kThreads = 256, kItems = ITEMS;
+    // registers: keys, values and ranks of ITEMS items stay in registers
+    static constexpr int kMinBlocks = (ITEMS * (sizeof(K) / 4 + 1) <= 48) ? 3 : 2;
 };
 
-template <typename K>
+template <typename K, int ITEMS>
 __host__ __device__ constexpr int pass_tile()
 {
-    return PassShape<K>::kThreads * PassShape<K>::kItems;
+    return PassShape<K, ITEMS>::kThreads * ITEMS;
 }
 
 // staged keys + values of one tile; values are re-ordered in place (they are
 // held in registers while the tile is ranked)
-template <typename K>
+template <typename K, int ITEMS>
 __host__ __device__ constexpr size_t pass_smem()
 {
-    return (size_t)pass_tile<K>() * (sizeof(K) + sizeof(uint32_t));
+    return (size_t)pass_tile<K, ITEMS>() * (sizeof(K) + sizeof(uint32_t));
 }
 
 // Per-tile digit counts of one pass, digit-major: counts[d * tiles + t].
 // Bytes per key: sizeof(K) read.
-template <typename K>
+template <typename K, int ITEMS>
 __global__ void __launch_bounds__(256) k_tile_counts(const K *__restrict__ keys, uint64_t n, int shift, uint32_t mask,
                                                      uint32_t *__restrict__ counts, uint32_t tiles)
 {
-    constexpr int TILE = pass_tile<K>();
+    constexpr int TILE = pass_tile<K, ITEMS>();
     constexpr int PER_VEC = 16 / sizeof(K);
     static_assert(TILE % (256 * PER_VEC) == 0, "tile is a whole number of 16-byte vectors per thread");
     __shared__ uint32_t h[8][256];
@@ -167,14 +166,15 @@ __global__ void __launch_bounds__(1024) k_tile_offsets(const uint32_t *__restric
 
 // Digit pass of one tile (tile = blockIdx.x): stage, rank stably, re-order by
 // digit in shared memory, write each digit run to its global offset.
-template <typename K>
-__global__ void __launch_bounds__(PassShape<K>::kThreads, PassShape<K>::kMinBlocks)
+// vin == nullptr: the values are implicit, value(i) = n - 1 - i (the suffix
+// indexes of seed keys written in reverse text order), so only keys are read.
+template <typename K, int ITEMS>
+__global__ void __launch_bounds__(PassShape<K, ITEMS>::kThreads, PassShape<K, ITEMS>::kMinBlocks)
     k_radix_pass(const K *__restrict__ kin, const uint32_t *__restrict__ vin, K *__restrict__ kout,
                  uint32_t *__restrict__ vout, uint64_t n, int shift, uint32_t mask,
                  const uint32_t *__restrict__ offs, uint32_t tiles, uint32_t *err)
 {
-    constexpr int THREADS = PassShape<K>::kThreads;
-    constexpr int ITEMS = PassShape<K>::kItems;
+    constexpr int THREADS = PassShape<K, ITEMS>::kThreads;
     static_assert(THREADS == 256, "one thread per digit");
     constexpr int TILE = THREADS * ITEMS;
     constexpr int WARPS = THREADS / 32;
@@ -194,12 +194,13 @@ __global__ void __launch_bounds__(PassShape<K>::kThreads, PassShape<K>::kMinBloc
     const uint32_t valid = (uint32_t)((n - base) < (uint64_t)TILE ? (n - base) : (uint64_t)TILE);
     const bool full = valid == TILE;
     const uint64_t stall_ns = full ? g_test_stall_wait_ns : 0;
+    const bool implicit = vin == nullptr;
     if (tid == 0 && full) {
         mbar_init(&s_bar, 1);
         if (stall_ns) mbar_init(&s_never, 1);
-        mbar_arrive_expect_tx(&s_bar, TILE * (uint32_t)(sizeof(K) + sizeof(uint32_t)));
+        mbar_arrive_expect_tx(&s_bar, TILE * (uint32_t)(sizeof(K) + (implicit ? 0 : sizeof(uint32_t))));
         bulk_copy_g2s(s_keys, kin + base, TILE * sizeof(K), &s_bar);
-        bulk_copy_g2s(s_vals, vin + base, TILE * sizeof(uint32_t), &s_bar);
+        if (!implicit) bulk_copy_g2s(s_vals, vin + base, TILE * sizeof(uint32_t), &s_bar);
     }
     for (int i = tid; i < WARPS * 256; i += THREADS) (&s_whist[0][0])[i] = 0;
     const uint32_t gofs = offs[(uint64_t)tid * tiles + tile];
@@ -220,10 +221,11 @@ __global__ void __launch_bounds__(PassShape<K>::kThreads, PassShape<K>::kMinBloc
     if (!full || !staged) {
         for (uint32_t i = tid; i < valid; i += THREADS) {
             s_keys[i] = kin[base + i];
-            s_vals[i] = vin[base + i];
+            if (!implicit) s_vals[i] = vin[base + i];
         }
         __syncthreads();
     }
+    const uint32_t vbase = (uint32_t)(n - 1 - base);   // implicit value of entry base + i: vbase - i
 
     // ---- rank inside each warp, in input order (stable).  Lanes with equal
     // digits are found with eight ballots; the lowest such lane advances the
@@ -238,7 +240,7 @@ __global__ void __launch_bounds__(PassShape<K>::kThreads, PassShape<K>::kMinBloc
             const int idx = wbase + k * 32 + lane;
             const K key = s_keys[idx];
             kr[k] = key;
-            vr[k] = s_vals[idx];
+            vr[k] = implicit ? vbase - (uint32_t)idx : s_vals[idx];
             const uint32_t d = (uint32_t)(key >> shift) & mask;
             uint32_t peers = GSAIS_FULL_MASK;
 #pragma unroll
@@ -260,7 +262,7 @@ __global__ void __launch_bounds__(PassShape<K>::kThreads, PassShape<K>::kMinBloc
             const bool ok = (uint32_t)idx < valid;
             const K key = ok ? s_keys[idx] : K(0);
             kr[k] = key;
-            vr[k] = ok ? s_vals[idx] : 0u;
+            vr[k] = ok ? (implicit ? vbase - (uint32_t)idx : s_vals[idx]) : 0u;
             const uint32_t d = ok ? ((uint32_t)(key >> shift) & mask) : 256u;
             const uint32_t peers = __match_any_sync(GSAIS_FULL_MASK, d);
             const uint32_t before = __popc(peers & lanemask_lt());
@@ -320,6 +322,15 @@ __global__ void __launch_bounds__(PassShape<K>::kThreads, PassShape<K>::kMinBloc
     if (bad) atomicOr(err, GSAIS_ERR_BOUNDS);
 }
 
+// vals[i] = n - 1 - i: the implicit values, materialised when no digit pass
+// ran (every key alike).
+__global__ void __launch_bounds__(256) k_fill_implicit(uint32_t *__restrict__ vals, uint64_t n)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        vals[i] = (uint32_t)(n - 1 - i);
+}
+
 __global__ void __launch_bounds__(256) k_read_back(uint32_t *__restrict__ dst, const uint32_t *__restrict__ src,
                                                    uint32_t words)
 {
@@ -334,7 +345,7 @@ int sm_count()
     return sms > 0 ? sms : 1;
 }
 
-template <typename K>
+template <typename K, int ITEMS>
 cudaError_t pass_attr()
 {
     // cudaFuncSetAttribute applies to the current device; remember per device
@@ -342,19 +353,81 @@ cudaError_t pass_attr()
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev >= 0 && dev < 64 && done[dev]) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(k_radix_pass<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)pass_smem<K>());
+    cudaError_t e = cudaFuncSetAttribute(k_radix_pass<K, ITEMS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)pass_smem<K, ITEMS>());
     if (e == cudaSuccess && dev >= 0 && dev < 64) done[dev] = true;
     return e;
 }
 
+// One digit pass (tile counts, tile offsets, scatter) with ITEMS keys per thread.
+template <typename K, int ITEMS>
+cudaError_t run_pass(K *kin, const uint32_t *vin, K *kout, uint32_t *vout, uint64_t n, int shift, uint32_t mask,
+                     const uint32_t *bases, uint32_t *counts, uint64_t status_words, RadixScratch &rs,
+                     uint32_t *d_err, cudaStream_t st, bool implicit)
+{
+    constexpr int TILE = pass_tile<K, ITEMS>();
+    const uint64_t tiles = (n + TILE - 1) / TILE;
+    if (tiles * 256 * 2 > status_words * 2) return cudaErrorInvalidValue;   // counts + offsets
+    cudaError_t e;
+    if ((e = pass_attr<K, ITEMS>()) != cudaSuccess) return e;
+    uint32_t *offs = counts + tiles * 256;
+    cudaEvent_t ev0 = rs.prof ? rs.prof->begin(st) : nullptr;
+    GSAIS_COUNTED((k_tile_counts<K, ITEMS><<<(unsigned)tiles, 256, 0, st>>>(kin, n, shift, mask, counts,
+                                                                             (uint32_t)tiles)));
+    GSAIS_COUNTED((k_tile_offsets<<<256, 1024, 0, st>>>(counts, (uint32_t)tiles, bases, offs)));
+    if (ev0) rs.prof->end(KK_TILE_COUNTS, ev0, st, n * sizeof(K));
+    cudaEvent_t ev1 = rs.prof ? rs.prof->begin(st) : nullptr;
+    GSAIS_COUNTED((k_radix_pass<K, ITEMS><<<(unsigned)tiles, 256, pass_smem<K, ITEMS>(), st>>>(
+        kin, implicit ? nullptr : vin, kout, vout, n, shift, mask, offs, (uint32_t)tiles, d_err)));
+    // algorithmic bytes: every (key, value) pair read once and written once
+    // (an implicit value is only written)
+    if (ev1) rs.prof->end(KK_RADIX_PASS, ev1, st, n * (2 * sizeof(K) + (implicit ? 1 : 2) * sizeof(uint32_t)));
+    return cudaGetLastError();
+}
+
+// Items per thread of the compiled pass instances, per key width.
+bool items_supported(int key_bytes, int items)
+{
+    if (key_bytes == 4) return items == 16 || items == 20 || items == 24 || items == 28;
+    return items == 12 || items == 16 || items == 20;
+}
+
+template <typename K>
+cudaError_t run_pass_items(int items, K *kin, const uint32_t *vin, K *kout, uint32_t *vout, uint64_t n, int shift,
+                           uint32_t mask, const uint32_t *bases, uint32_t *counts, uint64_t status_words,
+                           RadixScratch &rs, uint32_t *d_err, cudaStream_t st, bool implicit)
+{
+#define GSAIS_PASS(I) \
+    return run_pass<K, I>(kin, vin, kout, vout, n, shift, mask, bases, counts, status_words, rs, d_err, st, implicit)
+    if constexpr (sizeof(K) == 4) {
+        switch (items) {
+        case 16: GSAIS_PASS(16);
+        case 20: GSAIS_PASS(20);
+        case 28: GSAIS_PASS(28);
+        default: GSAIS_PASS(24);
+        }
+    } else {
+        switch (items) {
+        case 12: GSAIS_PASS(12);
+        case 20: GSAIS_PASS(20);
+        default: GSAIS_PASS(16);
+        }
+    }
+#undef GSAIS_PASS
+}
+
 template <typename K>
 cudaError_t sort_impl(K *keys[2], uint32_t *vals[2], uint64_t n, int begin_bit, int end_bit, RadixScratch &rs,
-                      uint32_t *d_err, cudaStream_t st, int *which, int *passes_run, bool hist_ready)
+                      uint32_t *d_err, cudaStream_t st, int *which, int *passes_run, bool hist_ready,
+                      bool implicit_vals = false)
 {
     *which = 0;
     if (passes_run) *passes_run = 0;
-    if (n <= 1 || end_bit <= begin_bit) return cudaSuccess;
+    if (n <= 1 || end_bit <= begin_bit) {
+        if (implicit_vals && n)
+            GSAIS_COUNTED((k_fill_implicit<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(vals[0], n)));
+        return cudaGetLastError();
+    }
     const int passes = (end_bit - begin_bit + 7) / 8;
     cudaError_t e;
     if (!hist_ready) {
@@ -369,13 +442,9 @@ cudaError_t sort_impl(K *keys[2], uint32_t *vals[2], uint64_t n, int begin_bit, 
     GSAIS_COUNTED((k_bucket_bases<<<passes, 256, 0, st>>>(rs.hist, rs.bases)));
     if ((e = read_back(rs.h_hist, rs.hist, (size_t)passes * 256 * sizeof(uint32_t), st)) != cudaSuccess) return e;
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
-    if ((e = pass_attr<K>()) != cudaSuccess) return e;
 
-    constexpr int TILE = pass_tile<K>();
-    const uint64_t tiles = (n + TILE - 1) / TILE;
-    if (tiles * 256 * 2 > (uint64_t)rs.status_words * 2) return cudaErrorInvalidValue;   // counts + offsets
+    const int items = sizeof(K) == 4 ? rs.items32 : rs.items64;
     uint32_t *counts = reinterpret_cast<uint32_t *>(rs.status);
-    uint32_t *offs = counts + tiles * 256;
     int cur = 0, ran = 0;
     for (int p = 0; p < passes; ++p) {
         bool trivial = false;
@@ -385,19 +454,15 @@ cudaError_t sort_impl(K *keys[2], uint32_t *vals[2], uint64_t n, int begin_bit, 
         const int shift = begin_bit + 8 * p;
         const int bits = end_bit - shift < 8 ? end_bit - shift : 8;
         const uint32_t mask = (1u << bits) - 1u;
-        cudaEvent_t ev0 = rs.prof ? rs.prof->begin(st) : nullptr;
-        GSAIS_COUNTED((k_tile_counts<K><<<(unsigned)tiles, 256, 0, st>>>(keys[cur], n, shift, mask, counts,
-                                                                          (uint32_t)tiles)));
-        GSAIS_COUNTED((k_tile_offsets<<<256, 1024, 0, st>>>(counts, (uint32_t)tiles, rs.bases + p * 256, offs)));
-        if (ev0) rs.prof->end(KK_TILE_COUNTS, ev0, st, n * sizeof(K));
-        cudaEvent_t ev1 = rs.prof ? rs.prof->begin(st) : nullptr;
-        GSAIS_COUNTED((k_radix_pass<K><<<(unsigned)tiles, PassShape<K>::kThreads, pass_smem<K>(), st>>>(
-            keys[cur], vals[cur], keys[cur ^ 1], vals[cur ^ 1], n, shift, mask, offs, (uint32_t)tiles, d_err)));
-        // algorithmic bytes: every (key, value) pair read once and written once
-        if (ev1) rs.prof->end(KK_RADIX_PASS, ev1, st, 2 * n * (sizeof(K) + sizeof(uint32_t)));
+        if ((e = run_pass_items<K>(items, keys[cur], vals[cur], keys[cur ^ 1], vals[cur ^ 1], n, shift, mask,
+                                   rs.bases + p * 256, counts, rs.status_words, rs, d_err, st,
+                                   implicit_vals && ran == 0)) != cudaSuccess)
+            return e;
         cur ^= 1;
         ++ran;
     }
+    if (implicit_vals && ran == 0)
+        GSAIS_COUNTED((k_fill_implicit<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(vals[0], n)));
     *which = cur;
     if (passes_run) *passes_run = ran;
     return cudaGetLastError();
@@ -428,12 +493,13 @@ cudaError_t read_back(void *h_dst, const void *d_src, size_t bytes, cudaStream_t
 size_t radix_status_words(uint64_t n)
 {
     // per (tile, digit): one 32-bit count and one 32-bit offset; sized for the
-    // smallest pass tile of either key width
-    constexpr uint64_t TILE = (uint64_t)(pass_tile<uint64_t>() < pass_tile<uint32_t>() ? pass_tile<uint64_t>()
-                                                                                     : pass_tile<uint32_t>());
+    // smallest pass tile of either key width (64-bit keys, 12 items)
+    constexpr uint64_t TILE = (uint64_t)pass_tile<uint64_t, 12>();
     const uint64_t tiles = (n + TILE - 1) / TILE;
     return (size_t)(tiles ? tiles : 1) * 256;
 }
+
+bool radix_items_supported(int key_bytes, int items) { return items_supported(key_bytes, items); }
 
 cudaError_t radix_sort_pairs(uint64_t *keys[2], uint32_t *vals[2], uint64_t n, int end_bit, RadixScratch &rs,
                              uint32_t *d_err, cudaStream_t st, int *which, int *passes_run, bool hist_ready)
@@ -442,9 +508,11 @@ cudaError_t radix_sort_pairs(uint64_t *keys[2], uint32_t *vals[2], uint64_t n, i
 }
 
 cudaError_t radix_sort_pairs32(uint32_t *keys[2], uint32_t *vals[2], uint64_t n, int end_bit, RadixScratch &rs,
-                               uint32_t *d_err, cudaStream_t st, int *which, int *passes_run, bool hist_ready)
+                               uint32_t *d_err, cudaStream_t st, int *which, int *passes_run, bool hist_ready,
+                               bool implicit_vals)
 {
-    return sort_impl<uint32_t>(keys, vals, n, 0, end_bit, rs, d_err, st, which, passes_run, hist_ready);
+    return sort_impl<uint32_t>(keys, vals, n, 0, end_bit, rs, d_err, st, which, passes_run, hist_ready,
+                               implicit_vals);
 }
 
 cudaError_t radix_partition32(uint32_t *keys[2], uint32_t *vals[2], uint64_t n, int begin_bit, int end_bit,

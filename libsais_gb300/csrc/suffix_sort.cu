@@ -98,7 +98,9 @@ __global__ void __launch_bounds__(256) k_hist_u16(const uint16_t *__restrict__ T
 // position x (the K = 32 / B codes from x) is one funnel shift of two words.
 // Also writes the packed text (least-significant-first, the layout the BWT
 // gather and the pair comparison read) and digit 0's histogram.
-// Bytes per suffix: T s read, key 4 + value 4 written (+ B/8 packed).
+// The suffix index is not written: key slot j holds suffix n - 1 - j, which
+// the first radix pass computes instead of reading a value array.
+// Bytes per suffix: T s read, key 4 written (+ B/8 packed).
 template <typename Sym, int B>
 __global__ void __launch_bounds__(256) k_seed_packed(const Sym *__restrict__ T, uint64_t n,
                                                      const uint16_t *__restrict__ codes, uint32_t *__restrict__ keys,
@@ -155,11 +157,8 @@ __global__ void __launch_bounds__(256) k_seed_packed(const Sym *__restrict__ T, 
             const uint32_t key = __funnelshift_l(w[i + 1], w[i], s);
             const uint64_t p = base + (uint64_t)x;
             const bool ok = p < n;
-            if (ok) {
-                const uint64_t j = n - 1 - p;   // reverse text order: shorter suffixes first
-                keys[j] = key;
-                vals[j] = (uint32_t)p;
-            }
+            if (ok) keys[n - 1 - p] = key;   // reverse text order: shorter suffixes first; the
+                                             // value (suffix index p) is implicit in the slot
             radix_hist_add(sh, (uint64_t)key, ok, 1, end_bit);
         }
     }
@@ -614,23 +613,26 @@ constexpr uint32_t kMedium = 0xFFFFFFFEu;
 // CTA path; large groups get an id and a slot range in the large list from
 // one combined counter, so ids and ranges are in the same order.
 // Bytes per group: 8 read, 4-8 written.
+// medium_small <= kMediumSmall and medium_max <= kMediumMax are the tuned
+// cut-overs (the capacities of the two CTA tiers are the compiled maxima).
 __global__ void __launch_bounds__(256) k_classify(const uint32_t *__restrict__ gstart, uint64_t G, uint64_t N,
                                                   uint32_t *__restrict__ lid, uint32_t *__restrict__ loff,
                                                   unsigned long long *__restrict__ lcount,
                                                   uint32_t *__restrict__ mlist, unsigned long long *__restrict__ mcount,
                                                   uint32_t *__restrict__ mlist2,
-                                                  unsigned long long *__restrict__ mcount2)
+                                                  unsigned long long *__restrict__ mcount2, uint32_t medium_small,
+                                                  uint32_t medium_max)
 {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < G; g += stride) {
         const uint64_t s = gstart[g];
         const uint64_t e = g + 1 < G ? gstart[g + 1] : N;
         const uint64_t size = e - s;
-        if (size > kMediumMax) {
+        if (size > medium_max) {
             const unsigned long long old = atomicAdd(lcount, (1ull << 32) | size);
             lid[g] = (uint32_t)(old >> 32);
             loff[g] = (uint32_t)old;
-        } else if (size > kMediumSmall) {
+        } else if (size > medium_small) {
             lid[g] = kMedium;
             mlist2[atomicAdd(mcount2, 1ull)] = (uint32_t)g;
         } else if (size > kSmallMax) {
@@ -1448,12 +1450,14 @@ __global__ void k_perm_cursors(uint32_t *__restrict__ cursor, uint32_t count, in
 // [lbase, lbase + RANGE) where lbase = (p0 >> lshift) << (lshift - shift) for
 // the tile's first position p0 (lshift = 0: lbase = 0).  Entries land at
 // cursor[digit]++ (order inside a digit is not kept: the scatter after the
-// last level does not need it).
-template <int RANGE>
+// last level does not need it).  PHI: the value of entry j is not read from
+// in_r but is in_pos[j - 1] (N for j = 0), the Phi array of a suffix array
+// (libsais src/libsais.c:8116 compute_phi: Phi[SA[j]] = SA[j-1]).
+template <int RANGE, bool PHI = false>
 __global__ void __launch_bounds__(kPermThreads) k_perm_partition(const uint32_t *__restrict__ in_pos,
                                                                  const uint32_t *__restrict__ in_r, uint64_t N,
                                                                  int shift, int lshift,
-                                                                 uint32_t *__restrict__ cursor,
+                                                                 uint32_t *__restrict__ cursor, uint32_t ncursor,
                                                                  uint32_t *__restrict__ out_pos,
                                                                  uint32_t *__restrict__ out_r,
                                                                  uint32_t *__restrict__ err)
@@ -1478,13 +1482,16 @@ __global__ void __launch_bounds__(kPermThreads) k_perm_partition(const uint32_t 
     for (int k = 0; k < kPermItems; ++k) {
         const uint32_t i = k * THREADS + tid;
         p[k] = i < valid ? in_pos[t0 + i] : 0xFFFFFFFFu;
-        r[k] = i < valid ? in_r[t0 + i] : 0u;
+        if (PHI)
+            r[k] = i < valid ? (t0 + i ? in_pos[t0 + i - 1] : (uint32_t)N) : 0u;
+        else
+            r[k] = i < valid ? in_r[t0 + i] : 0u;
     }
 #pragma unroll
     for (int k = 0; k < kPermItems; ++k) {
         if (p[k] != 0xFFFFFFFFu) {
             const uint32_t ld = (p[k] >> shift) - lbase;
-            if (ld < RANGE) {
+            if (ld < RANGE && (uint64_t)lbase + ld < ncursor) {
                 slot[k] = (uint16_t)atomicAdd(&s_cnt[ld], 1u);
             } else {
                 bad = true;
@@ -1506,7 +1513,7 @@ __global__ void __launch_bounds__(kPermThreads) k_perm_partition(const uint32_t 
 #pragma unroll
     for (int q = 0; q < PER; ++q) {
         const uint32_t ld = tid * PER + q;
-        if (ld < RANGE) {
+        if (ld < RANGE) {   // c[q] > 0 only for digits whose cursor exists
             s_lstart[ld] = a;
             s_g[ld] = c[q] ? atomicAdd(&cursor[lbase + ld], c[q]) : 0u;
         }
@@ -1555,6 +1562,26 @@ __global__ void __launch_bounds__(256) k_perm_window(const uint32_t *__restrict_
     }
     __syncthreads();
     for (uint32_t i = threadIdx.x; i < W; i += 256) rank[w0 + i] = s_win[i];
+    if (bad) atomicOr(err, GSAIS_ERR_BOUNDS);
+}
+
+// Window pass of the Phi permutation: like k_perm_window, but `out` may be
+// the same buffer as `r` (each CTA reads its whole window before writing it).
+__global__ void __launch_bounds__(256) k_phi_window(const uint32_t *__restrict__ pos, const uint32_t *r, uint64_t N,
+                                                    int shift, uint32_t *out, uint32_t *__restrict__ err)
+{
+    extern __shared__ uint32_t s_win[];
+    const uint64_t w0 = (uint64_t)blockIdx.x << shift;
+    const uint32_t W = (uint32_t)(N - w0 < (1ull << shift) ? N - w0 : (1ull << shift));
+    bool bad = false;
+    for (uint32_t i = threadIdx.x; i < W; i += 256) {
+        const uint32_t q = pos[w0 + i];
+        const uint64_t x = (uint64_t)q - w0;
+        if (q >= w0 && x < W) s_win[x] = r[w0 + i];
+        else bad = true;
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < W; i += 256) out[w0 + i] = s_win[i];
     if (bad) atomicOr(err, GSAIS_ERR_BOUNDS);
 }
 
@@ -1775,9 +1802,9 @@ static cudaError_t scatter_seed_ranks(SortWorkspace &ws, uint32_t *sorted_pos, u
             if (dev >= 0 && dev < 64) attr_done[dev] = true;
         }
         GSAIS_COUNTED((k_perm_partition<256><<<(unsigned)tiles, kPermThreads, kPermSmem, st>>>(
-            sorted_pos, ranks, N, shift1, 0, cur, ws.lvals[0], ws.lvals[1], d_err)));
+            sorted_pos, ranks, N, shift1, 0, cur, n1, ws.lvals[0], ws.lvals[1], d_err)));
         GSAIS_COUNTED((k_perm_partition<512><<<(unsigned)tiles, kPermThreads, kPermSmem, st>>>(
-            ws.lvals[0], ws.lvals[1], N, shift2, shift1, cur + n1, sorted_pos, ranks, d_err)));
+            ws.lvals[0], ws.lvals[1], N, shift2, shift1, cur + n1, n2, sorted_pos, ranks, d_err)));
         const size_t smem = (size_t)4 << shift2;
         if (smem > 48 * 1024 &&
             (e = cudaFuncSetAttribute(k_perm_window, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
@@ -1794,6 +1821,65 @@ static cudaError_t scatter_seed_ranks(SortWorkspace &ws, uint32_t *sorted_pos, u
     if (e != cudaSuccess) return e;
     GSAIS_COUNTED((k_scatter_ranks<<<stream_grid(N, 256), 256, 0, st>>>(kk[which], vv[which], N, nr, ws.rank,
                                                                         d_err)));
+    return cudaGetLastError();
+}
+
+// Phi[SA[j]] = SA[j-1] (Phi[SA[0]] = N) for a suffix array SA of N entries,
+// by two position partitions and a shared-memory window pass, so that no
+// random write reaches DRAM.  Scratch: phi_scratch_words(N) words.
+bool phi_partitioned(uint64_t N)
+{
+    if (N < (1ull << 23)) return false;
+    const int b = gsais_bits_for(N - 1);
+    return b - 16 <= 15;
+}
+
+// Cursor words: 256 for the first level, and for the second level every
+// index a tile can name (digits below 256 << 8 plus a 512-digit range), so
+// that even entries of a malformed SA stay inside the scratch.
+constexpr size_t kPhiCursorWords = 256 + (256 << 8) + 512;
+
+size_t phi_scratch_words(uint64_t N)
+{
+    if (!phi_partitioned(N)) return 0;
+    return (size_t)3 * ((N + 63) / 64 * 64) + kPhiCursorWords;
+}
+
+cudaError_t phi_permute(const uint32_t *SA, uint64_t N, uint32_t *phi, uint32_t *scratch, uint32_t *d_err,
+                        cudaStream_t st)
+{
+    cudaError_t e;
+    const int b = gsais_bits_for(N - 1);
+    const int shift1 = b - 8, shift2 = b - 16;
+    const uint64_t Np = (N + 63) / 64 * 64;
+    uint32_t *X = scratch, *Y = scratch + Np, *Z = scratch + 2 * Np, *cur = scratch + 3 * Np;
+    const uint64_t tiles = (N + kPermTile - 1) / kPermTile;
+    const uint32_t n2 = (uint32_t)(((N - 1) >> shift2) + 1);
+    // level-1 cursors at cur[0, 256), level-2 cursors from cur + 256
+    GSAIS_COUNTED((k_perm_cursors<<<1, 256, 0, st>>>(cur, 256, shift1, N)));
+    GSAIS_COUNTED((k_perm_cursors<<<(unsigned)((kPhiCursorWords - 256 + 255) / 256), 256, 0, st>>>(
+        cur + 256, (uint32_t)(kPhiCursorWords - 256), shift2, N)));
+    static bool attr_done[64] = {false};   // dynamic shared memory above 48 KB, per device
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64 || !attr_done[dev]) {
+        if ((e = cudaFuncSetAttribute(k_perm_partition<256, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)kPermSmem)) != cudaSuccess ||
+            (e = cudaFuncSetAttribute(k_perm_partition<512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)kPermSmem)) != cudaSuccess)
+            return e;
+        if (dev >= 0 && dev < 64) attr_done[dev] = true;
+    }
+    GSAIS_COUNTED((k_perm_partition<256, true><<<(unsigned)tiles, kPermThreads, kPermSmem, st>>>(
+        SA, nullptr, N, shift1, 0, cur, 256u, X, Y, d_err)));
+    GSAIS_COUNTED((k_perm_partition<512><<<(unsigned)tiles, kPermThreads, kPermSmem, st>>>(
+        X, Y, N, shift2, shift1, cur + 256, (uint32_t)(kPhiCursorWords - 256), Z, phi, d_err)));
+    const size_t smem = (size_t)4 << shift2;
+    if (smem > 48 * 1024 &&
+        (e = cudaFuncSetAttribute(k_phi_window, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+            cudaSuccess)
+        return e;
+    GSAIS_COUNTED((k_phi_window<<<n2, 256, smem, st>>>(Z, phi, N, shift2, phi, d_err)));
     return cudaGetLastError();
 }
 
@@ -1834,8 +1920,10 @@ static cudaError_t run_pair_compare(SortWorkspace &ws, const PairSource &ps, con
 }
 
 static cudaError_t run_rounds(SortWorkspace &ws, uint64_t nr, int K, uint32_t kept, uint32_t groups, int av, int pg,
-                              uint32_t *d_err, cudaStream_t st, SortStats &S, const PairSource &ps)
+                              uint32_t *d_err, cudaStream_t st, SortStats &S, const PairSource &ps, const Tuning &tn)
 {
+    const uint32_t medium_small = (uint32_t)(tn.medium_small < (int)kMediumSmall ? tn.medium_small : kMediumSmall);
+    const uint32_t medium_max = (uint32_t)(tn.medium_max < (int)kMediumMax ? tn.medium_max : kMediumMax);
     cudaError_t e;
     int ran = 0;
     const int b2 = gsais_bits_for(nr);
@@ -1864,7 +1952,7 @@ static cudaError_t run_rounds(SortWorkspace &ws, uint64_t nr, int K, uint32_t ke
         uint32_t *mlist2 = ws.lvals[1] + N / 2;   // medium groups have > 32 members: N / 33 of each at most
         GSAIS_COUNTED((k_classify<<<stream_grid(G, 256), 256, 0, st>>>(ws.gstart[pg], G, N, ws.lid, ws.loff,
                                                                       ws.counters + 1, mlist, ws.counters + 2, mlist2,
-                                                                      ws.counters + 5)));
+                                                                      ws.counters + 5, medium_small, medium_max)));
         cudaEvent_t ev_rk = ws.radix.prof ? ws.radix.prof->begin(st) : nullptr;
         GSAIS_COUNTED((k_round_r2<<<stream_grid(N, 256), 256, 0, st>>>(
             act_i, act_pos, act_gid, ws.gstart[pg], ws.lid, ws.loff, ws.rank, h, N, nr, b2, r2, ws.keys[0],
@@ -1991,6 +2079,10 @@ cudaError_t suffix_sort(const void *d_T, int symbytes, uint64_t n, bool gsa, Sor
         }
         bits = gsais_bits_for(sigma > 1 ? sigma - 1 : 1);
     }
+    const Tuning tn = opt.tuning_set ? opt.tuning : tuning_lookup(n, bits);
+    ws.radix.items32 = tn.radix_items32;
+    ws.radix.items64 = tn.radix_items64;
+    S.tuning = tn;
     int K = (opt.seed_key_bits <= 32 ? 32 : 64) / bits;
     if (K < 2 && bits <= 32) K = 64 / bits;   // wide symbols: at least two per key
     if (K < 1) K = 1;
@@ -2064,7 +2156,9 @@ cudaError_t suffix_sort(const void *d_T, int symbytes, uint64_t n, bool gsa, Sor
                 T16, n, ws.codes, bits, K, gsa ? 1 : 0, ws.keys[0], ws.vals[0], hist_passes, seed_end, ws.radix.hist,
                 ws.pack_bits, ws.packed)));
     }
-    if (ev_seed) ws.radix.prof->end(KK_SEED, ev_seed, st, n * (symbytes + (narrow ? 8 : 12)));
+    if (ev_seed)
+        ws.radix.prof->end(KK_SEED, ev_seed, st,
+                           fast_seed ? n * (symbytes + 4) + n * bits / 8 : n * (symbytes + (narrow ? 8 : 12)));
     if (grams) {
         uint32_t *h_hist0 = ws.radix.h_hist;
         uint8_t *h_edge = reinterpret_cast<uint8_t *>(ws.h_small + 16 + 65536 + 32768);
@@ -2084,7 +2178,8 @@ cudaError_t suffix_sort(const void *d_T, int symbytes, uint64_t n, bool gsa, Sor
     {
         uint32_t *vv[2] = {ws.vals[0], ws.vals[1]};
         if (narrow) {
-            if ((e = radix_sort_pairs32(k32, vv, n, seed_end, ws.radix, d_err, st, &w, &ran, true)) != cudaSuccess)
+            if ((e = radix_sort_pairs32(k32, vv, n, seed_end, ws.radix, d_err, st, &w, &ran, true, fast_seed)) !=
+                cudaSuccess)
                 return e;
         } else {
             uint64_t *kk[2] = {ws.keys[0], ws.keys[1]};
@@ -2182,7 +2277,7 @@ cudaError_t suffix_sort(const void *d_T, int symbytes, uint64_t n, bool gsa, Sor
     if (a.rank_out && (e = scatter_seed_ranks(ws, ws.vals[w], a.rank_out, n, n, d_err, st)) != cudaSuccess) return e;
 
     // ---- doubling rounds over the active suffixes
-    if ((e = run_rounds(ws, n, K, kept, groups, av, pg, d_err, st, S, ps)) != cudaSuccess) return e;
+    if ((e = run_rounds(ws, n, K, kept, groups, av, pg, d_err, st, S, ps, tn)) != cudaSuccess) return e;
     uint32_t herr = 0;
     if ((e = read_back(ws.h_small, d_err, 4, st)) != cudaSuccess) return e;
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
@@ -2252,7 +2347,8 @@ namespace gsais {
 size_t batch_workspace_bytes(uint64_t n, uint32_t count) { return sort_workspace_bytes(n + count, 1); }
 
 cudaError_t batch_suffix_sort(const uint8_t *d_T, uint64_t n, const uint64_t *d_offs, uint32_t count,
-                              SortWorkspace &ws, uint32_t *d_err, cudaStream_t st, SortStats *stats)
+                              SortWorkspace &ws, uint32_t *d_err, cudaStream_t st, SortStats *stats,
+                              const Tuning *tuning)
 {
     cudaError_t e;
     SortStats local;
@@ -2270,6 +2366,10 @@ cudaError_t batch_suffix_sort(const uint8_t *d_T, uint64_t n, const uint64_t *d_
         h_codes[c] = h_hist[c] ? (uint16_t)sigma : (uint16_t)0;   // codes 1..sigma; 0 = end of string
     }
     const int bits = gsais_bits_for(sigma);
+    const Tuning tn = tuning ? *tuning : tuning_lookup(n, bits);
+    ws.radix.items32 = tn.radix_items32;
+    ws.radix.items64 = tn.radix_items64;
+    S.tuning = tn;
     const int sid_bits = gsais_bits_for(count > 1 ? count - 1 : 0);
     int K = (64 - sid_bits) / bits;
     if (K < 1) K = 1;
@@ -2316,7 +2416,7 @@ cudaError_t batch_suffix_sort(const uint8_t *d_T, uint64_t n, const uint64_t *d_
         return e;
     if (a.rank_out && (e = scatter_seed_ranks(ws, ws.vals[w], a.rank_out, n, nr, d_err, st)) != cudaSuccess)
         return e;
-    if ((e = run_rounds(ws, nr, K, kept, groups, av, pg, d_err, st, S, PairSource())) != cudaSuccess) return e;
+    if ((e = run_rounds(ws, nr, K, kept, groups, av, pg, d_err, st, S, PairSource(), tn)) != cudaSuccess) return e;
     if ((e = cudaMemcpyAsync(ws.h_small, d_err, 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
     if (ws.radix.prof) ws.radix.prof->flush();

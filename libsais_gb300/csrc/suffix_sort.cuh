@@ -80,6 +80,8 @@ struct EarlySaCopy {
 };
 
 struct SortOptions {
+    Tuning tuning;            // used when tuning_set; otherwise tuning_lookup(n, code bits)
+    bool tuning_set = false;
     int seed_key_bits = 32;   // width of the packed seed prefix (32 or 64)
     uint32_t raw_max = 0;     // 32-bit integer symbols: the largest symbol value
     EarlySaCopy *early = nullptr;
@@ -104,7 +106,8 @@ cudaError_t suffix_sort(const void *d_T, int symbytes, uint64_t n, bool gsa, Sor
 // On return ws.sa holds the rows (rank coordinates) grouped by string.
 size_t batch_workspace_bytes(uint64_t n, uint32_t count);
 cudaError_t batch_suffix_sort(const uint8_t *d_T, uint64_t n, const uint64_t *d_offs, uint32_t count,
-                              SortWorkspace &ws, uint32_t *d_err, cudaStream_t st, SortStats *stats);
+                              SortWorkspace &ws, uint32_t *d_err, cudaStream_t st, SortStats *stats,
+                              const Tuning *tuning = nullptr);
 // Per-string SA (relative to each string), BWT (libsais_bwt layout) and
 // primary indexes from a finished batch_suffix_sort.
 cudaError_t batch_outputs(const SortWorkspace &ws, const uint8_t *d_T, uint64_t n, const uint64_t *d_offs,
@@ -118,6 +121,15 @@ cudaError_t batch_outputs(const SortWorkspace &ws, const uint8_t *d_T, uint64_t 
 cudaError_t symbol_histogram_part(const void *d_part, int symbytes, uint64_t len, uint32_t *d_hist, cudaStream_t st);
 cudaError_t symbol_histogram(const void *d_T, int symbytes, uint64_t n, uint32_t *d_hist, uint32_t *h_hist,
                              cudaStream_t st);
+
+// Phi[SA[j]] = SA[j-1], Phi[SA[0]] = N, for a suffix array of N entries
+// (a permutation of [0, N)), through position partitions when
+// phi_partitioned(N) (scratch: phi_scratch_words(N) words); the caller uses
+// a direct scatter otherwise.
+bool phi_partitioned(uint64_t N);
+size_t phi_scratch_words(uint64_t N);
+cudaError_t phi_permute(const uint32_t *SA, uint64_t N, uint32_t *phi, uint32_t *scratch, uint32_t *d_err,
+                        cudaStream_t st);
 
 // GSA validity of a device text: T[0] != 0, no two adjacent zeros,
 // T[n-1] == 0.  Result through a pinned host word.
