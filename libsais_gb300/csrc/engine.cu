@@ -646,10 +646,13 @@ int64_t gsais_sa_bwt_device(void *ctx, const void *T, int32_t symbytes, int64_t 
     if (!clear_err(c, st)) return fail(cudaErrorUnknown);
     const int64_t rc = run_sort(c, T, symbytes, n, false, ws, st);
     if (rc != 0) return rc;
+    cudaEvent_t ev_bwt = c->prof.begin(st);
     GS_TRY(bwt_gather(T, symbytes, ws.sa, ws.rank, n, U, packed_of(ws), c->d_misc, st));
+    if (ev_bwt) c->prof.end(KK_BWT, ev_bwt, st, n * (4 + 2 * (uint64_t)symbytes));   // SA read, T gathered, U written
     if (SA && sa_bytes == 8) GS_TRY(widen_u32_to_i64(ws.sa, static_cast<int64_t *>(SA), n, st));
     GS_TRY(cudaMemcpyAsync(c->h_small, ws.rank, 4, cudaMemcpyDeviceToHost, st));
     GS_TRY(sync_checked(c, st));
+    c->prof.flush();
     return (int64_t)c->h_small[0];
 }
 
@@ -886,7 +889,8 @@ int32_t gsais_profile_read(void *ctx, gsais_kernel_profile *out, int32_t max_kin
     std::lock_guard<std::mutex> lock(c->mu);
     static const char *names[KK_COUNT] = {"radix_pass",   "tile_counts", "upsweep",      "seed",
                                           "round_keys",   "tile_summary", "assign",      "small_groups",
-                                          "pair_compare", "unbwt"};
+                                          "pair_compare", "unbwt",        "histogram",   "rank_scatter",
+                                          "classify",     "medium_groups", "bwt"};
     int k = 0;
     for (; k < KK_COUNT && k < max_kinds; ++k) {
         out[k].name = names[k];

@@ -18,7 +18,10 @@ extern std::atomic<uint64_t> g_launches;
 // Optional per-kernel timing: CUDA events recorded on the launching stream
 // around each launch of the instrumented kernels, resolved after the stream
 // synchronises.  `bytes` is the algorithmic traffic of the launch.
-enum KernelKind { KK_RADIX_PASS = 0, KK_TILE_COUNTS, KK_UPSWEEP, KK_SEED, KK_ROUND_KEYS, KK_SUMMARY, KK_ASSIGN, KK_SMALL, KK_PAIRS, KK_UNBWT, KK_COUNT };
+enum KernelKind {
+    KK_RADIX_PASS = 0, KK_TILE_COUNTS, KK_UPSWEEP, KK_SEED, KK_ROUND_KEYS, KK_SUMMARY, KK_ASSIGN, KK_SMALL, KK_PAIRS,
+    KK_UNBWT, KK_HIST, KK_PERM, KK_CLASSIFY, KK_MEDIUM, KK_BWT, KK_COUNT
+};
 
 struct KernelProfiler {
     bool enabled = false;
@@ -33,6 +36,11 @@ struct KernelProfiler {
     // returns the start event to pair with end(); nullptr when disabled
     cudaEvent_t begin(cudaStream_t st);
     void end(int kind, cudaEvent_t a, cudaStream_t st, uint64_t bytes);
+    // algorithmic bytes known only after the launch (device-side counts)
+    void add_bytes(int kind, uint64_t b)
+    {
+        if (enabled) bytes[kind] += b;
+    }
     void flush();   // call after the stream has synchronised
     void reset();
     ~KernelProfiler();

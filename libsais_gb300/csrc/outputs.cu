@@ -357,35 +357,6 @@ __device__ __forceinline__ uint32_t lane_window(const TextWords &tw, uint64_t p,
     return (uint64_t)c > m - o ? (uint32_t)(m - o) : c;
 }
 
-// One warp extends from l, 16 bytes per lane per step, for at most `iters`
-// steps.  Returns the first mismatch offset (<= m) with *done, or the offset
-// reached with !*done.
-template <typename Sym, bool GSA>
-__device__ __forceinline__ uint64_t extend_warp(const TextWords &tw, uint64_t p, uint64_t q, uint64_t l, uint64_t m,
-                                                int iters, bool *done)
-{
-    constexpr int PER = 16 / sizeof(Sym);
-    const int lane = threadIdx.x & 31;
-    for (int it = 0; it < iters; ++it) {
-        if (l >= m) {
-            *done = true;
-            return m;
-        }
-        const uint64_t o = l + (uint64_t)lane * PER;
-        const uint32_t c = lane_window<Sym, GSA>(tw, p, q, o, m);
-        const uint32_t ball = __ballot_sync(GSAIS_FULL_MASK, c < (uint32_t)PER);
-        if (ball) {
-            const int f = __ffs(ball) - 1;
-            const uint64_t r = l + (uint64_t)f * PER + __shfl_sync(GSAIS_FULL_MASK, c, f);
-            *done = true;
-            return r < m ? r : m;
-        }
-        l += 32 * PER;
-    }
-    *done = false;
-    return l;
-}
-
 // PLCP of the first chunk start (position 0) from scratch, by every CTA of the
 // grid: CTA g compares blocks g, g + grid, ... of 16 bytes per thread and
 // lowers sparse[0] to the first mismatch it finds; a block that starts at or
@@ -428,10 +399,11 @@ __global__ void k_plcp_first_init(const uint32_t *__restrict__ phi, uint64_t n, 
 }
 
 // One level of exact PLCP values at chunk starts: chunk k = (2w+1)*half takes
-// its lower bound from chunk k - half (PLCP[i+d] >= PLCP[i] - d).  A warp per
-// chunk start extends for at most kLevelIters steps; starts still matching
-// go to the long list for k_plcp_long.
-constexpr int kLevelIters = 8;
+// its lower bound from chunk k - half (PLCP[i+d] >= PLCP[i] - d).  A thread
+// per chunk start extends 8 bytes per step for at most kLevelSteps steps
+// (the bound is tight for most starts); starts still matching go to the
+// long list for k_plcp_long.
+constexpr int kLevelSteps = 16;
 
 template <typename Sym, bool GSA>
 __global__ void __launch_bounds__(256) k_plcp_level(TextWords tw, uint64_t n, const uint32_t *__restrict__ phi,
@@ -439,13 +411,14 @@ __global__ void __launch_bounds__(256) k_plcp_level(TextWords tw, uint64_t n, co
                                                     uint32_t *__restrict__ sparse, uint2 *__restrict__ long_list,
                                                     uint32_t *__restrict__ long_count, uint32_t *__restrict__ err)
 {
-    const uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    constexpr int S = sizeof(Sym), PER = 8 / S;
+    const uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const uint64_t k = (2 * w + 1) * half;
     if (k >= nchunks) return;
     const uint64_t a = k * chunk;
     uint64_t b = phi[a];
     if (b > n) {
-        if ((threadIdx.x & 31) == 0) atomicOr(err, GSAIS_ERR_BOUNDS);
+        atomicOr(err, GSAIS_ERR_BOUNDS);
         b = n;
     }
     uint64_t l = 0;
@@ -457,15 +430,27 @@ __global__ void __launch_bounds__(256) k_plcp_level(TextWords tw, uint64_t n, co
         const uint64_t m = n - (a > b ? a : b);
         l = lp > d ? lp - d : 0;
         if (l > m) l = m;
-        l = extend_warp<Sym, GSA>(tw, a, b, l, m, kLevelIters, &done);
-    }
-    if ((threadIdx.x & 31) == 0) {
-        if (done) {
-            sparse[k] = (uint32_t)l;
-        } else {
-            const uint32_t slot = atomicAdd(long_count, 1u);
-            long_list[slot] = make_uint2((uint32_t)k, (uint32_t)l);
+        done = false;
+        for (int it = 0; it < kLevelSteps; ++it) {
+            if (l >= m) {
+                l = m;
+                done = true;
+                break;
+            }
+            const uint32_t c = eq_symbols<S, GSA>(load8(tw, (a + l) * S), load8(tw, (b + l) * S));
+            l += c;
+            if (c < (uint32_t)PER) {
+                if (l > m) l = m;
+                done = true;
+                break;
+            }
         }
+    }
+    if (done) {
+        sparse[k] = (uint32_t)l;
+    } else {
+        const uint32_t slot = atomicAdd(long_count, 1u);
+        long_list[slot] = make_uint2((uint32_t)k, (uint32_t)l);
     }
 }
 
@@ -645,8 +630,7 @@ cudaError_t plcp_run(const Sym *T, const uint32_t *SA, uint64_t n, uint32_t *plc
     for (uint64_t half = top >> 1; half >= 1; half >>= 1, ++level) {
         const uint64_t count = nchunks > half ? (nchunks - half + 2 * half - 1) / (2 * half) : 0;
         if (count == 0) continue;
-        const uint64_t threads = count * 32;
-        const unsigned blocks = (unsigned)((threads + 255) / 256);
+        const unsigned blocks = (unsigned)((count + 255) / 256);
         GSAIS_COUNTED((k_plcp_level<Sym, GSA><<<blocks, 256, 0, st>>>(tw, n, plcp, kPlcpChunk, nchunks, half,
                                                                        sparse, long_list, counts + level, err)));
         const unsigned lg = (unsigned)(count < (uint64_t)sm_count() * 2 ? count : (uint64_t)sm_count() * 2);

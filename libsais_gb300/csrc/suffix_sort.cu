@@ -633,11 +633,11 @@ __global__ void __launch_bounds__(256) k_classify(const uint32_t *__restrict__ g
             lid[g] = (uint32_t)(old >> 32);
             loff[g] = (uint32_t)old;
         } else if (size > medium_small) {
-            lid[g] = kMedium;
-            mlist2[atomicAdd(mcount2, 1ull)] = (uint32_t)g;
+            lid[g] = kMedium;   // count in the low half, members in the high half
+            mlist2[(uint32_t)atomicAdd(mcount2, (size << 32) | 1ull)] = (uint32_t)g;
         } else if (size > kSmallMax) {
             lid[g] = kMedium;
-            mlist[atomicAdd(mcount, 1ull)] = (uint32_t)g;
+            mlist[(uint32_t)atomicAdd(mcount, (size << 32) | 1ull)] = (uint32_t)g;
         } else {
             lid[g] = kNoLarge;
         }
@@ -1752,9 +1752,9 @@ static cudaError_t run_assign(const TileArgs &a, SortWorkspace &ws, uint32_t *ou
     }
     GSAIS_COUNTED((k_tile_summary<MODE><<<(unsigned)((tiles + 7) / 8), 256, 0, st>>>(a, ws.heads, ws.tile_info)));
     if (ev) prof->end(KK_SUMMARY, ev, st, a.N * (MODE == MODE_ROUND ? 12 : 16));
+    ev = prof ? prof->begin(st) : nullptr;   // the tile scan is timed with the assign
     GSAIS_COUNTED((k_tile_scan<<<1, 1024, 0, st>>>(ws.tile_info, ws.tile_carry, tiles, ws.totals, base,
                                                    a.pairs ? a.pair_count : nullptr)));
-    ev = prof ? prof->begin(st) : nullptr;
     GSAIS_COUNTED((k_assign<MODE><<<(unsigned)tiles, kAssignThreads, 0, st>>>(
         a, ws.tile_carry, ws.heads, ws.rank, ws.sa, out_i, out_pos, out_gid, gstart_out)));
     // algorithmic bytes: key 8 + value 4 + slot 4 read, rank 4 scattered, and
@@ -1776,8 +1776,23 @@ static cudaError_t run_assign(const TileArgs &a, SortWorkspace &ws, uint32_t *ou
 // bits followed by a scatter inside L2-resident windows.
 static bool use_two_level_ranks(uint64_t nr) { return nr >= (1ull << 23); }
 
+static cudaError_t scatter_seed_ranks_impl(SortWorkspace &ws, uint32_t *sorted_pos, uint32_t *ranks, uint64_t N,
+                                           uint64_t nr, uint32_t *d_err, cudaStream_t st);
+
+// Timed as one kernel family: two partitions (16 bytes per entry each) and
+// the window pass (12), or the radix partition and the windowed scatter.
 static cudaError_t scatter_seed_ranks(SortWorkspace &ws, uint32_t *sorted_pos, uint32_t *ranks, uint64_t N,
                                       uint64_t nr, uint32_t *d_err, cudaStream_t st)
+{
+    KernelProfiler *prof = ws.radix.prof;
+    cudaEvent_t ev = prof ? prof->begin(st) : nullptr;
+    const cudaError_t e = scatter_seed_ranks_impl(ws, sorted_pos, ranks, N, nr, d_err, st);
+    if (ev) prof->end(KK_PERM, ev, st, N * 44);
+    return e;
+}
+
+static cudaError_t scatter_seed_ranks_impl(SortWorkspace &ws, uint32_t *sorted_pos, uint32_t *ranks, uint64_t N,
+                                           uint64_t nr, uint32_t *d_err, cudaStream_t st)
 {
     cudaError_t e;
     const int b = gsais_bits_for(nr - 1);
@@ -1950,9 +1965,11 @@ static cudaError_t run_rounds(SortWorkspace &ws, uint64_t nr, int K, uint32_t ke
         if ((e = cudaMemsetAsync(ws.radix.hist, 0, (size_t)passes * 256 * 4, st)) != cudaSuccess) return e;
         uint32_t *mlist = ws.lvals[1];   // free until the large sort's first pass
         uint32_t *mlist2 = ws.lvals[1] + N / 2;   // medium groups have > 32 members: N / 33 of each at most
+        cudaEvent_t ev_cl = ws.radix.prof ? ws.radix.prof->begin(st) : nullptr;
         GSAIS_COUNTED((k_classify<<<stream_grid(G, 256), 256, 0, st>>>(ws.gstart[pg], G, N, ws.lid, ws.loff,
                                                                       ws.counters + 1, mlist, ws.counters + 2, mlist2,
                                                                       ws.counters + 5, medium_small, medium_max)));
+        if (ev_cl) ws.radix.prof->end(KK_CLASSIFY, ev_cl, st, G * 12);   // group table 8 read, class 4 written
         cudaEvent_t ev_rk = ws.radix.prof ? ws.radix.prof->begin(st) : nullptr;
         GSAIS_COUNTED((k_round_r2<<<stream_grid(N, 256), 256, 0, st>>>(
             act_i, act_pos, act_gid, ws.gstart[pg], ws.lid, ws.loff, ws.rank, h, N, nr, b2, r2, ws.keys[0],
@@ -1966,6 +1983,7 @@ static cudaError_t run_rounds(SortWorkspace &ws, uint64_t nr, int K, uint32_t ke
         // medium groups: one wave of resident CTAs, each looping over the
         // groups (their count is on the device)
         const uint64_t mg_max = G < N / (kSmallMax + 1) ? G : N / (kSmallMax + 1);
+        cudaEvent_t ev_md = ws.radix.prof ? ws.radix.prof->begin(st) : nullptr;
         GSAIS_COUNTED((k_medium_groups<128, kMediumSmall>
                        <<<resident_grid(k_medium_groups<128, kMediumSmall>, 128, mg_max), 128, 0, st>>>(
             mlist, ws.counters + 2, ws.gstart[pg], G, N, act_i, act_pos, r2, ws.rank, ws.sa, out_i, out_pos, out_gid,
@@ -1974,15 +1992,23 @@ static cudaError_t run_rounds(SortWorkspace &ws, uint64_t nr, int K, uint32_t ke
                        <<<resident_grid(k_medium_groups<256, kMediumMax>, 256, mg_max), 256, 0, st>>>(
             mlist2, ws.counters + 5, ws.gstart[pg], G, N, act_i, act_pos, r2, ws.rank, ws.sa, out_i, out_pos, out_gid,
             ws.gstart[pg ^ 1], ws.counters)));
+        if (ev_md) ws.radix.prof->end(KK_MEDIUM, ev_md, st, 0);   // bytes added once the member counts are read
         // members of a tied pair share 2h symbols: h by their group, h more by equal r2
         if (pairs && (e = run_pair_compare(ws, ps, pairs, N / 2, 2 * h, out_i, out_pos, out_gid, ws.gstart[pg ^ 1],
                                            d_err, st)) != cudaSuccess)
             return e;
-        if ((e = read_back(ws.h_small, ws.counters, 4 * sizeof(unsigned long long), st)) != cudaSuccess) return e;
+        if ((e = read_back(ws.h_small, ws.counters, 6 * sizeof(unsigned long long), st)) != cudaSuccess) return e;
         if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
-        const unsigned long long small_tot = reinterpret_cast<unsigned long long *>(ws.h_small)[0];
-        const unsigned long long large_tot = reinterpret_cast<unsigned long long *>(ws.h_small)[1];
-        S.pairs_direct += reinterpret_cast<unsigned long long *>(ws.h_small)[3];
+        const unsigned long long *hc = reinterpret_cast<const unsigned long long *>(ws.h_small);
+        const unsigned long long small_tot = hc[0];
+        const unsigned long long large_tot = hc[1];
+        S.pairs_direct += hc[3];
+        if (ws.radix.prof) {
+            // medium members: r2 4 + index 4 + slot 4 read, rank 4 + SA or survivors 8 written
+            ws.radix.prof->add_bytes(KK_MEDIUM, ((hc[2] >> 32) + (hc[5] >> 32)) * 24);
+            // tied pairs: two slots and two indexes read, two ranks and two SA entries written
+            ws.radix.prof->add_bytes(KK_PAIRS, hc[3] * 24);
+        }
         const uint64_t NL = (uint32_t)large_tot;
         if (NL == 0) {
             kept = (uint32_t)small_tot;
@@ -2069,8 +2095,10 @@ cudaError_t suffix_sort(const void *d_T, int symbytes, uint64_t n, bool gsa, Sor
             if ((e = cudaMemcpyAsync(h_hist, ws.hist, (size_t)nsym * 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
                 (e = cudaStreamSynchronize(st)) != cudaSuccess)
                 return e;
-        } else if ((e = symbol_histogram(d_T, symbytes, n, ws.hist, h_hist, st)) != cudaSuccess) {
-            return e;
+        } else {
+            cudaEvent_t ev_h = ws.radix.prof ? ws.radix.prof->begin(st) : nullptr;
+            if ((e = symbol_histogram(d_T, symbytes, n, ws.hist, h_hist, st)) != cudaSuccess) return e;
+            if (ev_h) ws.radix.prof->end(KK_HIST, ev_h, st, n * symbytes);
         }
         uint32_t sigma = 0;
         for (int c = 0; c < nsym; ++c) {
@@ -2256,6 +2284,7 @@ cudaError_t suffix_sort(const void *d_T, int symbytes, uint64_t n, bool gsa, Sor
         kept = (uint32_t)hc[0];
         groups = (uint32_t)(hc[0] >> 32);
         S.pairs_direct += hc[3];
+        if (ws.radix.prof) ws.radix.prof->add_bytes(KK_PAIRS, hc[3] * 24);
     }
 
     // ---- SA leaves for the host while the rank scatter and the rounds run
