@@ -148,7 +148,10 @@ extern "C" {
     * (16, 20, 24, 28) and 64-bit (12, 16, 20) keys, the tile being 256 threads times
     * that; medium_small (64..512) and medium_max (medium_small..4096): unsorted groups
     * of up to medium_small members are split by a 128-thread CTA, up to medium_max by
-    * a 256-thread CTA, larger ones by the global segmented radix sort.
+    * a 256-thread CTA, larger ones by the global segmented radix sort;
+    * large_few_others (0 or 1): a large group whose members mostly carry the same
+    * rank of their suffix h on (runs, tandem repeats) sorts only the other members and
+    * places the rest as one run.
     */
     typedef struct gsais_tuning
     {
@@ -157,6 +160,7 @@ extern "C" {
         int32_t radix_items64;
         int32_t medium_small;
         int32_t medium_max;
+        int32_t large_few_others;
     } gsais_tuning;
 
     /**

@@ -182,11 +182,11 @@ class GsaisStats(ctypes.Structure):
 
 class GsaisTuning(ctypes.Structure):
     _fields_ = [("digit_bits", _i32), ("radix_items32", _i32), ("radix_items64", _i32), ("medium_small", _i32),
-                ("medium_max", _i32)]
+                ("medium_max", _i32), ("large_few_others", _i32)]
 
 
 TUNING_DEFAULTS = {"digit_bits": 8, "radix_items32": 24, "radix_items64": 16, "medium_small": 512,
-                   "medium_max": 4096}
+                   "medium_max": 4096, "large_few_others": 1}
 
 
 def set_tuning(tuning=None, ctx=None) -> int:

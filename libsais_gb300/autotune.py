@@ -10,7 +10,10 @@ lib/libsais_gb300.so (include/libsais_gb300.h, gsais_tuning):
 * medium_small   groups of 33..medium_small members are split by a 128-thread CTA;
 * medium_max     groups up to medium_max by a 256-thread CTA, larger ones by the
                  global segmented radix sort (the cut-over from segmented radix
-                 sort to per-group shared-memory sort).
+                 sort to per-group shared-memory sort);
+* large_few_others  1: a large group whose members mostly share rank[i+h] sorts
+                 only the other members (runs, tandem repeats); 0: always the
+                 full segmented sort.
 
 ``tune(n, bits)`` times SA+BWT of a synthetic text of n symbols whose alphabet
 codes take `bits` bits, on the current GPU, by coordinate descent from the
@@ -39,8 +42,10 @@ CANDIDATES = {
     "radix_items64": [12, 16, 20],
     "medium_small": [128, 256, 512],
     "medium_max": [1024, 2048, 4096],
+    "large_few_others": [1, 0],
 }
-DEFAULTS = {"digit_bits": 8, "radix_items32": 24, "radix_items64": 16, "medium_small": 512, "medium_max": 4096}
+DEFAULTS = {"digit_bits": 8, "radix_items32": 24, "radix_items64": 16, "medium_small": 512, "medium_max": 4096,
+            "large_few_others": 1}
 
 
 def default_cache_path() -> str:

@@ -550,7 +550,7 @@ int64_t gsais_run_plcp(gsais_ctx *c, const void *T, int symbytes, const void *SA
     } else {
         GS_TRY(cudaMemcpyAsync(d_SA, SA, n * 4, cudaMemcpyHostToDevice, st));
     }
-    GS_TRY(plcp_build(d_T, symbytes, d_SA, n, gsa != 0, d_P, d_sparse, c->d_misc, st));
+    GS_TRY(plcp_build(d_T, symbytes, d_SA, n, gsa != 0, d_P, d_sparse, c->h_small + 16, c->d_misc, st));
     if (idx_bytes == 8) {
         GS_TRY(widen_u32_to_i64(d_P, d_wide, n, st));
         GS_TRY(cudaMemcpyAsync(PLCP, d_wide, n * 8, cudaMemcpyDeviceToHost, st));
@@ -682,7 +682,7 @@ int64_t gsais_plcp_device(void *ctx, const void *T, int32_t symbytes, const void
         d_SA = sa32;
     }
     uint32_t *d_sparse = cv.take<uint32_t>(plcp_sparse_words(n));
-    GS_TRY(plcp_build(T, symbytes, d_SA, n, gsa != 0, d_P, d_sparse, c->d_misc, st));
+    GS_TRY(plcp_build(T, symbytes, d_SA, n, gsa != 0, d_P, d_sparse, c->h_small + 16, c->d_misc, st));
     if (idx_bytes == 8) GS_TRY(widen_u32_to_i64(d_P, static_cast<int64_t *>(PLCP), n, st));
     GS_TRY(sync_checked(c, st));
     return 0;
@@ -850,6 +850,7 @@ int32_t gsais_set_tuning(void *ctx, const gsais_tuning *t)
     tn.radix_items64 = t->radix_items64;
     tn.medium_small = t->medium_small;
     tn.medium_max = t->medium_max;
+    tn.large_few_others = t->large_few_others;
     if (!tuning_valid(tn)) return -1;
     c->opt.tuning = tn;
     c->opt.tuning_set = true;
@@ -867,6 +868,7 @@ int32_t gsais_last_tuning(void *ctx, gsais_tuning *out)
     out->radix_items64 = tn.radix_items64;
     out->medium_small = tn.medium_small;
     out->medium_max = tn.medium_max;
+    out->large_few_others = tn.large_few_others;
     return 0;
 }
 
@@ -890,7 +892,7 @@ int32_t gsais_profile_read(void *ctx, gsais_kernel_profile *out, int32_t max_kin
     static const char *names[KK_COUNT] = {"radix_pass",   "tile_counts", "upsweep",      "seed",
                                           "round_keys",   "tile_summary", "assign",      "small_groups",
                                           "pair_compare", "unbwt",        "histogram",   "rank_scatter",
-                                          "classify",     "medium_groups", "bwt"};
+                                          "classify",     "medium_groups", "bwt",         "large_few"};
     int k = 0;
     for (; k < KK_COUNT && k < max_kinds; ++k) {
         out[k].name = names[k];

@@ -20,7 +20,7 @@ extern std::atomic<uint64_t> g_launches;
 // synchronises.  `bytes` is the algorithmic traffic of the launch.
 enum KernelKind {
     KK_RADIX_PASS = 0, KK_TILE_COUNTS, KK_UPSWEEP, KK_SEED, KK_ROUND_KEYS, KK_SUMMARY, KK_ASSIGN, KK_SMALL, KK_PAIRS,
-    KK_UNBWT, KK_HIST, KK_PERM, KK_CLASSIFY, KK_MEDIUM, KK_BWT, KK_COUNT
+    KK_UNBWT, KK_HIST, KK_PERM, KK_CLASSIFY, KK_MEDIUM, KK_BWT, KK_FEW, KK_COUNT
 };
 
 struct KernelProfiler {
@@ -106,6 +106,7 @@ struct SortStats {
     uint64_t early_patch = 0;      // SA slots written to the host after an early SA copy
     int radix_passes = 0;          // non-trivial digit passes over all sorts
     Tuning tuning;                 // the tuning the sort ran with
+    int few_rounds = 0;            // rounds whose large groups took the few-others path
 };
 
 }  // namespace gsais

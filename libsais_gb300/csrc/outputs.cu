@@ -6,6 +6,7 @@
 // the context's error word and the access is skipped, so a malformed caller
 // array becomes a -2 return instead of a device fault.
 #include <type_traits>
+#include <vector>
 
 #include "device_util.cuh"
 #include "engine.h"
@@ -98,35 +99,55 @@ __device__ __forceinline__ Sym bwt_symbol(const Sym *__restrict__ T, uint64_t q,
 }
 
 template <typename Sym>
-__global__ void __launch_bounds__(256, 4) k_bwt_words(const Sym *__restrict__ T, const uint32_t *__restrict__ SA,
-                                                      uint64_t n, const uint32_t *__restrict__ isa1,
-                                                      Sym *__restrict__ U, PackedText pk, uint32_t *__restrict__ err)
+__global__ void __launch_bounds__(256) k_bwt_words(const Sym *__restrict__ T, const uint32_t *__restrict__ SA,
+                                                   uint64_t n, const uint32_t *__restrict__ isa1,
+                                                   Sym *__restrict__ U, PackedText pk, uint32_t *__restrict__ err)
 {
-    constexpr int B = 2;
+    constexpr int B = 2;   // words per thread per step
     using Word = typename std::conditional<sizeof(Sym) == 1, uint32_t, uint2>::type;
     __shared__ Sym dec[16];
     if (threadIdx.x < 16) dec[threadIdx.x] = (Sym)pk.decode[threadIdx.x];
     __syncthreads();
     const uint8_t *packed = pk.packed;
     const int pack_bits = pk.pack_bits;
+    const int lane = threadIdx.x & 31;
     const uint64_t i0 = (uint64_t)isa1[0] - 1;   // SA row of suffix 0
     const uint64_t words = (n + 3) / 4;
+    const uint64_t full4 = n / 4;                 // whole 16-byte groups of SA
+    const uint4 *SA4 = reinterpret_cast<const uint4 *>(SA);
     const uint64_t span = (uint64_t)gridDim.x * blockDim.x * B;
     bool bad = false;
-    for (uint64_t w0 = (uint64_t)blockIdx.x * blockDim.x * B + threadIdx.x; w0 < words; w0 += span) {
+    // every thread of a warp runs the same number of steps (the shuffle below)
+    const uint64_t w_round = (words + 31) & ~31ull;
+    for (uint64_t w0 = (uint64_t)blockIdx.x * blockDim.x * B + threadIdx.x; w0 - lane < w_round; w0 += span) {
         uint32_t p[B][4];
-#pragma unroll
-        for (int j = 0; j < B; ++j)
-#pragma unroll
-            for (int r = 0; r < 4; ++r) {
-                const uint64_t k = (w0 + (uint64_t)j * blockDim.x) * 4 + r;
-                const uint64_t row = k <= i0 ? k - 1 : k;
-                p[j][r] = (k > 0 && k < n && row < n) ? SA[row] : 0u;
-            }
 #pragma unroll
         for (int j = 0; j < B; ++j) {
             const uint64_t w = w0 + (uint64_t)j * blockDim.x;
-            if (w >= words) break;
+            // rows 4w .. 4w+3, streamed (not kept in L2)
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (w < full4) {
+                v = __ldcs(SA4 + w);
+            } else if (w < words) {
+                uint32_t t[4] = {0, 0, 0, 0};
+                for (int r = 0; r < 4; ++r)
+                    if (w * 4 + r < n) t[r] = SA[w * 4 + r];
+                v = make_uint4(t[0], t[1], t[2], t[3]);
+            }
+            // row 4w - 1 (output 4w below the primary row): the previous lane's last row
+            uint32_t prev = __shfl_up_sync(GSAIS_FULL_MASK, v.w, 1);
+            if (lane == 0) prev = (w > 0 && w - 1 < words && 4 * w - 1 < n) ? SA[4 * w - 1] : 0u;
+            // output k = 4w + r takes row k - 1 up to the primary row, row k after it
+            const uint64_t k0 = w * 4;
+            p[j][0] = k0 <= i0 ? prev : v.x;
+            p[j][1] = k0 + 1 <= i0 ? v.x : v.y;
+            p[j][2] = k0 + 2 <= i0 ? v.y : v.z;
+            p[j][3] = k0 + 3 <= i0 ? v.z : v.w;
+        }
+#pragma unroll
+        for (int j = 0; j < B; ++j) {
+            const uint64_t w = w0 + (uint64_t)j * blockDim.x;
+            if (w >= words) continue;
             Sym v[4];
 #pragma unroll
             for (int r = 0; r < 4; ++r) {
@@ -151,7 +172,7 @@ __global__ void __launch_bounds__(256, 4) k_bwt_words(const Sym *__restrict__ T,
                     o2.y = (uint32_t)v[2] | ((uint32_t)v[3] << 16);
                     reinterpret_cast<uint2 &>(out) = o2;
                 }
-                reinterpret_cast<Word *>(U)[w] = out;
+                __stcs(reinterpret_cast<Word *>(U) + w, out);
             } else {
 #pragma unroll
                 for (int r = 0; r < 4; ++r)
@@ -285,14 +306,27 @@ __global__ void __launch_bounds__(256) k_phi(const uint32_t *__restrict__ SA, ui
     }
 }
 
-// ---- symbol comparison on 8-byte windows of the text.  The text is read as
-// aligned 64-bit words (a window at any byte offset is two words and a
-// funnel shift); a word not wholly inside the text is assembled byte by byte,
-// bytes past the end reading as 0 (every caller clamps lengths to the text).
+// ---- symbol comparison on 64-bit windows of the text.  A window at symbol p
+// holds the symbols p, p+1, ... least significant first, SB bits each:
+//   PB = 0: the raw text (SB = 8 * sizeof(Sym)), read as aligned 64-bit words
+//           (a window at any byte offset is two words and a funnel shift; a
+//           word not wholly inside the text is assembled byte by byte, bytes
+//           past the end reading as 0);
+//   PB = 2 or 4: the text as dense codes of PB bits (plcp_build packs it when
+//           the alphabet has at most 16 symbols), two 64-bit words and a
+//           funnel shift; the packed array ends with two zero words.
+// Every caller clamps lengths to the text, so the contents past the end do
+// not matter.
 struct TextWords {
-    const uint8_t *T;   // the text
-    uint64_t nbytes;    // its length in bytes
-    uint32_t mis;       // T's offset past the previous 8-byte boundary
+    const uint8_t *T;         // the raw text
+    uint64_t nbytes;          // its length in bytes
+    uint32_t mis;             // T's offset past the previous 8-byte boundary
+    const uint64_t *packed;   // PB > 0: the packed codes
+};
+
+template <typename Sym, int PB>
+struct SymBits {
+    static constexpr int value = PB ? PB : 8 * (int)sizeof(Sym);
 };
 
 __device__ __forceinline__ uint64_t load8(const TextWords &tw, uint64_t off)
@@ -315,57 +349,73 @@ __device__ __forceinline__ uint64_t load8(const TextWords &tw, uint64_t off)
     return v;
 }
 
-// Equal leading symbols of two 8-byte windows (S-byte symbols, little
-// endian); GSA also stops at a 0 symbol of x (a separator ends a suffix).
-template <int S, bool GSA>
+template <typename Sym, int PB>
+__device__ __forceinline__ uint64_t window(const TextWords &tw, uint64_t p)
+{
+    if (PB == 0) return load8(tw, p * sizeof(Sym));
+    const uint64_t bit = p * PB;
+    const uint64_t w = bit >> 6;
+    const uint32_t sh = (uint32_t)(bit & 63);
+    const uint64_t lo = __ldg(tw.packed + w);
+    if (sh == 0) return lo;
+    return (lo >> sh) | (__ldg(tw.packed + w + 1) << (64 - sh));
+}
+
+// Equal leading symbols of two windows of SB-bit symbols; GSA also stops at a
+// 0 symbol (code 0 when packed: the separator is the smallest symbol) of x.
+template <int SB, bool GSA>
 __device__ __forceinline__ uint32_t eq_symbols(uint64_t x, uint64_t y)
 {
     uint64_t stop = x ^ y;
     if (GSA) {
-        // lowest flagged symbol = the first 0 symbol (borrows only run upwards)
-        if (S == 1) stop |= (x - 0x0101010101010101ull) & ~x & 0x8080808080808080ull;
-        if (S == 2) stop |= (x - 0x0001000100010001ull) & ~x & 0x8000800080008000ull;
+        // lowest flagged field = the first 0 field (borrows only run upwards)
+        constexpr uint64_t lo = SB == 2 ? 0x5555555555555555ull
+                              : SB == 4 ? 0x1111111111111111ull
+                              : SB == 8 ? 0x0101010101010101ull
+                                        : 0x0001000100010001ull;
+        stop |= (x - lo) & ~x & (lo << (SB - 1));
     }
     const uint32_t bit = stop ? (uint32_t)(__ffsll((long long)stop) - 1) : 64u;
-    return bit / (8 * S);
+    return bit / SB;
 }
 
 // First mismatch offset >= l of the suffixes at p and q, at most m (one
-// thread, 8 bytes per step).  Plain texts: m = n - max(p, q) (src/libsais.c:8177);
-// GSA also stops at a separator (:8215-8238).
-template <typename Sym, bool GSA>
+// thread, one 64-bit window per step).  Plain texts: m = n - max(p, q)
+// (src/libsais.c:8177); GSA also stops at a separator (:8215-8238).
+template <typename Sym, bool GSA, int PB>
 __device__ __forceinline__ uint64_t extend_thread(const TextWords &tw, uint64_t p, uint64_t q, uint64_t l, uint64_t m)
 {
-    constexpr int S = sizeof(Sym), PER = 8 / S;
+    constexpr int SB = SymBits<Sym, PB>::value, PER = 64 / SB;
     while (l < m) {
-        const uint32_t c = eq_symbols<S, GSA>(load8(tw, (p + l) * S), load8(tw, (q + l) * S));
+        const uint32_t c = eq_symbols<SB, GSA>(window<Sym, PB>(tw, p + l), window<Sym, PB>(tw, q + l));
         l += c;
-        if (c < PER) break;
+        if (c < (uint32_t)PER) break;
     }
     return l < m ? l : m;
 }
 
-// Equal leading symbols of the 16-byte windows at symbol offset o (capped at
-// m - o; 0 if o >= m).
-template <typename Sym, bool GSA>
+// Equal leading symbols of two consecutive windows at symbol offset o
+// (capped at m - o; 0 if o >= m).
+template <typename Sym, bool GSA, int PB>
 __device__ __forceinline__ uint32_t lane_window(const TextWords &tw, uint64_t p, uint64_t q, uint64_t o, uint64_t m)
 {
-    constexpr int S = sizeof(Sym), HALF = 8 / S;
+    constexpr int SB = SymBits<Sym, PB>::value, HALF = 64 / SB;
     if (o >= m) return 0;
-    uint32_t c = eq_symbols<S, GSA>(load8(tw, (p + o) * S), load8(tw, (q + o) * S));
-    if (c == HALF) c += eq_symbols<S, GSA>(load8(tw, (p + o + HALF) * S), load8(tw, (q + o + HALF) * S));
+    uint32_t c = eq_symbols<SB, GSA>(window<Sym, PB>(tw, p + o), window<Sym, PB>(tw, q + o));
+    if (c == (uint32_t)HALF)
+        c += eq_symbols<SB, GSA>(window<Sym, PB>(tw, p + o + HALF), window<Sym, PB>(tw, q + o + HALF));
     return (uint64_t)c > m - o ? (uint32_t)(m - o) : c;
 }
 
 // PLCP of the first chunk start (position 0) from scratch, by every CTA of the
-// grid: CTA g compares blocks g, g + grid, ... of 16 bytes per thread and
+// grid: CTA g compares blocks g, g + grid, ... of two windows per thread and
 // lowers sparse[0] to the first mismatch it finds; a block that starts at or
 // beyond the value already found is skipped.  sparse[0] holds m (or 0) on entry.
-template <typename Sym, bool GSA>
+template <typename Sym, bool GSA, int PB>
 __global__ void __launch_bounds__(256) k_plcp_first(TextWords tw, uint64_t n, const uint32_t *__restrict__ phi,
                                                     uint32_t *sparse)
 {
-    constexpr int PER = 16 / sizeof(Sym);
+    constexpr int PER = 2 * 64 / SymBits<Sym, PB>::value;
     constexpr uint64_t BLK = 256 * PER;
     const uint64_t b = phi[0];
     if (b >= n) return;   // suffix 0 is first in SA (or a bad entry): PLCP 0
@@ -381,7 +431,7 @@ __global__ void __launch_bounds__(256) k_plcp_first(TextWords tw, uint64_t n, co
         __syncthreads();
         if (o0 >= m || o0 >= s_cur) break;   // the same decision in every thread
         const uint64_t o = o0 + (uint64_t)threadIdx.x * PER;
-        const uint32_t c = lane_window<Sym, GSA>(tw, 0, b, o, m);
+        const uint32_t c = lane_window<Sym, GSA, PB>(tw, 0, b, o, m);
         if (c < (uint32_t)PER) atomicMin(&s_min, (unsigned long long)(o + c));
         __syncthreads();
         if (threadIdx.x == 0 && s_min != ~0ull) atomicMin(sparse, (uint32_t)(s_min < m ? s_min : m));
@@ -400,18 +450,18 @@ __global__ void k_plcp_first_init(const uint32_t *__restrict__ phi, uint64_t n, 
 
 // One level of exact PLCP values at chunk starts: chunk k = (2w+1)*half takes
 // its lower bound from chunk k - half (PLCP[i+d] >= PLCP[i] - d).  A thread
-// per chunk start extends 8 bytes per step for at most kLevelSteps steps
+// per chunk start extends one window per step for at most kLevelSteps steps
 // (the bound is tight for most starts); starts still matching go to the
 // long list for k_plcp_long.
 constexpr int kLevelSteps = 16;
 
-template <typename Sym, bool GSA>
+template <typename Sym, bool GSA, int PB>
 __global__ void __launch_bounds__(256) k_plcp_level(TextWords tw, uint64_t n, const uint32_t *__restrict__ phi,
                                                     uint32_t chunk, uint64_t nchunks, uint64_t half,
                                                     uint32_t *__restrict__ sparse, uint2 *__restrict__ long_list,
                                                     uint32_t *__restrict__ long_count, uint32_t *__restrict__ err)
 {
-    constexpr int S = sizeof(Sym), PER = 8 / S;
+    constexpr int SB = SymBits<Sym, PB>::value, PER = 64 / SB;
     const uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const uint64_t k = (2 * w + 1) * half;
     if (k >= nchunks) return;
@@ -437,7 +487,7 @@ __global__ void __launch_bounds__(256) k_plcp_level(TextWords tw, uint64_t n, co
                 done = true;
                 break;
             }
-            const uint32_t c = eq_symbols<S, GSA>(load8(tw, (a + l) * S), load8(tw, (b + l) * S));
+            const uint32_t c = eq_symbols<SB, GSA>(window<Sym, PB>(tw, a + l), window<Sym, PB>(tw, b + l));
             l += c;
             if (c < (uint32_t)PER) {
                 if (l > m) l = m;
@@ -454,15 +504,15 @@ __global__ void __launch_bounds__(256) k_plcp_level(TextWords tw, uint64_t n, co
     }
 }
 
-// The long extensions of one level: a CTA per listed start, 256 threads x 16
-// bytes per step.
-template <typename Sym, bool GSA>
+// The long extensions of one level: a CTA per listed start, 256 threads x two
+// windows per step.
+template <typename Sym, bool GSA, int PB>
 __global__ void __launch_bounds__(256) k_plcp_long(TextWords tw, uint64_t n, const uint32_t *__restrict__ phi,
                                                    uint32_t chunk, uint32_t *__restrict__ sparse,
                                                    const uint2 *__restrict__ long_list,
                                                    const uint32_t *__restrict__ long_count)
 {
-    constexpr int PER = 16 / sizeof(Sym);
+    constexpr int PER = 2 * 64 / SymBits<Sym, PB>::value;
     __shared__ unsigned long long s_min;
     const uint32_t count = *long_count;
     for (uint32_t j = blockIdx.x; j < count; j += gridDim.x) {
@@ -475,7 +525,7 @@ __global__ void __launch_bounds__(256) k_plcp_long(TextWords tw, uint64_t n, con
             if (threadIdx.x == 0) s_min = ~0ull;
             __syncthreads();
             const uint64_t o = l + (uint64_t)threadIdx.x * PER;
-            const uint32_t c = lane_window<Sym, GSA>(tw, a, b, o, m);
+            const uint32_t c = lane_window<Sym, GSA, PB>(tw, a, b, o, m);
             if (c < (uint32_t)PER) atomicMin(&s_min, (unsigned long long)(o + c));
             __syncthreads();
             const unsigned long long r = s_min;
@@ -499,7 +549,7 @@ constexpr uint32_t kPlcpChunk = 64;
 constexpr int kKasaiThreads = 128;
 constexpr int kKasaiStride = kPlcpChunk + 1;   // padded rows: no bank conflicts
 
-template <typename Sym, bool GSA>
+template <typename Sym, bool GSA, int PB>
 __global__ void __launch_bounds__(kKasaiThreads) k_plcp_kasai(TextWords tw, uint64_t n, uint64_t nchunks,
                                                               const uint32_t *__restrict__ sparse,
                                                               uint32_t *__restrict__ plcp, uint32_t *__restrict__ err)
@@ -531,7 +581,7 @@ __global__ void __launch_bounds__(kKasaiThreads) k_plcp_kasai(TextWords tw, uint
                 l = l ? l - 1 : 0;
                 const uint64_t m = n - (x > b ? x : b);
                 if (l > m) l = m;
-                l = extend_thread<Sym, GSA>(tw, x, b, l, m);
+                l = extend_thread<Sym, GSA, PB>(tw, x, b, l, m);
             }
             row[x - a] = (uint32_t)l;
         }
@@ -576,37 +626,71 @@ __global__ void __launch_bounds__(256) k_lcp(const uint32_t *__restrict__ plcp, 
     if (bad) atomicOr(err, GSAIS_ERR_BOUNDS);
 }
 
+// The text as dense codes of B bits, least significant first, one 64-bit
+// word per thread step; words past the text (the two padding words) are 0.
+// Bytes per symbol: sizeof(Sym) read (+ a code-table lookup), B/8 written.
+template <typename Sym, int B>
+__global__ void __launch_bounds__(256) k_pack_codes(const Sym *__restrict__ T, uint64_t n,
+                                                    const uint16_t *__restrict__ codes, uint64_t *__restrict__ packed,
+                                                    uint64_t words)
+{
+    constexpr int SPW = 64 / B;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; w < words; w += stride) {
+        uint64_t v = 0;
+        const uint64_t p0 = w * SPW;
+#pragma unroll 8
+        for (int k = 0; k < SPW; ++k) {
+            const uint64_t p = p0 + k;
+            if (p < n) v |= (uint64_t)__ldg(codes + T[p]) << (k * B);
+        }
+        packed[w] = v;
+    }
+}
+
 // Scratch of plcp_run, in words: chunk-start values, the long list (two words
 // per entry, at most one entry per chunk start of a level), per-level long
-// counts, and the Phi partitions' scratch.
+// counts, the Phi partitions' scratch, and the packed text with its symbol
+// histogram and code table.
 constexpr int kMaxLevels = 40;
 
 uint64_t plcp_chunks(uint64_t n) { return (n + kPlcpChunk - 1) / kPlcpChunk; }
 
-size_t plcp_scratch_layout(uint64_t n, size_t *o_long, size_t *o_counts, size_t *o_phi)
+struct PlcpLayout {
+    size_t o_long, o_counts, o_phi, o_hist, o_codes, o_packed, total;
+};
+
+PlcpLayout plcp_scratch_layout(uint64_t n)
 {
+    PlcpLayout L;
     const uint64_t nc = plcp_chunks(n);
     size_t w = (nc + 2 + 63) / 64 * 64;   // sparse
-    *o_long = w;
+    L.o_long = w;
     w += 2 * ((nc / 2 + 2 + 31) / 32 * 32);
-    *o_counts = w;
+    L.o_counts = w;
     w += 64;
-    *o_phi = w;
-    w += phi_scratch_words(n);
-    return w;
+    L.o_phi = w;
+    w += (phi_scratch_words(n) + 63) / 64 * 64;
+    L.o_hist = w;
+    w += 65536;
+    L.o_codes = w;
+    w += 32768;   // 65536 16-bit codes
+    L.o_packed = w;
+    w += 2 * ((n + 15) / 16 + 2) + 64;   // 4-bit codes at most, as 64-bit words + 2 padding words
+    L.total = w;
+    return L;
 }
 
-template <typename Sym, bool GSA>
+template <typename Sym, bool GSA, int PB>
 cudaError_t plcp_run(const Sym *T, const uint32_t *SA, uint64_t n, uint32_t *plcp, uint32_t *scratch, uint32_t *err,
                      cudaStream_t st)
 {
-    size_t o_long, o_counts, o_phi;
-    plcp_scratch_layout(n, &o_long, &o_counts, &o_phi);
+    const PlcpLayout L = plcp_scratch_layout(n);
     uint32_t *sparse = scratch;
-    uint2 *long_list = reinterpret_cast<uint2 *>(scratch + o_long);
-    uint32_t *counts = scratch + o_counts;
+    uint2 *long_list = reinterpret_cast<uint2 *>(scratch + L.o_long);
+    uint32_t *counts = scratch + L.o_counts;
     if (phi_partitioned(n)) {
-        cudaError_t e = phi_permute(SA, n, plcp, scratch + o_phi, err, st);
+        cudaError_t e = phi_permute(SA, n, plcp, scratch + L.o_phi, err, st);
         if (e != cudaSuccess) return e;
     } else {
         GSAIS_COUNTED((k_phi<<<grid_for(n, 256), 256, 0, st>>>(SA, n, plcp, err)));
@@ -615,6 +699,7 @@ cudaError_t plcp_run(const Sym *T, const uint32_t *SA, uint64_t n, uint32_t *plc
     tw.T = reinterpret_cast<const uint8_t *>(T);
     tw.nbytes = n * sizeof(Sym);
     tw.mis = (uint32_t)(reinterpret_cast<uintptr_t>(T) & 7);
+    tw.packed = reinterpret_cast<const uint64_t *>(scratch + L.o_packed);
     const uint64_t nchunks = plcp_chunks(n);
     uint64_t top = 1;
     int levels = 0;
@@ -625,21 +710,68 @@ cudaError_t plcp_run(const Sym *T, const uint32_t *SA, uint64_t n, uint32_t *plc
     if (levels > kMaxLevels) return cudaErrorInvalidValue;
     // level 0: chunk 0 from scratch, by the whole grid
     GSAIS_COUNTED((k_plcp_first_init<<<1, 1, 0, st>>>(plcp, n, sparse, counts, levels, err)));
-    GSAIS_COUNTED((k_plcp_first<Sym, GSA><<<sm_count() * 4, 256, 0, st>>>(tw, n, plcp, sparse)));
+    GSAIS_COUNTED((k_plcp_first<Sym, GSA, PB><<<sm_count() * 4, 256, 0, st>>>(tw, n, plcp, sparse)));
     int level = 0;
     for (uint64_t half = top >> 1; half >= 1; half >>= 1, ++level) {
         const uint64_t count = nchunks > half ? (nchunks - half + 2 * half - 1) / (2 * half) : 0;
         if (count == 0) continue;
         const unsigned blocks = (unsigned)((count + 255) / 256);
-        GSAIS_COUNTED((k_plcp_level<Sym, GSA><<<blocks, 256, 0, st>>>(tw, n, plcp, kPlcpChunk, nchunks, half,
-                                                                       sparse, long_list, counts + level, err)));
+        GSAIS_COUNTED((k_plcp_level<Sym, GSA, PB><<<blocks, 256, 0, st>>>(tw, n, plcp, kPlcpChunk, nchunks, half,
+                                                                           sparse, long_list, counts + level, err)));
         const unsigned lg = (unsigned)(count < (uint64_t)sm_count() * 2 ? count : (uint64_t)sm_count() * 2);
-        GSAIS_COUNTED((k_plcp_long<Sym, GSA><<<lg, 256, 0, st>>>(tw, n, plcp, kPlcpChunk, sparse, long_list,
-                                                                 counts + level)));
+        GSAIS_COUNTED((k_plcp_long<Sym, GSA, PB><<<lg, 256, 0, st>>>(tw, n, plcp, kPlcpChunk, sparse, long_list,
+                                                                     counts + level)));
     }
-    GSAIS_COUNTED((k_plcp_kasai<Sym, GSA><<<(unsigned)((nchunks + kKasaiThreads - 1) / kKasaiThreads), kKasaiThreads,
-                                            0, st>>>(tw, n, nchunks, sparse, plcp, err)));
+    GSAIS_COUNTED((k_plcp_kasai<Sym, GSA, PB><<<(unsigned)((nchunks + kKasaiThreads - 1) / kKasaiThreads),
+                                                kKasaiThreads, 0, st>>>(tw, n, nchunks, sparse, plcp, err)));
     return cudaGetLastError();
+}
+
+// Packs an 8- or 16-bit text into dense 2- or 4-bit codes when its alphabet
+// has at most 16 symbols (the random text reads of the PLCP kernels then hit
+// a quarter or half of the bytes, which stays in L2 for texts up to ~2^29
+// symbols).  Returns the code width (0: not packed).  Synchronises st.
+template <typename Sym>
+cudaError_t pack_for_plcp(const Sym *T, uint64_t n, uint32_t *scratch, uint32_t *h_hist, cudaStream_t st, int *bits)
+{
+    *bits = 0;
+    if (!h_hist || n < (1u << 16)) return cudaSuccess;   // small texts: the raw text is cache-resident anyway
+    const PlcpLayout L = plcp_scratch_layout(n);
+    const int nsym = sizeof(Sym) == 1 ? 256 : 65536;
+    cudaError_t e = symbol_histogram(T, (int)sizeof(Sym), n, scratch + L.o_hist, h_hist, st);
+    if (e != cudaSuccess) return e;
+    std::vector<uint16_t> codes(nsym, 0);
+    uint32_t sigma = 0;
+    for (int c = 0; c < nsym; ++c) {
+        codes[c] = (uint16_t)sigma;
+        if (h_hist[c]) ++sigma;
+    }
+    if (sigma > 16) return cudaSuccess;
+    const int B = sigma <= 4 ? 2 : 4;
+    uint16_t *d_codes = reinterpret_cast<uint16_t *>(scratch + L.o_codes);
+    if ((e = cudaMemcpyAsync(d_codes, codes.data(), (size_t)nsym * 2, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+        return e;
+    uint64_t *packed = reinterpret_cast<uint64_t *>(scratch + L.o_packed);
+    const uint64_t words = (n * B + 63) / 64 + 2;
+    if (B == 2)
+        GSAIS_COUNTED((k_pack_codes<Sym, 2><<<grid_for(words, 256), 256, 0, st>>>(T, n, d_codes, packed, words)));
+    else
+        GSAIS_COUNTED((k_pack_codes<Sym, 4><<<grid_for(words, 256), 256, 0, st>>>(T, n, d_codes, packed, words)));
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;   // codes (pageable) are copied
+    *bits = B;
+    return cudaGetLastError();
+}
+
+template <typename Sym, bool GSA>
+cudaError_t plcp_dispatch(const Sym *T, const uint32_t *SA, uint64_t n, uint32_t *plcp, uint32_t *scratch,
+                          uint32_t *h_hist, uint32_t *err, cudaStream_t st)
+{
+    int bits = 0;
+    cudaError_t e = pack_for_plcp(T, n, scratch, h_hist, st, &bits);
+    if (e != cudaSuccess) return e;
+    if (bits == 2) return plcp_run<Sym, GSA, 2>(T, SA, n, plcp, scratch, err, st);
+    if (bits == 4) return plcp_run<Sym, GSA, 4>(T, SA, n, plcp, scratch, err, st);
+    return plcp_run<Sym, GSA, 0>(T, SA, n, plcp, scratch, err, st);
 }
 
 }  // namespace
@@ -649,12 +781,13 @@ cudaError_t bwt_gather(const void *d_T, int symbytes, const uint32_t *d_SA, cons
 {
     if (n == 0) return cudaSuccess;
     const uintptr_t ua = reinterpret_cast<uintptr_t>(d_U);
-    if (symbytes == 1 && (ua & 3) == 0) {
+    const bool sa16 = (reinterpret_cast<uintptr_t>(d_SA) & 15) == 0;   // 16-byte SA loads
+    if (symbytes == 1 && (ua & 3) == 0 && sa16) {
         GSAIS_COUNTED((k_bwt_words<uint8_t><<<grid_for((n + 7) / 8, 256), 256, 0, st>>>(
             static_cast<const uint8_t *>(d_T), d_SA, n, d_isa1, static_cast<uint8_t *>(d_U), pk, err)));
         return cudaGetLastError();
     }
-    if (symbytes == 2 && (ua & 7) == 0) {
+    if (symbytes == 2 && (ua & 7) == 0 && sa16) {
         GSAIS_COUNTED((k_bwt_words<uint16_t><<<grid_for((n + 7) / 8, 256), 256, 0, st>>>(
             static_cast<const uint16_t *>(d_T), d_SA, n, d_isa1, static_cast<uint16_t *>(d_U), pk, err)));
         return cudaGetLastError();
@@ -709,28 +842,24 @@ cudaError_t narrow_i64_to_u32(const int64_t *src, uint32_t *dst, uint64_t n, uin
     return cudaGetLastError();
 }
 
-size_t plcp_sparse_words(uint64_t n)
-{
-    size_t a, b, c;
-    return plcp_scratch_layout(n, &a, &b, &c);
-}
+size_t plcp_sparse_words(uint64_t n) { return plcp_scratch_layout(n).total; }
 
 cudaError_t plcp_build(const void *d_T, int symbytes, const uint32_t *d_SA, uint64_t n, bool gsa, uint32_t *d_PLCP,
-                       uint32_t *d_sparse, uint32_t *err, cudaStream_t st)
+                       uint32_t *d_sparse, uint32_t *h_hist, uint32_t *err, cudaStream_t st)
 {
     if (n == 0) return cudaSuccess;
     if (symbytes == 4) {   // integer symbols (libsais_plcp_int, src/libsais.c:8399): plain stop rule
         const uint32_t *T = static_cast<const uint32_t *>(d_T);
-        return plcp_run<uint32_t, false>(T, d_SA, n, d_PLCP, d_sparse, err, st);
+        return plcp_run<uint32_t, false, 0>(T, d_SA, n, d_PLCP, d_sparse, err, st);
     }
     if (symbytes == 1) {
         const uint8_t *T = static_cast<const uint8_t *>(d_T);
-        return gsa ? plcp_run<uint8_t, true>(T, d_SA, n, d_PLCP, d_sparse, err, st)
-                   : plcp_run<uint8_t, false>(T, d_SA, n, d_PLCP, d_sparse, err, st);
+        return gsa ? plcp_dispatch<uint8_t, true>(T, d_SA, n, d_PLCP, d_sparse, h_hist, err, st)
+                   : plcp_dispatch<uint8_t, false>(T, d_SA, n, d_PLCP, d_sparse, h_hist, err, st);
     }
     const uint16_t *T = static_cast<const uint16_t *>(d_T);
-    return gsa ? plcp_run<uint16_t, true>(T, d_SA, n, d_PLCP, d_sparse, err, st)
-               : plcp_run<uint16_t, false>(T, d_SA, n, d_PLCP, d_sparse, err, st);
+    return gsa ? plcp_dispatch<uint16_t, true>(T, d_SA, n, d_PLCP, d_sparse, h_hist, err, st)
+               : plcp_dispatch<uint16_t, false>(T, d_SA, n, d_PLCP, d_sparse, h_hist, err, st);
 }
 
 cudaError_t int_alphabet_scan(const void *d_T, int tbytes, uint64_t n, int64_t k, unsigned long long *d_out,

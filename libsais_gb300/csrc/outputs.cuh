@@ -38,9 +38,12 @@ cudaError_t narrow_i64_to_u32(const int64_t *src, uint32_t *dst, uint64_t n, uin
 
 // PLCP of (T, SA) into d_PLCP (uint32), using d_sparse (plcp_sparse_words(n)
 // words) as scratch.  gsa stops at separators (src/libsais.c:8215-8238).
+// h_hist (65536 host words, may be null): read-back buffer for the symbol
+// histogram; with it, 8- and 16-bit texts of at most 16 symbols are packed
+// into 2- or 4-bit codes first and the comparisons read the packed text.
 size_t plcp_sparse_words(uint64_t n);
 cudaError_t plcp_build(const void *d_T, int symbytes, const uint32_t *d_SA, uint64_t n, bool gsa, uint32_t *d_PLCP,
-                       uint32_t *d_sparse, uint32_t *err, cudaStream_t st);
+                       uint32_t *d_sparse, uint32_t *h_hist, uint32_t *err, cudaStream_t st);
 
 // Integer alphabets (int32 or int64 symbols, tbytes 4 or 8): d_out[0] = the
 // largest value, d_out[1] = 1 if some value lies outside [0, k).

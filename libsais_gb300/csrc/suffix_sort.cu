@@ -621,7 +621,7 @@ __global__ void __launch_bounds__(256) k_classify(const uint32_t *__restrict__ g
                                                   uint32_t *__restrict__ mlist, unsigned long long *__restrict__ mcount,
                                                   uint32_t *__restrict__ mlist2,
                                                   unsigned long long *__restrict__ mcount2, uint32_t medium_small,
-                                                  uint32_t medium_max)
+                                                  uint32_t medium_max, uint32_t *__restrict__ lstart)
 {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < G; g += stride) {
@@ -632,6 +632,7 @@ __global__ void __launch_bounds__(256) k_classify(const uint32_t *__restrict__ g
             const unsigned long long old = atomicAdd(lcount, (1ull << 32) | size);
             lid[g] = (uint32_t)(old >> 32);
             loff[g] = (uint32_t)old;
+            lstart[old >> 32] = (uint32_t)old;   // large id -> first slot in the large list
         } else if (size > medium_small) {
             lid[g] = kMedium;   // count in the low half, members in the high half
             mlist2[(uint32_t)atomicAdd(mcount2, (size << 32) | 1ull)] = (uint32_t)g;
@@ -643,6 +644,230 @@ __global__ void __launch_bounds__(256) k_classify(const uint32_t *__restrict__ g
         }
     }
 }
+
+// ---- large groups with few differing members.  In a round, the members of
+// a large group are ordered by r = rank[i + h].  On repetitive texts (runs,
+// tandem repeats) almost all members of such a group carry the same r: the
+// group's copy one period on.  Then only the few others are radix-sorted and
+// the majority is placed as one run between the others below and above it,
+// which gives the same list (up to order inside runs of equal keys) that the
+// full sort of the group would.  The large list holds group L's members at
+// [lstart[L], lstart[L+1]) with keys (L << b2) | r.
+constexpr int kFewTile = 2048;               // entries per CTA (256 threads x 8)
+constexpr int kFewSpan = 64;                 // large groups a tile may aggregate in shared memory
+
+// Words of the few-others scratch: five per-group arrays (lstart, candidate,
+// below, above, others before the group) and two per-tile arrays.  Large
+// groups have more than 64 members, so there are at most n / 64 of them.
+uint64_t few_group_words(uint64_t n) { return n / 64 + 64; }
+uint64_t few_tile_words(uint64_t n) { return n / kFewTile + 64; }
+size_t few_scratch_bytes(uint64_t n) { return (size_t)(5 * few_group_words(n) + 2 * few_tile_words(n)) * 4; }
+
+// One warp per large group: the most frequent r among 32 members sampled
+// evenly over the group.
+__global__ void __launch_bounds__(256) k_large_cand(const uint64_t *__restrict__ lkeys,
+                                                    const uint32_t *__restrict__ lstart, uint64_t LG, int b2,
+                                                    uint32_t *__restrict__ cand)
+{
+    const uint64_t L = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (L >= LG) return;
+    const int lane = threadIdx.x & 31;
+    const uint64_t s = lstart[L], e = lstart[L + 1];
+    const uint64_t mask = (1ull << b2) - 1;
+    const uint32_t v = (uint32_t)(lkeys[s + (e - s) * (uint64_t)lane / 32] & mask);
+    const uint32_t peers = __match_any_sync(GSAIS_FULL_MASK, v);
+    uint32_t best = (uint32_t)__popc(peers) << 5 | (31u - (uint32_t)lane);   // ties: lowest lane
+    for (int o = 16; o > 0; o >>= 1) {
+        const uint32_t y = __shfl_xor_sync(GSAIS_FULL_MASK, best, o);
+        best = y > best ? y : best;
+    }
+    const int src = 31 - (int)(best & 31u);
+    const uint32_t c = __shfl_sync(GSAIS_FULL_MASK, v, src);
+    if (lane == 0) cand[L] = c;
+}
+
+// Per tile: the number of members that differ from their group's candidate
+// (tile_other[tile]); per group the numbers below and above it (less[L],
+// greater[L]), aggregated in shared memory over the groups a tile spans.
+// Bytes per entry: key 8 read.
+__global__ void __launch_bounds__(256) k_large_count(const uint64_t *__restrict__ lkeys, uint64_t NL, uint64_t LG,
+                                                     int b2, const uint32_t *__restrict__ cand,
+                                                     uint32_t *__restrict__ less, uint32_t *__restrict__ greater,
+                                                     uint32_t *__restrict__ tile_other, uint32_t *__restrict__ err)
+{
+    __shared__ uint32_t s_lo[kFewSpan], s_hi[kFewSpan];
+    __shared__ uint32_t s_tot;
+    const uint64_t t0 = (uint64_t)blockIdx.x * kFewTile;
+    const uint64_t mask = (1ull << b2) - 1;
+    const uint64_t L0 = lkeys[t0] >> b2;
+    if (threadIdx.x < kFewSpan) {
+        s_lo[threadIdx.x] = 0;
+        s_hi[threadIdx.x] = 0;
+    }
+    if (threadIdx.x == 0) s_tot = 0;
+    __syncthreads();
+    uint32_t mine = 0;
+    for (int k = 0; k < kFewTile / 256; ++k) {
+        const uint64_t d = t0 + (uint64_t)k * 256 + threadIdx.x;
+        if (d >= NL) break;
+        const uint64_t key = lkeys[d];
+        const uint64_t L = key >> b2;
+        if (L >= LG) {
+            atomicOr(err, GSAIS_ERR_BOUNDS);
+            continue;
+        }
+        const uint32_t r = (uint32_t)(key & mask), c = cand[L];
+        if (r == c) continue;
+        ++mine;
+        const uint64_t x = L - L0;
+        if (x < (uint64_t)kFewSpan) {
+            atomicAdd(r < c ? &s_lo[x] : &s_hi[x], 1u);
+        } else {
+            atomicAdd(r < c ? &less[L] : &greater[L], 1u);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) mine += __shfl_xor_sync(GSAIS_FULL_MASK, mine, o);
+    if ((threadIdx.x & 31) == 0 && mine) atomicAdd(&s_tot, mine);
+    __syncthreads();
+    if (threadIdx.x < kFewSpan) {
+        const uint64_t L = L0 + threadIdx.x;   // counts exist only for L < LG
+        if (s_lo[threadIdx.x]) atomicAdd(&less[L], s_lo[threadIdx.x]);
+        if (s_hi[threadIdx.x]) atomicAdd(&greater[L], s_hi[threadIdx.x]);
+    }
+    if (threadIdx.x == 0) tile_other[blockIdx.x] = s_tot;
+}
+
+// Exclusive prefix sums of count values (a[i], plus b[i] when b is given)
+// into out[0..count], out[count] = total, by one CTA.
+__global__ void __launch_bounds__(1024) k_scan_counts(const uint32_t *__restrict__ a, const uint32_t *__restrict__ b,
+                                                      uint64_t count, uint32_t *__restrict__ out)
+{
+    __shared__ uint32_t wbuf[33];
+    uint32_t run = 0;
+    const uint64_t per = (count + 1023) / 1024;
+    for (uint64_t base = 0; base < count; base += 1024 * 4) {
+        uint32_t v[4], sum = 0;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const uint64_t i = base + (uint64_t)threadIdx.x * 4 + q;
+            v[q] = i < count ? a[i] + (b ? b[i] : 0u) : 0u;
+            sum += v[q];
+        }
+        uint32_t total;
+        uint32_t x = run + block_exclusive_sum<uint32_t, 1024>(sum, wbuf, total);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const uint64_t i = base + (uint64_t)threadIdx.x * 4 + q;
+            if (i < count) out[i] = x;
+            x += v[q];
+        }
+        run += total;
+    }
+    (void)per;
+    if (threadIdx.x == 0) out[count] = run;
+}
+
+// Places the majority members of each group at lstart[L] + less[L] + their
+// index among the group's majority (list order), and appends the others, in
+// list order, to the others list at their global index.  O(d) (others before
+// d) = tile_off[tile] + the others before d inside the tile; the group's
+// others before its start = ocum[L].  Bytes per entry: key 8 + value 4 read,
+// 12 written.
+__global__ void __launch_bounds__(256) k_large_place(const uint64_t *__restrict__ lkeys,
+                                                     const uint32_t *__restrict__ lvals, uint64_t NL, uint64_t LG,
+                                                     int b2,
+                                                     const uint32_t *__restrict__ cand,
+                                                     const uint32_t *__restrict__ lstart,
+                                                     const uint32_t *__restrict__ less,
+                                                     const uint32_t *__restrict__ ocum,
+                                                     const uint32_t *__restrict__ tile_off,
+                                                     uint64_t *__restrict__ out_keys, uint32_t *__restrict__ out_vals,
+                                                     uint64_t *__restrict__ okeys, uint32_t *__restrict__ ovals,
+                                                     uint32_t *__restrict__ err)
+{
+    __shared__ uint32_t s_w[8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint64_t t0 = (uint64_t)blockIdx.x * kFewTile;
+    const uint64_t mask = (1ull << b2) - 1;
+    // warp w handles the 256 entries [t0 + 256 w, ...), eight rows of 32
+    uint64_t key[8];
+    uint32_t val[8], oth = 0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const uint64_t d = t0 + (uint64_t)warp * 256 + q * 32 + lane;
+        const bool ok = d < NL && (lkeys[d] >> b2) < LG;   // k_large_count flags keys of no large group
+        key[q] = ok ? lkeys[d] : 0ull;
+        val[q] = ok ? lvals[d] : 0u;
+        const bool o = ok && (uint32_t)(key[q] & mask) != cand[key[q] >> b2];
+        if (!ok) key[q] = ~0ull;   // marks an entry to skip
+        oth |= (uint32_t)o << q;
+    }
+    uint32_t wtot = 0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) wtot += (uint32_t)__popc(__ballot_sync(GSAIS_FULL_MASK, (oth >> q) & 1u));
+    if (lane == 0) s_w[warp] = wtot;
+    __syncthreads();
+    uint32_t before = tile_off[blockIdx.x];
+    for (int w = 0; w < warp; ++w) before += s_w[w];
+    bool bad = false;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const uint64_t d = t0 + (uint64_t)warp * 256 + q * 32 + lane;
+        const uint32_t ball = __ballot_sync(GSAIS_FULL_MASK, (oth >> q) & 1u);
+        const uint32_t Od = before + (uint32_t)__popc(ball & lanemask_lt());
+        before += (uint32_t)__popc(ball);
+        if (d >= NL || key[q] == ~0ull) continue;
+        const uint64_t L = key[q] >> b2;
+        if ((oth >> q) & 1u) {
+            okeys[Od] = key[q];
+            ovals[Od] = val[q];
+        } else {
+            const uint64_t dest = (uint64_t)less[L] + d - Od + ocum[L];
+            if (dest < lstart[L] || dest >= lstart[L + 1]) {
+                bad = true;
+                continue;
+            }
+            out_keys[dest] = key[q];
+            out_vals[dest] = val[q];
+        }
+    }
+    if (bad) atomicOr(err, GSAIS_ERR_BOUNDS);
+}
+
+// The sorted others into their groups: below the majority run when r < c,
+// above it otherwise.  Bytes per other: 12 read, 12 written.
+__global__ void __launch_bounds__(256) k_others_place(const uint64_t *__restrict__ okeys,
+                                                      const uint32_t *__restrict__ ovals, uint64_t O, int b2,
+                                                      const uint32_t *__restrict__ lstart,
+                                                      const uint32_t *__restrict__ less,
+                                                      const uint32_t *__restrict__ greater,
+                                                      const uint32_t *__restrict__ ocum, uint64_t LG,
+                                                      uint64_t *__restrict__ out_keys, uint32_t *__restrict__ out_vals,
+                                                      uint32_t *__restrict__ err)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < O; q += stride) {
+        const uint64_t key = okeys[q];
+        const uint64_t L = key >> b2;
+        if (L >= LG) {
+            atomicOr(err, GSAIS_ERR_BOUNDS);
+            continue;
+        }
+        const uint64_t s = lstart[L], size = lstart[L + 1] - s;
+        const uint64_t t = q - ocum[L];
+        const uint64_t lo = less[L], hi = greater[L];
+        const uint64_t M = size - lo - hi;
+        const uint64_t dest = s + (t < lo ? t : M + t);
+        if (t >= lo + hi || dest >= s + size) {
+            atomicOr(err, GSAIS_ERR_BOUNDS);
+            continue;
+        }
+        out_keys[dest] = key;
+        out_vals[dest] = ovals[q];
+    }
+}
+
+__global__ void k_set_word(uint32_t *__restrict__ p, uint32_t v) { *p = v; }
 
 // Bitonic sort of THREADS * R keys held R to a thread (thread t holds
 // positions t*R .. t*R+R-1), stages k <= pw only (pw a power of two; the
@@ -1623,6 +1848,7 @@ size_t sort_workspace_bytes(uint64_t n, int symbytes)
     s += 2 * align_up(8 * 256 * 4, A);             // radix hist + bases
     s += align_up(8 * 4, A);                       // radix counters
     s += align_up(radix_status_words(n) * 8, A);   // radix tile counts + offsets
+    s += align_up(few_scratch_bytes(n), A);         // large groups with few differing members
     return s;
 }
 
@@ -1660,6 +1886,8 @@ void sort_workspace_carve(SortWorkspace &ws, void *base, uint64_t n, int symbyte
     ws.radix.counters = reinterpret_cast<uint32_t *>(take(8 * 4));
     ws.radix.status_words = radix_status_words(n);
     ws.radix.status = reinterpret_cast<uint64_t *>(take(ws.radix.status_words * 8));
+    ws.few = reinterpret_cast<uint32_t *>(take(few_scratch_bytes(n)));
+    ws.n_cap = n;
     ws.radix.h_hist = h_hist;
     ws.h_small = h_small;
 }
@@ -1934,6 +2162,62 @@ static cudaError_t run_pair_compare(SortWorkspace &ws, const PairSource &ps, con
     return cudaGetLastError();
 }
 
+// The large groups of a round (NL members in LG groups, large list in
+// keys[0] / lvals[0]): if at most a quarter of the members differ from their
+// group's candidate value, sorts only those and places the majority runs,
+// leaving the sorted list in keys[1] / lvals[1] (*few = true).  The others
+// and their sort use the active list's buffers, which the round has consumed.
+static cudaError_t large_few_others(SortWorkspace &ws, uint64_t NL, uint64_t LG, int b2, int end_bit, uint64_t N,
+                                    int av, int pg, uint32_t *d_err, cudaStream_t st, SortStats &S, bool *few)
+{
+    cudaError_t e;
+    *few = false;
+    const uint64_t GW = few_group_words(ws.n_cap), TW = few_tile_words(ws.n_cap);
+    // the others and their sort live in halves of the active list's buffers
+    if (LG + 1 > GW || N < 4096) return cudaSuccess;
+    uint32_t *lstart = ws.few, *cand = lstart + GW, *less = cand + GW, *greater = less + GW, *ocum = greater + GW;
+    uint32_t *tile_other = ocum + GW, *tile_off = tile_other + TW;
+    const uint64_t ftiles = (NL + kFewTile - 1) / kFewTile;
+    if (ftiles + 1 > TW) return cudaSuccess;
+    KernelProfiler *prof = ws.radix.prof;
+    cudaEvent_t ev = prof ? prof->begin(st) : nullptr;
+    GSAIS_COUNTED((k_set_word<<<1, 1, 0, st>>>(lstart + LG, (uint32_t)NL)));
+    if ((e = cudaMemsetAsync(less, 0, LG * 4, st)) != cudaSuccess ||
+        (e = cudaMemsetAsync(greater, 0, LG * 4, st)) != cudaSuccess)
+        return e;
+    GSAIS_COUNTED((k_large_cand<<<(unsigned)((LG * 32 + 255) / 256), 256, 0, st>>>(ws.keys[0], lstart, LG, b2, cand)));
+    GSAIS_COUNTED((k_large_count<<<(unsigned)ftiles, 256, 0, st>>>(ws.keys[0], NL, LG, b2, cand, less, greater,
+                                                                  tile_other, d_err)));
+    GSAIS_COUNTED((k_scan_counts<<<1, 1024, 0, st>>>(tile_other, nullptr, ftiles, tile_off)));
+    if ((e = read_back(ws.h_small, tile_off + ftiles, 4, st)) != cudaSuccess) return e;
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+    const uint64_t O = ws.h_small[0];
+    if (ev) prof->end(KK_FEW, ev, st, NL * 8);
+    if (O > NL / 4) return cudaSuccess;
+    *few = true;
+    ev = prof ? prof->begin(st) : nullptr;
+    GSAIS_COUNTED((k_scan_counts<<<1, 1024, 0, st>>>(less, greater, LG, ocum)));
+    const uint64_t half = (N / 2 + 63) & ~63ull;
+    uint64_t *ok[2] = {reinterpret_cast<uint64_t *>(ws.pos[pg]), reinterpret_cast<uint64_t *>(ws.gid[pg])};
+    uint32_t *ov[2] = {ws.vals[av], ws.vals[av] + half};
+    GSAIS_COUNTED((k_large_place<<<(unsigned)ftiles, 256, 0, st>>>(ws.keys[0], ws.lvals[0], NL, LG, b2, cand, lstart,
+                                                                  less,
+                                                                  ocum, tile_off, ws.keys[1], ws.lvals[1], ok[0],
+                                                                  ov[0], d_err)));
+    if (ev) prof->end(KK_FEW, ev, st, NL * 24);
+    if (O > 0) {
+        int which = 0, ran = 0;
+        if ((e = radix_sort_pairs(ok, ov, O, end_bit, ws.radix, d_err, st, &which, &ran, false)) != cudaSuccess)
+            return e;
+        S.radix_passes += ran;
+        GSAIS_COUNTED((k_others_place<<<stream_grid(O, 256), 256, 0, st>>>(ok[which], ov[which], O, b2, lstart, less,
+                                                                          greater, ocum, LG, ws.keys[1], ws.lvals[1],
+                                                                          d_err)));
+    }
+    S.few_rounds += 1;
+    return cudaGetLastError();
+}
+
 static cudaError_t run_rounds(SortWorkspace &ws, uint64_t nr, int K, uint32_t kept, uint32_t groups, int av, int pg,
                               uint32_t *d_err, cudaStream_t st, SortStats &S, const PairSource &ps, const Tuning &tn)
 {
@@ -1968,7 +2252,8 @@ static cudaError_t run_rounds(SortWorkspace &ws, uint64_t nr, int K, uint32_t ke
         cudaEvent_t ev_cl = ws.radix.prof ? ws.radix.prof->begin(st) : nullptr;
         GSAIS_COUNTED((k_classify<<<stream_grid(G, 256), 256, 0, st>>>(ws.gstart[pg], G, N, ws.lid, ws.loff,
                                                                       ws.counters + 1, mlist, ws.counters + 2, mlist2,
-                                                                      ws.counters + 5, medium_small, medium_max)));
+                                                                      ws.counters + 5, medium_small, medium_max,
+                                                                      ws.few)));
         if (ev_cl) ws.radix.prof->end(KK_CLASSIFY, ev_cl, st, G * 12);   // group table 8 read, class 4 written
         cudaEvent_t ev_rk = ws.radix.prof ? ws.radix.prof->begin(st) : nullptr;
         GSAIS_COUNTED((k_round_r2<<<stream_grid(N, 256), 256, 0, st>>>(
@@ -2014,17 +2299,34 @@ static cudaError_t run_rounds(SortWorkspace &ws, uint64_t nr, int K, uint32_t ke
             kept = (uint32_t)small_tot;
             groups = (uint32_t)(small_tot >> 32);
         } else {
-            uint64_t *kk[2] = {ws.keys[0], ws.keys[1]};
-            uint32_t *vv[2] = {ws.lvals[0], ws.lvals[1]};
-            int which = 0;
-            if ((e = radix_sort_pairs(kk, vv, NL, end_bit, ws.radix, d_err, st, &which, &ran, true)) != cudaSuccess)
-                return e;
-            S.radix_passes += ran;
+            const uint64_t LG = large_tot >> 32;
+            const uint64_t* sorted_keys = nullptr;
+            const uint32_t* sorted_vals = nullptr;
+            bool few = false;
+            if (tn.large_few_others && LG > 0) {
+                if ((e = large_few_others(ws, NL, LG, b2, end_bit, N, av, pg, d_err, st, S, &few)) != cudaSuccess)
+                    return e;
+                if (few) {
+                    sorted_keys = ws.keys[1];
+                    sorted_vals = ws.lvals[1];
+                }
+            }
+            if (!few) {
+                uint64_t *kk[2] = {ws.keys[0], ws.keys[1]};
+                uint32_t *vv[2] = {ws.lvals[0], ws.lvals[1]};
+                int which = 0;
+                if ((e = radix_sort_pairs(kk, vv, NL, end_bit, ws.radix, d_err, st, &which, &ran, true)) !=
+                    cudaSuccess)
+                    return e;
+                S.radix_passes += ran;
+                sorted_keys = kk[which];
+                sorted_vals = vv[which];
+            }
             S.large_total += NL;
             TileArgs r;
-            r.keys = kk[which];
+            r.keys = sorted_keys;
             r.keys32 = nullptr;
-            r.vals = vv[which];
+            r.vals = sorted_vals;
             r.pos = ws.lpos;
             r.rank_out = nullptr;
             r.pairs = nullptr;

@@ -33,6 +33,8 @@ struct SortWorkspace {
     uint8_t *packed = nullptr;               // text as packed codes when they fit 2 or 4 bits
     int pack_bits = 0;                       // 0 (not packed), 2 or 4
     uint16_t decode[16] = {0};               // symbol of each code when packed
+    uint32_t *few = nullptr;                 // scratch of the large groups with few differing members
+    uint64_t n_cap = 0;                      // symbols the workspace was carved for
     RadixScratch radix;
     uint32_t *h_small = nullptr;             // pinned host scratch (kHostSmallWords words)
 };

@@ -3,9 +3,10 @@
 //
 // A tuning names, for one sort, the radix digit width, the keys per thread of
 // a digit pass for 32- and 64-bit keys (the tile is 256 threads x that many
-// keys), and the group sizes at which the doubling rounds switch from the
+// keys), the group sizes at which the doubling rounds switch from the
 // 128-thread CTA sort to the 256-thread CTA sort (medium_small) and from
-// there to the global segmented radix sort (medium_max).  The cache is a JSON
+// there to the global segmented radix sort (medium_max), and whether large
+// groups whose members mostly share rank[i+h] sort only the others.  The cache is a JSON
 // file of entries keyed by (GPU name, n bucket = ceil(log2 n), code bits of the
 // alphabet); a sort without an explicit tuning takes the entry for its GPU
 // and code bits with the nearest n bucket, else the built-in defaults.
@@ -126,6 +127,7 @@ bool parse_entry(Reader &r, CacheEntry &ce)
         else if (key == "radix_items64") ce.t.radix_items64 = v;
         else if (key == "medium_small") ce.t.medium_small = v;
         else if (key == "medium_max") ce.t.medium_max = v;
+        else if (key == "large_few_others") ce.t.large_few_others = v;
         if (r.lit(',')) continue;
         return r.lit('}');
     }
@@ -190,7 +192,8 @@ bool tuning_valid(const Tuning &t)
 {
     return t.digit_bits == 8 && radix_items_supported(4, t.radix_items32) &&
            radix_items_supported(8, t.radix_items64) && t.medium_small >= 64 && t.medium_small <= 512 &&
-           t.medium_max >= t.medium_small && t.medium_max <= 4096;
+           t.medium_max >= t.medium_small && t.medium_max <= 4096 &&
+           (t.large_few_others == 0 || t.large_few_others == 1);
 }
 
 Tuning tuning_lookup(uint64_t n, int bits)

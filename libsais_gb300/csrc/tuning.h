@@ -10,6 +10,7 @@ struct Tuning {
     int radix_items64 = 16;    // the same for 64-bit keys: 12, 16, 20
     int medium_small = 512;    // groups of 33..medium_small members: 128-thread CTA sort
     int medium_max = 4096;     // groups up to medium_max: 256-thread CTA sort; larger: global radix sort
+    int large_few_others = 1;  // large groups whose members mostly share rank[i+h]: sort only the others
 };
 
 bool tuning_valid(const Tuning &t);
