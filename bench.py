@@ -228,9 +228,62 @@ def port_step(T: np.ndarray):
     return time.perf_counter() - t0
 
 
+def serving_cpu_reference(sample_jobs: int, jobs_per_rate: int, seed: int = 6):
+    """The serving stream's host aggregate: the reference libsais (OpenMP, all
+    host threads) on a seeded sample of the stream's jobs, one after another:
+    SA + BWT per job (libsais_omp + libsais_bwt_omp, the 16-bit jobs through
+    libsais16_omp + libsais16_bwt_omp)."""
+    import ctypes
+    from libsais_gb300 import textgen
+    from oracle.oracle import ORACLE_SO, Reference, build
+    if not os.path.exists(ORACLE_SO):
+        build(with_reference=False)
+    textgen.set_library(ORACLE_SO)
+    try:
+        jobs = make_serving_jobs(jobs_per_rate, seed)
+    finally:
+        textgen.set_library(None)
+    lib = Reference().lib
+    p_, i32 = ctypes.c_void_p, ctypes.c_int32
+    for name in ("libsais16_omp",):
+        getattr(lib, name).argtypes = [p_, p_, i32, i32, p_, i32]
+        getattr(lib, name).restype = i32
+    lib.libsais16_bwt_omp.argtypes = [p_, p_, p_, i32, i32, p_, i32]
+    lib.libsais16_bwt_omp.restype = i32
+    threads = host_threads()
+    sample = serving_sample(jobs_per_rate, sample_jobs, seed + 1)
+    total, secs = 0, 0.0
+    for k in sample:
+        t = np.ascontiguousarray(jobs[k])
+        n = t.size
+        SA = np.zeros(n, dtype=np.int32)
+        A = np.zeros(n, dtype=np.int32)
+        U = np.zeros(n, dtype=t.dtype)
+        freq = np.zeros(65536, dtype=np.int32)
+        t0 = time.perf_counter()
+        if t.dtype == np.uint16:
+            rc = lib.libsais16_omp(t.ctypes.data, SA.ctypes.data, n, 0, freq.ctypes.data, threads)
+            prim = lib.libsais16_bwt_omp(t.ctypes.data, U.ctypes.data, A.ctypes.data, n, 0, freq.ctypes.data, threads)
+        else:
+            rc = lib.libsais_omp(t.ctypes.data, SA.ctypes.data, n, 0, freq.ctypes.data, threads)
+            prim = lib.libsais_bwt_omp(t.ctypes.data, U.ctypes.data, A.ctypes.data, n, 0, freq.ctypes.data, threads)
+        secs += time.perf_counter() - t0
+        if rc != 0 or prim < 0:
+            raise SystemExit(f"reference failed on serving job {k}")
+        total += n
+    return {"mb_s": round(total / 1e6 / secs, 2), "jobs": int(sample.size), "input_mb": round(total / 1e6, 1),
+            "threads": threads, "kind": "reference",
+            "sample": "seeded sample of the stream's jobs (seed + 101), one after another"}
+
+
 def run_reference(args, rank):
     """The reference arm: libsais built with OpenMP, on the host cores."""
     if rank != 0:
+        return
+    if args.serving_cpu:
+        os.environ.setdefault("OMP_PROC_BIND", "close")
+        os.environ.setdefault("OMP_DYNAMIC", "false")
+        print(json.dumps({"serving_cpu": serving_cpu_reference(args.serving_cpu, args.serving_jobs)}), flush=True)
         return
     name = args.workload
     n = args.n or WORKLOADS[name][1]
@@ -287,6 +340,17 @@ def _ref_version() -> str:
             return f.read().strip()
     except OSError:
         return "?"
+
+
+def serving_cpu_child(sample_jobs: int, jobs_per_rate: int):
+    env = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK")}
+    cmd = [sys.executable, os.path.abspath(__file__), "--impl", "reference", "--serving-cpu", str(sample_jobs),
+           "--serving-jobs", str(jobs_per_rate)]
+    r = subprocess.run(cmd, capture_output=True, text=True, env=env)
+    for ln in reversed(r.stdout.splitlines()):
+        if ln.startswith("{"):
+            return json.loads(ln)["serving_cpu"]
+    return {"mb_s": None, "note": "child failed: " + (r.stderr.strip().splitlines() or ["?"])[-1][:160]}
 
 
 def cpu_baseline_child(name: str, n: int):
@@ -389,98 +453,174 @@ def run_batched(G, torch, count: int = 4096, steps: int = 3, warmup: int = 1, cp
             "cpu_port_mb_s": round(cpu_n / 1e6 / cpu_s, 2), "cpu_sample": f"first {cpu_strings} strings, 1 thread"}
 
 
-def _job_hash(res, SA, U) -> int:
-    """64-bit wrapping checksum of one job's outputs (compare two paths bit for bit)."""
-    m = np.uint64(0x9E3779B97F4A7C15)
-    with np.errstate(over="ignore"):
-        h = int((SA.astype(np.uint64) * m).sum(dtype=np.uint64))
-        h ^= int((U.astype(np.uint64) * np.uint64(1099511628211)).sum(dtype=np.uint64)) << 1
-    return (h ^ (int(res) & 0xFFFFFFFFFFFFFFFF)) & 0xFFFFFFFFFFFFFFFF
+SERVING_RATES = (100, 300, 1000, 3000, 5000)
 
 
-def make_serving_jobs(count: int, seed: int = 6):
+def make_serving_jobs(count: int, seed: int = 6, pools=None):
     """The serving stream's jobs: lengths log-uniform over 4 KiB - 64 MiB; 70% order-2
     Markov ACGT uint8, 20% uniform 0-255 uint8, 10% uint16 Zipf(1.1) over 1..65535.
-    Texts are seeded slices of three seeded pools (so generation stays fast)."""
+    Texts are seeded slices of three seeded pools (so generation stays fast);
+    `pools` = (dna, bytes, zipf) arrays to slice (e.g. pinned copies)."""
     from libsais_gb300 import textgen
     u = textgen.uniform(3 * count, seed)
     lens = textgen.loguniform_lengths(count, 4096, 64 << 20, seed + 1)
-    dna = textgen.markov2_dna(1 << 29, seed=seed + 2)
-    byt = np.frombuffer(np.random.default_rng(seed + 3).bytes(1 << 27), dtype=np.uint8)
-    zipf = textgen.zipf_u16(1 << 26, seed=seed + 4)
+    if pools is None:
+        pools = serving_pools(seed)
+    dna, byt, zipf = pools
     jobs = []
     for k in range(count):
         n = int(lens[k])
-        if u[3 * k] < 0.7:
-            pool = dna
-        elif u[3 * k] < 0.9:
-            pool = byt
-        else:
-            pool = zipf
+        pool = dna if u[3 * k] < 0.7 else (byt if u[3 * k] < 0.9 else zipf)
         n = min(n, pool.size)
         a = int(u[3 * k + 1] * (pool.size - n))
         jobs.append(pool[a:a + n])
     return jobs
 
 
-def run_serving(G, rates=(100, 1000, 5000), max_jobs: int = 600, seconds: float = 4.0, seed: int = 6,
-                budget: int = 120 << 30, workers: int = 3, oracle_jobs: int = 12):
-    """Continuous-batching server vs the plain one-job-at-a-time GPU path.  The
-    first `oracle_jobs` jobs of at most 8 Mi symbols of each rate are checked
-    against the oracle; every job is compared with the single-job path."""
+def serving_pools(seed: int = 6):
+    from libsais_gb300 import textgen
+    dna = textgen.markov2_dna(1 << 29, seed=seed + 2)
+    byt = np.frombuffer(np.random.default_rng(seed + 3).bytes(1 << 27), dtype=np.uint8)
+    zipf = textgen.zipf_u16(1 << 26, seed=seed + 4)
+    return dna, byt, zipf
+
+
+def serving_sample(count: int, size: int, seed: int = 6):
+    """A seeded sample of job indexes of the stream (for the one-job-at-a-time
+    GPU path and the host reference, which cannot run the whole stream)."""
+    rng = np.random.default_rng(seed + 100)
+    return np.sort(rng.choice(count, size=min(size, count), replace=False))
+
+
+class OutputRing:
+    """Pinned host memory for job outputs, taken and given back in submission
+    order; take() blocks while the ring is full (the client's backpressure)."""
+
+    def __init__(self, torch, nbytes: int):
+        self.buf = torch.empty(nbytes, dtype=torch.uint8).pin_memory().numpy()
+        self.n = nbytes
+        self.head = 0       # next free byte (monotone)
+        self.tail = 0       # oldest byte still in use (monotone)
+        self.cv = threading.Condition()
+
+    def take(self, nbytes: int):
+        nbytes = (nbytes + 255) & ~255
+        if nbytes > self.n:
+            raise ValueError("job larger than the output ring")
+        with self.cv:
+            while True:
+                start = self.head
+                off = start % self.n
+                if off + nbytes > self.n:   # wrap: skip the ring's tail end
+                    start += self.n - off
+                    off = 0
+                if start + nbytes - self.tail <= self.n:
+                    self.head = start + nbytes
+                    return start, off, nbytes
+                self.cv.wait()
+
+    def give(self, start: int, nbytes: int):
+        with self.cv:
+            self.tail = start + nbytes
+            self.cv.notify_all()
+
+    def views(self, off: int, n: int, dtype):
+        SA = self.buf[off:off + 4 * n].view(np.int32)
+        isz = np.dtype(dtype).itemsize
+        o2 = off + ((4 * n + 255) & ~255)
+        U = self.buf[o2:o2 + isz * n].view(dtype)
+        return SA, U
+
+    @staticmethod
+    def bytes_for(n: int, itemsize: int) -> int:
+        return ((4 * n + 255) & ~255) + itemsize * n
+
+
+def run_serving(G, torch, rates=SERVING_RATES, jobs_per_rate: int = 20000, seed: int = 6, budget: int = 120 << 30,
+                workers: int = 3, oracle_jobs: int = 8, plain_sample: int = 300, ring_bytes: int = 8 << 30):
+    """The serving stream: `jobs_per_rate` SA+BWT jobs with Poisson arrivals at
+    each rate, open loop (latency is measured from each job's scheduled arrival,
+    so time spent waiting for output space or for the server counts), under
+    an HBM budget, with small jobs coalesced.  Job texts are slices of pinned
+    pools and outputs land in a pinned ring.  Checked: the first `oracle_jobs`
+    jobs of at most 4 Mi symbols of each rate against the oracle.  Beside it:
+    the plain one-job-at-a-time GPU path on a seeded sample of the stream."""
+    from libsais_gb300 import textgen
     from oracle.oracle import Oracle
     O = Oracle()
-    jobs_all = make_serving_jobs(max_jobs, seed)
-    out = {"budget_bytes": budget, "workers": workers, "rates": []}
-    from libsais_gb300 import textgen
+    pools = tuple(torch.from_numpy(np.ascontiguousarray(p)).pin_memory().numpy() if p.dtype != np.uint16 else
+                  torch.from_numpy(p.view(np.int16)).pin_memory().numpy().view(np.uint16) for p in serving_pools(seed))
+    jobs = make_serving_jobs(jobs_per_rate, seed, pools)
+    sym = int(sum(t.size for t in jobs))
+    ring = OutputRing(torch, ring_bytes)
+    out = {"jobs_per_rate": jobs_per_rate, "input_mb_per_rate": round(sym / 1e6, 1), "budget_bytes": budget,
+           "workers": workers, "footprint_bytes_per_symbol": 80.0, "rates": []}
     for rate in rates:
-        count = int(min(max_jobs, max(50, rate * seconds)))
-        jobs = jobs_all[:count]
-        arrivals = textgen.poisson_arrivals(count, float(rate), seed + 10 + rate)
+        arrivals = textgen.poisson_arrivals(jobs_per_rate, float(rate), seed + 10 + rate)
         srv = G.Server(hbm_budget_bytes=budget, workers=workers, small_job_symbols=1 << 20, max_batch=256)
-        ids, hashes, lat, queued = [], [], [], []
-        check = set(int(k) for k in np.flatnonzero([t.size <= (8 << 20) for t in jobs])[:oracle_jobs])
-        checked = []
+        lat = np.zeros(jobs_per_rate)
+        check = [k for k in range(jobs_per_rate) if jobs[k].size <= (4 << 20)][:oracle_jobs]
+        checked = {}
+        ids = [0] * jobs_per_rate
+        slots = [None] * jobs_per_rate
+        delay = np.zeros(jobs_per_rate)
+        submitted = threading.Semaphore(0)
+        fails = []
+
+        def waiter():
+            for k in range(jobs_per_rate):
+                submitted.acquire()
+                res, SA, U, q, total, b = srv.wait(ids[k])
+                lat[k] = delay[k] + total
+                if res < 0:
+                    fails.append((k, res))
+                if k in check:
+                    checked[k] = (res, SA.copy(), U.copy())
+                ring.give(slots[k][0], slots[k][2])
+
+        th = threading.Thread(target=waiter, daemon=True)
+        th.start()
         t0 = time.perf_counter()
         for k, t in enumerate(jobs):
-            delay = arrivals[k] - (time.perf_counter() - t0)
-            if delay > 0:
-                time.sleep(delay)
-            ids.append(srv.submit(t))
-        for k, jid in enumerate(ids):
-            res, SA, U, q, total, b = srv.wait(jid)
-            hashes.append(_job_hash(res, SA, U))
-            lat.append(total)
-            queued.append(q)
-            if k in check:
-                checked.append((k, res, SA, U))
+            wait_s = arrivals[k] - (time.perf_counter() - t0)
+            if wait_s > 0:
+                time.sleep(wait_s)
+            slots[k] = ring.take(OutputRing.bytes_for(t.size, t.itemsize))
+            SA, U = ring.views(slots[k][1], t.size, t.dtype)
+            delay[k] = (time.perf_counter() - t0) - arrivals[k]
+            ids[k] = srv.submit_into(t, SA, U)
+            submitted.release()
+        th.join()
+        wall = time.perf_counter() - t0
         st = srv.stats()
         srv.close()
-        sym = int(sum(t.size for t in jobs))
-        lat_ms = np.array(lat) * 1e3
-        # plain path: one job at a time through the host C-ABI, same outputs expected
-        lib = G.load()
-        same = True
-        t1 = time.perf_counter()
-        for k, t in enumerate(jobs):
-            SA = np.empty(t.size, dtype=np.int32)
-            U = np.empty_like(t)
-            res = lib.gsais_sa_bwt(None, t.ctypes.data, t.itemsize, t.size, SA.ctypes.data, 4, U.ctypes.data,
-                                   None, 4)
-            same &= _job_hash(res, SA, U) == hashes[k]
-        plain_s = time.perf_counter() - t1
-        oracle_ok = all(oracle_check_sa_bwt(O, jobs[k], SA, U, res) for k, res, SA, U in checked)
+        ok = not fails and all(oracle_check_sa_bwt(O, jobs[k], SA, U, res) for k, (res, SA, U) in checked.items())
+        lat_ms = lat * 1e3
         out["rates"].append({
-            "rate_per_s": rate, "jobs": count, "input_mb": round(sym / 1e6, 1),
+            "rate_per_s": rate, "jobs": jobs_per_rate, "wall_s": round(wall, 2),
             "p50_ms": round(float(np.percentile(lat_ms, 50)), 2), "p95_ms": round(float(np.percentile(lat_ms, 95)), 2),
             "p99_ms": round(float(np.percentile(lat_ms, 99)), 2),
-            "served_mb_s": round(sym / 1e6 / st["busy_seconds"], 1),
-            "plain_one_job_at_a_time_mb_s": round(sym / 1e6 / plain_s, 1),
+            "served_mb_s": round(sym / 1e6 / st["busy_seconds"], 1) if st["busy_seconds"] else None,
             "coalesced_batches": st["batches"], "coalesced_jobs": st["batched_jobs"],
             "hbm_high_water_gb": round(st["hbm_high_water_bytes"] / 1e9, 2), "rejected": st["rejected"],
-            "identical_to_single_job_path": bool(same), "oracle_checked_jobs": len(checked),
-            "oracle_ok": bool(oracle_ok)})
-    out["footprint_bytes_per_symbol"] = 80.0
+            "failed": len(fails), "oracle_checked_jobs": len(checked), "oracle_ok": bool(ok)})
+    # the plain path: one job at a time through the host C-ABI, pinned buffers, on a sample
+    lib = G.load()
+    sample = serving_sample(jobs_per_rate, plain_sample, seed)
+    s_sym = int(sum(jobs[k].size for k in sample))
+    t1 = time.perf_counter()
+    for k in sample:
+        t = jobs[k]
+        start, off, nb = ring.take(OutputRing.bytes_for(t.size, t.itemsize))
+        SA, U = ring.views(off, t.size, t.dtype)
+        res = lib.gsais_sa_bwt(None, t.ctypes.data, t.itemsize, t.size, SA.ctypes.data, 4, U.ctypes.data, None, 4)
+        ring.give(start, nb)
+        if res < 0:
+            raise SystemExit(f"plain path failed on job {k}: {res}")
+    plain_s = time.perf_counter() - t1
+    out["plain_one_job_at_a_time"] = {"mb_s": round(s_sym / 1e6 / plain_s, 1), "jobs": int(sample.size),
+                                      "input_mb": round(s_sym / 1e6, 1),
+                                      "sample": "seeded sample of the stream's jobs (seed + 100)"}
     return out
 
 
@@ -635,6 +775,8 @@ def main():
     ap.add_argument("--no-extras", action="store_true", help="skip the measurements beside the headline")
     ap.add_argument("--batch-strings", type=int, default=4096)
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (built-in tuning defaults)")
+    ap.add_argument("--serving-jobs", type=int, default=20000, help="jobs per arrival rate of the serving stream")
+    ap.add_argument("--serving-cpu", type=int, default=0, help=argparse.SUPPRESS)
     args = ap.parse_args()
     if args.baseline_child:
         args.steps, args.warmup = 1, 1
@@ -807,7 +949,8 @@ def main():
         extras["batched"] = run_batched(G, torch, count=args.batch_strings)
         G.release_workspace()
         torch.cuda.empty_cache()
-        extras["serving"] = run_serving(G)
+        extras["serving"] = run_serving(G, torch, jobs_per_rate=args.serving_jobs)
+        extras["serving"]["cpu_reference"] = serving_cpu_child(40, args.serving_jobs)
 
     if rank == 0:
         line = {

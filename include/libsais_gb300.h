@@ -80,6 +80,13 @@ extern "C" {
     int64_t gsais_batch_sa_bwt_device(void * ctx, const void * T, int64_t n, const int64_t * offsets, int32_t count, int32_t * SA, uint8_t * U, int32_t * primary, void * stream);
 
     /**
+    * gsais_batch_sa_bwt_device for strings of 8- or 16-bit symbols (symbytes 1 or 2; U has
+    * the same symbol width as T).  Each string's SA and BWT equal libsais/libsais16 and
+    * libsais_bwt/libsais16_bwt on it alone (src/libsais16.c:6995, :7074).
+    */
+    int64_t gsais_batch_sa_bwt_sym_device(void * ctx, const void * T, int32_t symbytes, int64_t n, const int64_t * offsets, int32_t count, int32_t * SA, void * U, int32_t * primary, void * stream);
+
+    /**
     * SA+BWT request loop with continuous batching.  `workers` host threads each own a
     * CUDA stream and device workspace, so jobs taken by different workers overlap on
     * the GPU; a free worker takes the oldest queued job and, if it is a small 8-bit job

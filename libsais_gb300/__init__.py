@@ -162,6 +162,7 @@ _SIGS = {
     "gsais_test_fail_allocations": (_i32, [_i32]),
     "gsais_batch_sa_bwt": (_i64, [_p, _p, _p, _i32, _p, _p, _p]),
     "gsais_batch_sa_bwt_device": (_i64, [_p, _p, _i64, _p, _i32, _p, _p, _p, _p]),
+    "gsais_batch_sa_bwt_sym_device": (_i64, [_p, _p, _i32, _i64, _p, _i32, _p, _p, _p, _p]),
     "gsais_server_create": (_p, [_i64, _i32, _i64, _i32]),
     "gsais_server_submit": (_i64, [_p, _p, _i32, _i64, _p, _p]),
     "gsais_server_wait": (_i32, [_p, _i64, _p, _p, _p, _p]),
@@ -616,6 +617,16 @@ def batch_sa_bwt_device(T, offsets, SA, U, primary, ctx=None, stream=None):
                                              primary.data_ptr(), _stream_handle(stream)))
 
 
+def batch_sa_bwt_sym_device(T, offsets, SA, U, primary, symbytes=1, ctx=None, stream=None):
+    """gsais_batch_sa_bwt_sym_device: T and U hold 8-bit (symbytes 1, uint8 tensors) or
+    16-bit symbols (symbytes 2, int16 tensors viewed as uint16)."""
+    lib = load()
+    count = offsets.numel() - 1
+    return int(lib.gsais_batch_sa_bwt_sym_device(ctx.handle if ctx else None, T.data_ptr(), symbytes, T.numel(),
+                                                 offsets.data_ptr(), count, SA.data_ptr(), U.data_ptr(),
+                                                 primary.data_ptr(), _stream_handle(stream)))
+
+
 def release_workspace(ctx=None) -> None:
     """Free the device workspace cached by a context (the process-wide one by default)."""
     load().gsais_release_workspace(ctx.handle if ctx else None)
@@ -647,6 +658,18 @@ class Server:
         jid = int(self.lib.gsais_server_submit(self.handle, _ptr(T), T.itemsize, n, _ptr(SA), _ptr(U)))
         if jid > 0:
             self._keep[jid] = (T, SA, U)
+        return jid
+
+    def submit_into(self, T, SA, U):
+        """Submits T with caller-owned output arrays (SA int32 and U of T's dtype,
+        at least T.size long; pinned host memory lets the copies run as DMA)."""
+        T = _text(T)
+        n = T.size
+        if SA.dtype != np.int32 or SA.size < n or U.dtype != T.dtype or U.size < n:
+            raise ValueError("SA must be int32 and U of the text's dtype, each at least n long")
+        jid = int(self.lib.gsais_server_submit(self.handle, _ptr(T), T.itemsize, n, _ptr(SA), _ptr(U)))
+        if jid > 0:
+            self._keep[jid] = (T, SA[:n], U[:n])
         return jid
 
     def wait(self, jid: int):

@@ -741,35 +741,95 @@ int64_t gsais_sa_bwt(void *ctx, const void *T, int32_t symbytes, int64_t n, void
     return gsais_run_bwt(c, T, symbytes, n, U, freq, freq_bytes, 0, nullptr, 4, SA, sa_bytes);
 }
 
-static int64_t batch_run(gsais_ctx *c, const uint8_t *d_T, int64_t n_, const uint64_t *d_offs, int32_t count,
-                         int32_t *d_SA, uint8_t *d_U, int32_t *d_primary, cudaStream_t st, size_t extra_front)
+static int64_t batch_run(gsais_ctx *c, const void *d_T, int symbytes, int64_t n_, const uint64_t *d_offs,
+                         int32_t count, int32_t *d_SA, void *d_U, int32_t *d_primary, cudaStream_t st,
+                         size_t extra_front)
 {
     const uint64_t n = (uint64_t)n_;
     SortWorkspace ws;
     Carver cv(static_cast<char *>(c->arena) + extra_front);
-    sort_workspace_carve(ws, cv.p, n + (uint64_t)count, 1, c->h_small, c->h_hist);
+    sort_workspace_carve(ws, cv.p, n + (uint64_t)count, symbytes, c->h_small, c->h_hist);
     ws.radix.prof = &c->prof;
     if (!clear_err(c, st)) return fail(cudaErrorUnknown);
-    GS_TRY(batch_suffix_sort(d_T, n, d_offs, (uint32_t)count, ws, c->d_misc, st, &c->stats,
+    GS_TRY(batch_suffix_sort(d_T, symbytes, n, d_offs, (uint32_t)count, ws, c->d_misc, st, &c->stats,
                              c->opt.tuning_set ? &c->opt.tuning : nullptr));
-    GS_TRY(batch_outputs(ws, d_T, n, d_offs, (uint32_t)count, d_SA, d_U, d_primary, c->d_misc, st));
+    GS_TRY(batch_outputs(ws, d_T, symbytes, n, d_offs, (uint32_t)count, d_SA, d_U, d_primary, c->d_misc, st));
     GS_TRY(sync_checked(c, st));
     return 0;
 }
 
-int64_t gsais_batch_sa_bwt_device(void *ctx, const void *T, int64_t n, const int64_t *offsets, int32_t count,
-                                  int32_t *SA, uint8_t *U, int32_t *primary, void *stream)
+int64_t gsais_batch_sa_bwt_sym_device(void *ctx, const void *T, int32_t symbytes, int64_t n, const int64_t *offsets,
+                                      int32_t count, int32_t *SA, void *U, int32_t *primary, void *stream)
 {
     gsais_ctx *c = resolve(ctx);
-    if (!c || !T || !offsets || !SA || !U || !primary || n < 0 || count <= 0) return -1;
+    if (!c || !T || !offsets || !SA || !U || !primary || n < 0 || count <= 0 || (symbytes != 1 && symbytes != 2))
+        return -1;
     std::lock_guard<std::mutex> lock(c->mu);
     if ((uint64_t)n + (uint64_t)count > kMaxN) return -2;
     if (!ctx_init(c)) return fail(cudaErrorUnknown);
     DeviceGuard g(c->device);
     cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : c->stream;
     if (!ensure_arena(c, batch_workspace_bytes((uint64_t)n, (uint32_t)count))) return -2;
-    return batch_run(c, static_cast<const uint8_t *>(T), n, reinterpret_cast<const uint64_t *>(offsets), count, SA,
-                     U, primary, st, 0);
+    return batch_run(c, T, symbytes, n, reinterpret_cast<const uint64_t *>(offsets), count, SA, U, primary, st, 0);
+}
+
+int64_t gsais_batch_sa_bwt_device(void *ctx, const void *T, int64_t n, const int64_t *offsets, int32_t count,
+                                  int32_t *SA, uint8_t *U, int32_t *primary, void *stream)
+{
+    return gsais_batch_sa_bwt_sym_device(ctx, T, 1, n, offsets, count, SA, U, primary, stream);
+}
+
+int64_t gsais_batch_jobs(gsais_ctx *c, int32_t symbytes, int32_t count, const void *const *T, const int64_t *n,
+                         int32_t *const *SA, void *const *U, int64_t *result)
+{
+    if (!c || !T || !n || !SA || !U || !result || count <= 0 || (symbytes != 1 && symbytes != 2)) return -1;
+    uint64_t total = 0;
+    for (int32_t k = 0; k < count; ++k) {
+        if (!T[k] || !SA[k] || !U[k] || n[k] < 1) return -1;
+        total += (uint64_t)n[k];
+    }
+    std::lock_guard<std::mutex> lock(c->mu);
+    if (total + (uint64_t)count > kMaxN) return -2;
+    if (!ctx_init(c)) return fail(cudaErrorUnknown);
+    DeviceGuard g(c->device);
+    cudaStream_t st = c->stream;
+    const size_t sb = (size_t)symbytes;
+    const size_t front = align_up(total * sb) + align_up((size_t)(count + 1) * 8) + align_up(total * 4) +
+                         align_up(total * sb) + align_up((size_t)count * 4);
+    if (!ensure_arena(c, front + batch_workspace_bytes(total, (uint32_t)count))) return -2;
+    Carver cv(c->arena);
+    uint8_t *d_T = cv.take<uint8_t>(total * sb);
+    uint64_t *d_offs = cv.take<uint64_t>(count + 1);
+    int32_t *d_SA = cv.take<int32_t>(total);
+    uint8_t *d_U = cv.take<uint8_t>(total * sb);
+    int32_t *d_P = cv.take<int32_t>(count);
+    // offsets and primary indexes through the pinned scratch (at most 32000 jobs)
+    if ((size_t)(count + 1) * 2 + 2 + (size_t)count > kSmallWords - 16) return -1;
+    uint64_t *h_offs = reinterpret_cast<uint64_t *>(c->h_small + 16);
+    h_offs[0] = 0;
+    for (int32_t k = 0; k < count; ++k) h_offs[k + 1] = h_offs[k] + (uint64_t)n[k];
+    // one copy per job straight from its buffer (DMA when the buffer is pinned)
+    for (int32_t k = 0; k < count; ++k)
+        GS_TRY(cudaMemcpyAsync(d_T + h_offs[k] * sb, T[k], (size_t)n[k] * sb, cudaMemcpyHostToDevice, st));
+    GS_TRY(cudaMemcpyAsync(d_offs, h_offs, (size_t)(count + 1) * 8, cudaMemcpyHostToDevice, st));
+    const int64_t rc = batch_run(c, d_T, symbytes, (int64_t)total, d_offs, count, d_SA, d_U, d_P, st, front);
+    if (rc != 0) return rc;
+    int32_t *h_prim = reinterpret_cast<int32_t *>(c->h_small + 16 + 2 * (count + 1) + 2);
+    for (int32_t k = 0; k < count; ++k) {
+        GS_TRY(cudaMemcpyAsync(SA[k], d_SA + h_offs[k], (size_t)n[k] * 4, cudaMemcpyDeviceToHost, st));
+        GS_TRY(cudaMemcpyAsync(U[k], d_U + h_offs[k] * sb, (size_t)n[k] * sb, cudaMemcpyDeviceToHost, st));
+    }
+    GS_TRY(cudaMemcpyAsync(h_prim, d_P, (size_t)count * 4, cudaMemcpyDeviceToHost, st));
+    GS_TRY(cudaStreamSynchronize(st));
+    for (int32_t k = 0; k < count; ++k) result[k] = h_prim[k];
+    return 0;
+}
+
+int64_t gsais_ctx_workspace_bytes(gsais_ctx *c)
+{
+    if (!c) return 0;
+    std::lock_guard<std::mutex> lock(c->mu);
+    return (int64_t)c->arena_bytes;
 }
 
 int64_t gsais_batch_sa_bwt(void *ctx, const void *T, const int64_t *offsets, int32_t count, int32_t *SA, uint8_t *U,
@@ -798,7 +858,7 @@ int64_t gsais_batch_sa_bwt(void *ctx, const void *T, const int64_t *offsets, int
     int32_t *d_P = cv.take<int32_t>(count);
     GS_TRY(cudaMemcpyAsync(d_T, T, n, cudaMemcpyHostToDevice, st));
     GS_TRY(cudaMemcpyAsync(d_offs, offsets, (size_t)(count + 1) * 8, cudaMemcpyHostToDevice, st));
-    const int64_t rc = batch_run(c, d_T, n_, d_offs, count, d_SA, d_U, d_P, st, front);
+    const int64_t rc = batch_run(c, d_T, 1, n_, d_offs, count, d_SA, d_U, d_P, st, front);
     if (rc != 0) return rc;
     GS_TRY(cudaMemcpyAsync(SA, d_SA, n * 4, cudaMemcpyDeviceToHost, st));
     GS_TRY(cudaMemcpyAsync(U, d_U, n, cudaMemcpyDeviceToHost, st));

@@ -54,6 +54,16 @@ int64_t gsais_run_plcp(gsais_ctx *ctx, const void *T, int symbytes, const void *
 /* LCP[i] = PLCP[SA[i]] (idx_bytes wide). */
 int64_t gsais_run_lcp(gsais_ctx *ctx, const void *PLCP, const void *SA, void *LCP, int idx_bytes, int64_t n);
 
+/* SA + BWT of `count` small jobs sorted together (one batched sort), each job
+ * k with its own host buffers: text T[k] of n[k] symbols (symbytes 1 or 2),
+ * SA[k] (int32) and U[k].  result[k] receives the primary index.  Returns 0,
+ * -1 for invalid arguments, -2 on device failure.  At most 32000 jobs. */
+int64_t gsais_batch_jobs(gsais_ctx *ctx, int32_t symbytes, int32_t count, const void *const *T, const int64_t *n,
+                         int32_t *const *SA, void *const *U, int64_t *result);
+
+/* Device workspace currently held by ctx (bytes). */
+int64_t gsais_ctx_workspace_bytes(gsais_ctx *ctx);
+
 #ifdef __cplusplus
 }
 #endif

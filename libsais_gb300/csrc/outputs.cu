@@ -79,110 +79,6 @@ __global__ void __launch_bounds__(256) k_bwt(const Sym *__restrict__ T, const ui
     }
 }
 
-// The same gather with four consecutive output symbols per thread, stored
-// as one 4-byte (8-bit symbols) or 8-byte (16-bit symbols) word: U must be
-// aligned to that word.  Rows per thread per step: 4 x B, all SA loads first,
-// then all gathers.
-template <typename Sym>
-__device__ __forceinline__ Sym bwt_symbol(const Sym *__restrict__ T, uint64_t q, const uint8_t *packed,
-                                          int pack_bits, const Sym *dec)
-{
-    if (pack_bits == 2) {
-        const uint32_t w = __ldg(reinterpret_cast<const uint16_t *>(packed) + ((q - 1) >> 3));
-        return dec[(w >> (2 * ((q - 1) & 7))) & 3u];
-    }
-    if (pack_bits == 4) {
-        const uint32_t w = __ldg(reinterpret_cast<const uint32_t *>(packed) + ((q - 1) >> 3));
-        return dec[(w >> (4 * ((q - 1) & 7))) & 15u];
-    }
-    return T[q - 1];
-}
-
-template <typename Sym>
-__global__ void __launch_bounds__(256) k_bwt_words(const Sym *__restrict__ T, const uint32_t *__restrict__ SA,
-                                                   uint64_t n, const uint32_t *__restrict__ isa1,
-                                                   Sym *__restrict__ U, PackedText pk, uint32_t *__restrict__ err)
-{
-    constexpr int B = 2;   // words per thread per step
-    using Word = typename std::conditional<sizeof(Sym) == 1, uint32_t, uint2>::type;
-    __shared__ Sym dec[16];
-    if (threadIdx.x < 16) dec[threadIdx.x] = (Sym)pk.decode[threadIdx.x];
-    __syncthreads();
-    const uint8_t *packed = pk.packed;
-    const int pack_bits = pk.pack_bits;
-    const int lane = threadIdx.x & 31;
-    const uint64_t i0 = (uint64_t)isa1[0] - 1;   // SA row of suffix 0
-    const uint64_t words = (n + 3) / 4;
-    const uint64_t full4 = n / 4;                 // whole 16-byte groups of SA
-    const uint4 *SA4 = reinterpret_cast<const uint4 *>(SA);
-    const uint64_t span = (uint64_t)gridDim.x * blockDim.x * B;
-    bool bad = false;
-    // every thread of a warp runs the same number of steps (the shuffle below)
-    const uint64_t w_round = (words + 31) & ~31ull;
-    for (uint64_t w0 = (uint64_t)blockIdx.x * blockDim.x * B + threadIdx.x; w0 - lane < w_round; w0 += span) {
-        uint32_t p[B][4];
-#pragma unroll
-        for (int j = 0; j < B; ++j) {
-            const uint64_t w = w0 + (uint64_t)j * blockDim.x;
-            // rows 4w .. 4w+3, streamed (not kept in L2)
-            uint4 v = make_uint4(0, 0, 0, 0);
-            if (w < full4) {
-                v = __ldcs(SA4 + w);
-            } else if (w < words) {
-                uint32_t t[4] = {0, 0, 0, 0};
-                for (int r = 0; r < 4; ++r)
-                    if (w * 4 + r < n) t[r] = SA[w * 4 + r];
-                v = make_uint4(t[0], t[1], t[2], t[3]);
-            }
-            // row 4w - 1 (output 4w below the primary row): the previous lane's last row
-            uint32_t prev = __shfl_up_sync(GSAIS_FULL_MASK, v.w, 1);
-            if (lane == 0) prev = (w > 0 && w - 1 < words && 4 * w - 1 < n) ? SA[4 * w - 1] : 0u;
-            // output k = 4w + r takes row k - 1 up to the primary row, row k after it
-            const uint64_t k0 = w * 4;
-            p[j][0] = k0 <= i0 ? prev : v.x;
-            p[j][1] = k0 + 1 <= i0 ? v.x : v.y;
-            p[j][2] = k0 + 2 <= i0 ? v.y : v.z;
-            p[j][3] = k0 + 3 <= i0 ? v.z : v.w;
-        }
-#pragma unroll
-        for (int j = 0; j < B; ++j) {
-            const uint64_t w = w0 + (uint64_t)j * blockDim.x;
-            if (w >= words) continue;
-            Sym v[4];
-#pragma unroll
-            for (int r = 0; r < 4; ++r) {
-                const uint64_t k = w * 4 + r;
-                const uint64_t q = p[j][r];
-                v[r] = 0;
-                if (k == 0) {
-                    v[r] = T[n - 1];
-                } else if (k < n) {
-                    if (q == 0 || q > n) bad = true;
-                    else v[r] = bwt_symbol(T, q, packed, pack_bits, dec);
-                }
-            }
-            if (w * 4 + 4 <= n) {
-                Word out;
-                if (sizeof(Sym) == 1) {
-                    reinterpret_cast<uint32_t &>(out) = (uint32_t)v[0] | ((uint32_t)v[1] << 8) |
-                                                         ((uint32_t)v[2] << 16) | ((uint32_t)v[3] << 24);
-                } else {
-                    uint2 o2;
-                    o2.x = (uint32_t)v[0] | ((uint32_t)v[1] << 16);
-                    o2.y = (uint32_t)v[2] | ((uint32_t)v[3] << 16);
-                    reinterpret_cast<uint2 &>(out) = o2;
-                }
-                __stcs(reinterpret_cast<Word *>(U) + w, out);
-            } else {
-#pragma unroll
-                for (int r = 0; r < 4; ++r)
-                    if (w * 4 + r < n) U[w * 4 + r] = v[r];
-            }
-        }
-    }
-    if (bad && err) atomicOr(err, GSAIS_ERR_BOUNDS);
-}
-
 // BWT rows of the marked SA slots: the rows of slots still unresolved when
 // an early BWT was taken (their U positions are the same under the
 // provisional and the final primary row, as every row between the two lies
@@ -542,56 +438,42 @@ __global__ void __launch_bounds__(256) k_plcp_long(TextWords tw, uint64_t n, con
 
 // Kasai's carried length inside each chunk of kPlcpChunk positions, starting
 // from the exact value at the chunk start (src/libsais.c:8167 compute_plcp
-// restarts at block starts too).  A CTA stages the Phi values of 128 chunks
-// in shared memory (coalesced), each thread walks its chunk, and the PLCP
-// values go back over Phi, coalesced.
+// restarts at block starts too).  A thread per chunk; Phi (read-only) and
+// PLCP are separate arrays, so the Phi sectors a lane walks stay in L1 while
+// its PLCP stores go out, and no shared memory limits the threads in flight
+// (each thread's steps form one dependent chain of text reads).
 constexpr uint32_t kPlcpChunk = 64;
-constexpr int kKasaiThreads = 128;
-constexpr int kKasaiStride = kPlcpChunk + 1;   // padded rows: no bank conflicts
 
 template <typename Sym, bool GSA, int PB>
-__global__ void __launch_bounds__(kKasaiThreads) k_plcp_kasai(TextWords tw, uint64_t n, uint64_t nchunks,
-                                                              const uint32_t *__restrict__ sparse,
-                                                              uint32_t *__restrict__ plcp, uint32_t *__restrict__ err)
+__global__ void __launch_bounds__(256) k_plcp_kasai(TextWords tw, uint64_t n, uint64_t nchunks,
+                                                    const uint32_t *__restrict__ sparse,
+                                                    const uint32_t *__restrict__ phi, uint32_t *__restrict__ plcp,
+                                                    uint32_t *__restrict__ err)
 {
-    __shared__ uint32_t s[kKasaiThreads * kKasaiStride];
-    const uint64_t tile0 = (uint64_t)blockIdx.x * kKasaiThreads * kPlcpChunk;
-    for (uint32_t e = threadIdx.x; e < kKasaiThreads * kPlcpChunk; e += kKasaiThreads) {
-        const uint64_t x = tile0 + e;
-        if (x < n) s[(e / kPlcpChunk) * kKasaiStride + (e % kPlcpChunk)] = plcp[x];
-    }
-    __syncthreads();
-    const uint64_t k = (uint64_t)blockIdx.x * kKasaiThreads + threadIdx.x;
+    const uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nchunks) return;
+    const uint64_t a = k * kPlcpChunk;
+    const uint64_t e = a + kPlcpChunk < n ? a + kPlcpChunk : n;
+    uint64_t l = sparse[k];
+    plcp[a] = (uint32_t)l;
     bool bad = false;
-    if (k < nchunks) {
-        uint32_t *row = s + threadIdx.x * kKasaiStride;
-        const uint64_t a = k * kPlcpChunk;
-        const uint64_t e = a + kPlcpChunk < n ? a + kPlcpChunk : n;
-        uint64_t l = sparse[k];
-        row[0] = (uint32_t)l;
-        for (uint64_t x = a + 1; x < e; ++x) {
-            uint64_t b = row[x - a];
-            if (b > n) {
-                bad = true;
-                b = n;
-            }
-            if (b == n) {
-                l = 0;
-            } else {
-                l = l ? l - 1 : 0;
-                const uint64_t m = n - (x > b ? x : b);
-                if (l > m) l = m;
-                l = extend_thread<Sym, GSA, PB>(tw, x, b, l, m);
-            }
-            row[x - a] = (uint32_t)l;
+    for (uint64_t x = a + 1; x < e; ++x) {
+        uint64_t b = __ldg(phi + x);
+        if (b > n) {
+            bad = true;
+            b = n;
         }
+        if (b == n) {
+            l = 0;
+        } else {
+            l = l ? l - 1 : 0;
+            const uint64_t m = n - (x > b ? x : b);
+            if (l > m) l = m;
+            l = extend_thread<Sym, GSA, PB>(tw, x, b, l, m);
+        }
+        plcp[x] = (uint32_t)l;
     }
     if (bad) atomicOr(err, GSAIS_ERR_BOUNDS);
-    __syncthreads();
-    for (uint32_t e = threadIdx.x; e < kKasaiThreads * kPlcpChunk; e += kKasaiThreads) {
-        const uint64_t x = tile0 + e;
-        if (x < n) plcp[x] = s[(e / kPlcpChunk) * kKasaiStride + (e % kPlcpChunk)];
-    }
 }
 
 // LCP[i] = PLCP[SA[i]] (src/libsais.c:8311 compute_lcp).  Bytes: 12 per row.
@@ -657,7 +539,7 @@ constexpr int kMaxLevels = 40;
 uint64_t plcp_chunks(uint64_t n) { return (n + kPlcpChunk - 1) / kPlcpChunk; }
 
 struct PlcpLayout {
-    size_t o_long, o_counts, o_phi, o_hist, o_codes, o_packed, total;
+    size_t o_long, o_counts, o_phi, o_phiarr, o_hist, o_codes, o_packed, total;
 };
 
 PlcpLayout plcp_scratch_layout(uint64_t n)
@@ -671,6 +553,8 @@ PlcpLayout plcp_scratch_layout(uint64_t n)
     w += 64;
     L.o_phi = w;
     w += (phi_scratch_words(n) + 63) / 64 * 64;
+    L.o_phiarr = w;   // Phi itself
+    w += (n + 63) / 64 * 64;
     L.o_hist = w;
     w += 65536;
     L.o_codes = w;
@@ -689,11 +573,12 @@ cudaError_t plcp_run(const Sym *T, const uint32_t *SA, uint64_t n, uint32_t *plc
     uint32_t *sparse = scratch;
     uint2 *long_list = reinterpret_cast<uint2 *>(scratch + L.o_long);
     uint32_t *counts = scratch + L.o_counts;
+    uint32_t *phi = scratch + L.o_phiarr;
     if (phi_partitioned(n)) {
-        cudaError_t e = phi_permute(SA, n, plcp, scratch + L.o_phi, err, st);
+        cudaError_t e = phi_permute(SA, n, phi, scratch + L.o_phi, err, st);
         if (e != cudaSuccess) return e;
     } else {
-        GSAIS_COUNTED((k_phi<<<grid_for(n, 256), 256, 0, st>>>(SA, n, plcp, err)));
+        GSAIS_COUNTED((k_phi<<<grid_for(n, 256), 256, 0, st>>>(SA, n, phi, err)));
     }
     TextWords tw;
     tw.T = reinterpret_cast<const uint8_t *>(T);
@@ -709,21 +594,21 @@ cudaError_t plcp_run(const Sym *T, const uint32_t *SA, uint64_t n, uint32_t *plc
     }
     if (levels > kMaxLevels) return cudaErrorInvalidValue;
     // level 0: chunk 0 from scratch, by the whole grid
-    GSAIS_COUNTED((k_plcp_first_init<<<1, 1, 0, st>>>(plcp, n, sparse, counts, levels, err)));
-    GSAIS_COUNTED((k_plcp_first<Sym, GSA, PB><<<sm_count() * 4, 256, 0, st>>>(tw, n, plcp, sparse)));
+    GSAIS_COUNTED((k_plcp_first_init<<<1, 1, 0, st>>>(phi, n, sparse, counts, levels, err)));
+    GSAIS_COUNTED((k_plcp_first<Sym, GSA, PB><<<sm_count() * 4, 256, 0, st>>>(tw, n, phi, sparse)));
     int level = 0;
     for (uint64_t half = top >> 1; half >= 1; half >>= 1, ++level) {
         const uint64_t count = nchunks > half ? (nchunks - half + 2 * half - 1) / (2 * half) : 0;
         if (count == 0) continue;
         const unsigned blocks = (unsigned)((count + 255) / 256);
-        GSAIS_COUNTED((k_plcp_level<Sym, GSA, PB><<<blocks, 256, 0, st>>>(tw, n, plcp, kPlcpChunk, nchunks, half,
+        GSAIS_COUNTED((k_plcp_level<Sym, GSA, PB><<<blocks, 256, 0, st>>>(tw, n, phi, kPlcpChunk, nchunks, half,
                                                                            sparse, long_list, counts + level, err)));
         const unsigned lg = (unsigned)(count < (uint64_t)sm_count() * 2 ? count : (uint64_t)sm_count() * 2);
-        GSAIS_COUNTED((k_plcp_long<Sym, GSA, PB><<<lg, 256, 0, st>>>(tw, n, plcp, kPlcpChunk, sparse, long_list,
+        GSAIS_COUNTED((k_plcp_long<Sym, GSA, PB><<<lg, 256, 0, st>>>(tw, n, phi, kPlcpChunk, sparse, long_list,
                                                                      counts + level)));
     }
-    GSAIS_COUNTED((k_plcp_kasai<Sym, GSA, PB><<<(unsigned)((nchunks + kKasaiThreads - 1) / kKasaiThreads),
-                                                kKasaiThreads, 0, st>>>(tw, n, nchunks, sparse, plcp, err)));
+    GSAIS_COUNTED((k_plcp_kasai<Sym, GSA, PB><<<(unsigned)((nchunks + 255) / 256), 256, 0, st>>>(
+        tw, n, nchunks, sparse, phi, plcp, err)));
     return cudaGetLastError();
 }
 
@@ -780,18 +665,6 @@ cudaError_t bwt_gather(const void *d_T, int symbytes, const uint32_t *d_SA, cons
                        void *d_U, const PackedText &pk, uint32_t *err, cudaStream_t st)
 {
     if (n == 0) return cudaSuccess;
-    const uintptr_t ua = reinterpret_cast<uintptr_t>(d_U);
-    const bool sa16 = (reinterpret_cast<uintptr_t>(d_SA) & 15) == 0;   // 16-byte SA loads
-    if (symbytes == 1 && (ua & 3) == 0 && sa16) {
-        GSAIS_COUNTED((k_bwt_words<uint8_t><<<grid_for((n + 7) / 8, 256), 256, 0, st>>>(
-            static_cast<const uint8_t *>(d_T), d_SA, n, d_isa1, static_cast<uint8_t *>(d_U), pk, err)));
-        return cudaGetLastError();
-    }
-    if (symbytes == 2 && (ua & 7) == 0 && sa16) {
-        GSAIS_COUNTED((k_bwt_words<uint16_t><<<grid_for((n + 7) / 8, 256), 256, 0, st>>>(
-            static_cast<const uint16_t *>(d_T), d_SA, n, d_isa1, static_cast<uint16_t *>(d_U), pk, err)));
-        return cudaGetLastError();
-    }
     if (symbytes == 1)
         GSAIS_COUNTED((k_bwt<uint8_t><<<grid_for((n + 7) / 8, 256), 256, 0, st>>>(
             static_cast<const uint8_t *>(d_T), d_SA, n, d_isa1, static_cast<uint8_t *>(d_U), pk, err)));
@@ -898,8 +771,20 @@ cudaError_t lcp_gather(const uint32_t *d_PLCP, const uint32_t *d_SA, uint32_t *d
                        cudaStream_t st)
 {
     if (n == 0) return cudaSuccess;
+    // The gather reads 4 bytes at random from PLCP: ask the L2 to fetch single
+    // 32-byte sectors on its misses for this launch (a per-context hint that
+    // ends with the process), then restore the previous setting.
+    size_t prev = 0;
+    const bool hint = cudaDeviceGetLimit(&prev, cudaLimitMaxL2FetchGranularity) == cudaSuccess &&
+                      cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, 32) == cudaSuccess;
+    cudaGetLastError();
     GSAIS_COUNTED((k_lcp<<<grid_for(n, 256), 256, 0, st>>>(d_PLCP, d_SA, d_LCP, n, err)));
-    return cudaGetLastError();
+    const cudaError_t e = cudaGetLastError();
+    if (hint) {
+        cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, prev);
+        cudaGetLastError();
+    }
+    return e;
 }
 
 }  // namespace gsais

@@ -2,17 +2,26 @@
 //
 // Jobs (text in host memory, outputs SA/U in host memory) are queued as they
 // arrive.  `workers` host threads each own a context (CUDA stream + device
-// arena), so jobs taken by different workers run concurrently on the GPU.
-// When a worker becomes free it takes the oldest queued job; if that job is
-// small (n <= small_job_symbols, 8-bit), it also takes the queued small 8-bit
-// jobs behind it (up to max_batch jobs) and sorts them together with the
-// batched path (one set of launches per doubling round for all of them).
-// Admission is against an HBM budget: every worker may hold at most
-// budget / workers bytes of device memory, and a job (or batch) is admitted
-// to a worker only if its footprint -- kFootprintPerSymbol bytes per symbol
-// (sort workspace + text + outputs) -- fits that share.  A job larger than a
-// worker's share is rejected with -2 (the reference would fail allocation
-// with -2 as well, src/libsais.c:6930-6932).
+// arena) and run one job or one coalesced batch at a time, so up to `workers`
+// batches overlap on the GPU; a job that arrives while others run is admitted
+// as soon as a worker and HBM are free.  Every copy goes straight between the
+// job's own buffers and the device (DMA when the caller's buffers are pinned;
+// the driver stages pageable ones), one copy per job and direction.
+//
+// Admission is against one HBM pool of `budget` bytes shared by all workers.
+// A worker's reservation is the larger of the arena it holds and the
+// footprint of the work it runs -- kFootprintPerSymbol bytes per symbol (sort
+// workspace + text + outputs).  The oldest queued job is admitted when its
+// reservation fits the pool; when it does not, idle workers give their arenas
+// back first, and otherwise the job waits for running work to finish.  A job
+// whose footprint exceeds the whole budget is rejected with -2 (the reference
+// fails an allocation with -2 as well, src/libsais.c:6930-6932).
+//
+// Coalescing: when the admitted job is small (n <= small_job_symbols), the
+// queued small jobs of the same symbol width behind it (up to max_batch) are
+// sorted together with it in one batched sort -- one set of launches per
+// doubling round for all of them -- for 8- and 16-bit texts alike.
+#include <algorithm>
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
@@ -28,7 +37,7 @@
 
 namespace {
 
-// device bytes per text symbol: workspace (~68.5) + text + SA + BWT + slack
+// device bytes per text symbol: workspace (~70) + text + SA + BWT + slack
 constexpr double kFootprintPerSymbol = 80.0;
 
 double now_s()
@@ -50,6 +59,12 @@ struct Job {
     int batched = 0;   // number of jobs in the batch it ran in
 };
 
+struct WorkerState {
+    bool busy = false;
+    size_t held = 0;       // arena its context holds
+    size_t reserved = 0;   // its share of the pool: max(held, footprint of its running work)
+};
+
 struct Server {
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
@@ -57,27 +72,19 @@ struct Server {
     std::unordered_map<int64_t, Job *> jobs;
     std::vector<std::thread> threads;
     std::vector<gsais_ctx *> ctxs;
-    size_t budget = 0, share = 0;
+    std::vector<WorkerState> ws;
+    size_t budget = 0, reserved_total = 0, reserved_hwm = 0;
     int64_t small_limit = 0;
     int max_batch = 1;
     bool stopping = false;
     int64_t next_id = 1;
     // statistics
-    int64_t submitted = 0, completed = 0, rejected = 0, batches = 0, batched_jobs = 0;
+    int64_t submitted = 0, completed = 0, rejected = 0, batches = 0, batched_jobs = 0, releases = 0;
     int64_t symbols_done = 0;
-    std::atomic<int64_t> in_flight_bytes{0}, hwm_bytes{0};
     double first_submit = 0, last_done = 0;
 };
 
 size_t footprint(int64_t n) { return (size_t)(kFootprintPerSymbol * (double)n) + ((size_t)8 << 20); }
-
-void note_bytes(Server *s, int64_t delta)
-{
-    const int64_t v = s->in_flight_bytes.fetch_add(delta) + delta;
-    int64_t h = s->hwm_bytes.load();
-    while (v > h && !s->hwm_bytes.compare_exchange_weak(h, v)) {
-    }
-}
 
 void run_single(gsais_ctx *c, Job *j)
 {
@@ -87,23 +94,77 @@ void run_single(gsais_ctx *c, Job *j)
 void run_batch(gsais_ctx *c, std::vector<Job *> &b)
 {
     const int count = (int)b.size();
-    std::vector<int64_t> offs(count + 1, 0);
-    for (int k = 0; k < count; ++k) offs[k + 1] = offs[k] + b[k]->n;
-    const int64_t n = offs[count];
-    std::vector<uint8_t> T((size_t)n), U((size_t)n);
-    std::vector<int32_t> SA((size_t)n), prim(count);
-    for (int k = 0; k < count; ++k) std::memcpy(T.data() + offs[k], b[k]->T, (size_t)b[k]->n);
-    const int64_t rc = gsais_batch_sa_bwt(c, T.data(), offs.data(), count, SA.data(), U.data(), prim.data());
+    std::vector<const void *> T(count);
+    std::vector<int64_t> n(count), res(count, 0);
+    std::vector<int32_t *> SA(count);
+    std::vector<void *> U(count);
     for (int k = 0; k < count; ++k) {
-        Job *j = b[k];
-        if (rc == 0) {
-            std::memcpy(j->SA, SA.data() + offs[k], (size_t)j->n * 4);
-            std::memcpy(j->U, U.data() + offs[k], (size_t)j->n);
-            j->result = prim[k];
-        } else {
-            j->result = rc;
+        T[k] = b[k]->T;
+        n[k] = b[k]->n;
+        SA[k] = b[k]->SA;
+        U[k] = b[k]->U;
+    }
+    const int64_t rc = gsais_batch_jobs(c, b[0]->symbytes, count, T.data(), n.data(), SA.data(), U.data(), res.data());
+    for (int k = 0; k < count; ++k) b[k]->result = rc == 0 ? res[k] : rc;
+}
+
+// Under s->mu: the jobs worker w takes next (oldest first, then the small jobs
+// of the same width behind it), if their reservation fits the pool, after
+// idle workers have given their arenas back if needed.  Empty: wait.
+std::vector<Job *> admit(Server *s, int w)
+{
+    std::vector<Job *> batch;
+    if (s->queue.empty()) return batch;
+    Job *first = s->queue.front();
+    WorkerState &me = s->ws[w];
+    const size_t others = s->reserved_total - me.reserved;   // reserved by the other workers
+    const size_t avail = s->budget > others ? s->budget - others : 0;
+    size_t need = footprint(first->n);
+    std::vector<std::deque<Job *>::iterator> picks;
+    if (first->n <= s->small_limit) {
+        for (auto it = std::next(s->queue.begin()); it != s->queue.end() && (int)picks.size() + 1 < s->max_batch;
+             ++it) {
+            Job *j = *it;
+            if (j->symbytes == first->symbytes && j->n <= s->small_limit && need + footprint(j->n) <= avail) {
+                need += footprint(j->n);
+                picks.push_back(it);
+            }
         }
     }
+    size_t want = std::max(me.held, need);
+    // give back idle workers' arenas (largest first) while the pool is short
+    while (s->reserved_total - me.reserved + want > s->budget) {
+        int victim = -1;
+        for (int o = 0; o < (int)s->ws.size(); ++o)
+            if (o != w && !s->ws[o].busy && s->ws[o].held > 0 && (victim < 0 || s->ws[o].held > s->ws[victim].held))
+                victim = o;
+        if (victim < 0) break;
+        gsais_release_workspace(s->ctxs[victim]);   // idle: its context runs nothing
+        s->reserved_total -= s->ws[victim].reserved;
+        s->ws[victim].held = s->ws[victim].reserved = 0;
+        ++s->releases;
+    }
+    if (s->reserved_total - me.reserved + want > s->budget && me.held > need) {
+        // this worker's own arena is what is too large: give it back too
+        gsais_release_workspace(s->ctxs[w]);
+        s->reserved_total -= me.reserved;
+        me.held = me.reserved = 0;
+        ++s->releases;
+        want = need;
+    }
+    if (s->reserved_total - me.reserved + want > s->budget) return batch;   // wait for running work
+    for (auto it = picks.rbegin(); it != picks.rend(); ++it) {
+        batch.push_back(**it);
+        s->queue.erase(*it);
+    }
+    std::reverse(batch.begin(), batch.end());
+    batch.insert(batch.begin(), first);
+    s->queue.pop_front();
+    s->reserved_total += want - me.reserved;
+    me.reserved = want;
+    me.busy = true;
+    s->reserved_hwm = std::max(s->reserved_hwm, s->reserved_total);
+    return batch;
 }
 
 void worker(Server *s, int w)
@@ -113,39 +174,26 @@ void worker(Server *s, int w)
         std::vector<Job *> batch;
         {
             std::unique_lock<std::mutex> lk(s->mu);
-            s->cv_work.wait(lk, [&] { return s->stopping || !s->queue.empty(); });
-            if (s->queue.empty()) return;   // stopping and drained
-            Job *first = s->queue.front();
-            s->queue.pop_front();
-            batch.push_back(first);
-            size_t bytes = footprint(first->n);
-            if (first->symbytes == 1 && first->n <= s->small_limit) {
-                // coalesce the queued small 8-bit jobs behind it
-                for (auto it = s->queue.begin(); it != s->queue.end() && (int)batch.size() < s->max_batch;) {
-                    Job *j = *it;
-                    if (j->symbytes == 1 && j->n <= s->small_limit && bytes + footprint(j->n) <= s->share) {
-                        bytes += footprint(j->n);
-                        batch.push_back(j);
-                        it = s->queue.erase(it);
-                    } else {
-                        ++it;
-                    }
-                }
+            for (;;) {
+                if (s->stopping && s->queue.empty()) return;   // stopping and drained
+                batch = admit(s, w);
+                if (!batch.empty()) break;
+                s->cv_work.wait(lk);
             }
         }
         const double t0 = now_s();
-        size_t bytes = 0;
-        for (Job *j : batch) {
-            j->t_start = t0;
-            bytes += footprint(j->n);
-        }
-        note_bytes(s, (int64_t)bytes);
+        for (Job *j : batch) j->t_start = t0;
         if (batch.size() == 1) run_single(c, batch[0]);
         else run_batch(c, batch);
-        note_bytes(s, -(int64_t)bytes);
+        const size_t held = (size_t)gsais_ctx_workspace_bytes(c);
         const double t1 = now_s();
         {
             std::lock_guard<std::mutex> lk(s->mu);
+            WorkerState &me = s->ws[w];
+            s->reserved_total -= me.reserved;
+            me.held = me.reserved = held;
+            s->reserved_total += held;
+            me.busy = false;
             for (Job *j : batch) {
                 j->t_done = t1;
                 j->done = true;
@@ -160,6 +208,7 @@ void worker(Server *s, int w)
             s->last_done = t1;
         }
         s->cv_done.notify_all();
+        s->cv_work.notify_all();   // the pool has room again
     }
 }
 
@@ -169,11 +218,10 @@ extern "C" {
 
 void *gsais_server_create(int64_t hbm_budget_bytes, int32_t workers, int64_t small_job_symbols, int32_t max_batch)
 {
-    if (hbm_budget_bytes <= 0 || workers <= 0 || max_batch <= 0) return nullptr;
+    if (hbm_budget_bytes <= 0 || workers <= 0 || max_batch <= 0 || max_batch > 32000) return nullptr;
     Server *s = new (std::nothrow) Server();
     if (!s) return nullptr;
     s->budget = (size_t)hbm_budget_bytes;
-    s->share = s->budget / (size_t)workers;
     s->small_limit = small_job_symbols;
     s->max_batch = max_batch;
     for (int w = 0; w < workers; ++w) {
@@ -186,6 +234,7 @@ void *gsais_server_create(int64_t hbm_budget_bytes, int32_t workers, int64_t sma
         delete s;
         return nullptr;
     }
+    s->ws.resize(workers);
     for (int w = 0; w < workers; ++w) s->threads.emplace_back(worker, s, w);
     return s;
 }
@@ -212,8 +261,8 @@ int64_t gsais_server_submit(void *srv, const void *T, int32_t symbytes, int64_t 
         s->jobs[j->id] = j;
         ++s->submitted;
         if (s->first_submit == 0) s->first_submit = j->t_submit;
-        if (footprint(n) > s->share) {
-            // does not fit a worker's share of the HBM budget
+        if (footprint(n) > s->budget) {
+            // larger than the whole HBM budget
             j->result = -2;
             j->done = true;
             j->t_done = j->t_submit;
@@ -224,7 +273,7 @@ int64_t gsais_server_submit(void *srv, const void *T, int32_t symbytes, int64_t 
         }
         s->queue.push_back(j);
     }
-    s->cv_work.notify_one();
+    s->cv_work.notify_all();
     return j->id;
 }
 
@@ -260,7 +309,7 @@ int32_t gsais_server_get_stats(void *srv, gsais_server_stats *out)
     out->batches = s->batches;
     out->batched_jobs = s->batched_jobs;
     out->symbols_done = s->symbols_done;
-    out->hbm_high_water_bytes = s->hwm_bytes.load();
+    out->hbm_high_water_bytes = (int64_t)s->reserved_hwm;
     out->hbm_budget_bytes = (int64_t)s->budget;
     out->busy_seconds = s->last_done > s->first_submit ? s->last_done - s->first_submit : 0;
     out->footprint_bytes_per_symbol = kFootprintPerSymbol;

@@ -1164,13 +1164,17 @@ __global__ void __launch_bounds__(256) k_small_groups(const uint32_t *__restrict
                                                       uint32_t *__restrict__ gstart_out,
                                                       unsigned long long *__restrict__ counter,
                                                       uint32_t *__restrict__ pairs,
-                                                      unsigned long long *__restrict__ pair_count)
+                                                      unsigned long long *__restrict__ pair_count,
+                                                      uint64_t tiles)
 {
     constexpr int WARPS = 8;
     __shared__ uint32_t s_we[WARPS], s_wg[WARPS];
     __shared__ unsigned long long s_base;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint64_t wb = ((uint64_t)blockIdx.x * WARPS + warp) * 32;
+    // a resident grid walks the tiles of 256 list positions; a tile whose
+    // warps own no group (all in medium or large groups) is skipped whole
+    for (uint64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    const uint64_t wb = (tile * WARPS + warp) * 32;
     const uint64_t j0 = wb + lane, j1 = wb + 32 + lane;
     const bool v0 = j0 < N, v1 = j1 < N;
     const uint32_t g0 = v0 ? act_gid[j0] : 0xFFFFFFFFu;
@@ -1212,6 +1216,7 @@ __global__ void __launch_bounds__(256) k_small_groups(const uint32_t *__restrict
         (void)j;
         own[e] = ok;
     }
+    if (!__syncthreads_or(own[0] || own[1])) continue;   // the same decision in every thread
     const uint32_t rr0 = own[0] ? r2[j0] : 0u, rr1 = own[1] ? r2[j1] : 0u;
     const uint32_t p0 = own[0] ? act_pos[j0] : 0u, p1 = own[1] ? act_pos[j1] : 0u;
     const uint32_t i0 = own[0] ? act_i[j0] : 0u, i1 = own[1] ? act_i[j1] : 0u;
@@ -1346,6 +1351,8 @@ __global__ void __launch_bounds__(256) k_small_groups(const uint32_t *__restrict
         out_gid[c] = g;
         if (hsub[e]) gstart_out[g] = c;
     }
+    __syncthreads();   // s_we, s_wg and s_base are reused by the next tile
+    }
 }
 
 // ------------------------------------------------------ batched strings
@@ -1371,8 +1378,9 @@ __device__ __forceinline__ uint32_t string_of(const uint64_t *__restrict__ offs,
     return lo;
 }
 
-// Bytes per suffix: T 1 read (windows overlap in L1), key 8 + value 4 written.
-__global__ void __launch_bounds__(256) k_seed_batch(const uint8_t *__restrict__ T, uint64_t n,
+// Bytes per suffix: T s read (windows overlap in L1), key 8 + value 4 written.
+template <typename Sym>
+__global__ void __launch_bounds__(256) k_seed_batch(const Sym *__restrict__ T, uint64_t n,
                                                     const uint64_t *__restrict__ offs, uint32_t count,
                                                     const uint16_t *__restrict__ codes, int bits, int K,
                                                     uint64_t *__restrict__ keys, uint32_t *__restrict__ vals,
@@ -1406,10 +1414,11 @@ __global__ void __launch_bounds__(256) k_seed_batch(const uint8_t *__restrict__ 
 // Per-string outputs from the batched rows: SA relative to the string start,
 // BWT in libsais_bwt's layout and the primary index of every string.
 // Bytes per row: SA 4 read + 4 gathered, T 1 gathered; SA 4 + U 1 written.
+template <typename Sym>
 __global__ void __launch_bounds__(256) k_batch_outputs(const uint32_t *__restrict__ SA, const uint32_t *__restrict__ isa1,
-                                                       const uint8_t *__restrict__ T, uint64_t n,
+                                                       const Sym *__restrict__ T, uint64_t n,
                                                        const uint64_t *__restrict__ offs, uint32_t count,
-                                                       int32_t *__restrict__ sa_out, uint8_t *__restrict__ U,
+                                                       int32_t *__restrict__ sa_out, Sym *__restrict__ U,
                                                        int32_t *__restrict__ primary, uint32_t *__restrict__ err)
 {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -2223,6 +2232,9 @@ static cudaError_t run_rounds(SortWorkspace &ws, uint64_t nr, int K, uint32_t ke
 {
     const uint32_t medium_small = (uint32_t)(tn.medium_small < (int)kMediumSmall ? tn.medium_small : kMediumSmall);
     const uint32_t medium_max = (uint32_t)(tn.medium_max < (int)kMediumMax ? tn.medium_max : kMediumMax);
+    // the large groups of the previous round took the few-others path: this
+    // round's keys skip the digit histograms (a full sort counts its own)
+    bool few_last = false;
     cudaError_t e;
     int ran = 0;
     const int b2 = gsais_bits_for(nr);
@@ -2256,14 +2268,16 @@ static cudaError_t run_rounds(SortWorkspace &ws, uint64_t nr, int K, uint32_t ke
                                                                       ws.few)));
         if (ev_cl) ws.radix.prof->end(KK_CLASSIFY, ev_cl, st, G * 12);   // group table 8 read, class 4 written
         cudaEvent_t ev_rk = ws.radix.prof ? ws.radix.prof->begin(st) : nullptr;
+        const int hist_passes = (tn.large_few_others && few_last) ? 0 : passes;
         GSAIS_COUNTED((k_round_r2<<<stream_grid(N, 256), 256, 0, st>>>(
             act_i, act_pos, act_gid, ws.gstart[pg], ws.lid, ws.loff, ws.rank, h, N, nr, b2, r2, ws.keys[0],
-            ws.lvals[0], ws.lpos, d_err, passes, end_bit, ws.radix.hist)));
+            ws.lvals[0], ws.lpos, d_err, hist_passes, end_bit, ws.radix.hist)));
         if (ev_rk) ws.radix.prof->end(KK_ROUND_KEYS, ev_rk, st, N * 28);
         cudaEvent_t ev_sm = ws.radix.prof ? ws.radix.prof->begin(st) : nullptr;
-        GSAIS_COUNTED((k_small_groups<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(
+        const uint64_t sg_tiles = (N + 255) / 256;
+        GSAIS_COUNTED((k_small_groups<<<resident_grid(k_small_groups, 256, sg_tiles), 256, 0, st>>>(
             act_i, act_pos, act_gid, r2, N, ws.rank, ws.sa, out_i, out_pos, out_gid, ws.gstart[pg ^ 1],
-            ws.counters, pairs, ws.counters + 3)));
+            ws.counters, pairs, ws.counters + 3, sg_tiles)));
         if (ev_sm) ws.radix.prof->end(KK_SMALL, ev_sm, st, N * 32);
         // medium groups: one wave of resident CTAs, each looping over the
         // groups (their count is on the device)
@@ -2311,12 +2325,13 @@ static cudaError_t run_rounds(SortWorkspace &ws, uint64_t nr, int K, uint32_t ke
                     sorted_vals = ws.lvals[1];
                 }
             }
+            few_last = few;
             if (!few) {
                 uint64_t *kk[2] = {ws.keys[0], ws.keys[1]};
                 uint32_t *vv[2] = {ws.lvals[0], ws.lvals[1]};
                 int which = 0;
-                if ((e = radix_sort_pairs(kk, vv, NL, end_bit, ws.radix, d_err, st, &which, &ran, true)) !=
-                    cudaSuccess)
+                if ((e = radix_sort_pairs(kk, vv, NL, end_bit, ws.radix, d_err, st, &which, &ran,
+                                          hist_passes > 0)) != cudaSuccess)
                     return e;
                 S.radix_passes += ran;
                 sorted_keys = kk[which];
@@ -2677,7 +2692,7 @@ namespace gsais {
 
 size_t batch_workspace_bytes(uint64_t n, uint32_t count) { return sort_workspace_bytes(n + count, 1); }
 
-cudaError_t batch_suffix_sort(const uint8_t *d_T, uint64_t n, const uint64_t *d_offs, uint32_t count,
+cudaError_t batch_suffix_sort(const void *d_T, int symbytes, uint64_t n, const uint64_t *d_offs, uint32_t count,
                               SortWorkspace &ws, uint32_t *d_err, cudaStream_t st, SortStats *stats,
                               const Tuning *tuning)
 {
@@ -2690,9 +2705,10 @@ cudaError_t batch_suffix_sort(const uint8_t *d_T, uint64_t n, const uint64_t *d_
 
     uint32_t *h_hist = ws.h_small + 16;
     uint16_t *h_codes = reinterpret_cast<uint16_t *>(ws.h_small + 16 + 65536);
-    if ((e = symbol_histogram(d_T, 1, n, ws.hist, h_hist, st)) != cudaSuccess) return e;
+    const int nsym = symbytes == 1 ? 256 : 65536;
+    if ((e = symbol_histogram(d_T, symbytes, n, ws.hist, h_hist, st)) != cudaSuccess) return e;
     uint32_t sigma = 0;
-    for (int c = 0; c < 256; ++c) {
+    for (int c = 0; c < nsym; ++c) {
         if (h_hist[c]) ++sigma;
         h_codes[c] = h_hist[c] ? (uint16_t)sigma : (uint16_t)0;   // codes 1..sigma; 0 = end of string
     }
@@ -2707,16 +2723,22 @@ cudaError_t batch_suffix_sort(const uint8_t *d_T, uint64_t n, const uint64_t *d_
     S.seed_symbols = K;
     S.seed_bits = bits;
     ws.pack_bits = 0;
-    if ((e = cudaMemcpyAsync(ws.codes, h_codes, 256 * 2, cudaMemcpyHostToDevice, st)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(ws.codes, h_codes, (size_t)nsym * 2, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+        return e;
     if ((e = cudaMemsetAsync(ws.rank, 0, (nr + 1) * sizeof(uint32_t), st)) != cudaSuccess) return e;
 
     const int seed_end = K * bits + sid_bits;
     const int seed_passes = (seed_end + 7) / 8;
     if ((e = cudaMemsetAsync(ws.radix.hist, 0, (size_t)seed_passes * 256 * 4, st)) != cudaSuccess) return e;
     cudaEvent_t ev_seed = ws.radix.prof ? ws.radix.prof->begin(st) : nullptr;
-    GSAIS_COUNTED((k_seed_batch<<<stream_grid(n, 256), 256, 0, st>>>(d_T, n, d_offs, count, ws.codes, bits, K,
-                                                                     ws.keys[0], ws.vals[0], seed_passes, seed_end,
-                                                                     ws.radix.hist)));
+    if (symbytes == 1)
+        GSAIS_COUNTED((k_seed_batch<uint8_t><<<stream_grid(n, 256), 256, 0, st>>>(
+            static_cast<const uint8_t *>(d_T), n, d_offs, count, ws.codes, bits, K, ws.keys[0], ws.vals[0],
+            seed_passes, seed_end, ws.radix.hist)));
+    else
+        GSAIS_COUNTED((k_seed_batch<uint16_t><<<stream_grid(n, 256), 256, 0, st>>>(
+            static_cast<const uint16_t *>(d_T), n, d_offs, count, ws.codes, bits, K, ws.keys[0], ws.vals[0],
+            seed_passes, seed_end, ws.radix.hist)));
     if (ev_seed) ws.radix.prof->end(KK_SEED, ev_seed, st, n * 13);
     int w = 0, ran = 0;
     {
@@ -2754,15 +2776,21 @@ cudaError_t batch_suffix_sort(const uint8_t *d_T, uint64_t n, const uint64_t *d_
     return ws.h_small[0] ? cudaErrorUnknown : cudaSuccess;
 }
 
-cudaError_t batch_outputs(const SortWorkspace &ws, const uint8_t *d_T, uint64_t n, const uint64_t *d_offs,
-                          uint32_t count, int32_t *d_sa, uint8_t *d_U, int32_t *d_primary, uint32_t *d_err,
+cudaError_t batch_outputs(const SortWorkspace &ws, const void *d_T, int symbytes, uint64_t n, const uint64_t *d_offs,
+                          uint32_t count, int32_t *d_sa, void *d_U, int32_t *d_primary, uint32_t *d_err,
                           cudaStream_t st)
 {
     cudaError_t e;
     if ((e = cudaMemsetAsync(d_primary, 0, (size_t)count * sizeof(int32_t), st)) != cudaSuccess) return e;
     if (n == 0) return cudaSuccess;
-    GSAIS_COUNTED((k_batch_outputs<<<stream_grid(n, 256), 256, 0, st>>>(ws.sa, ws.rank, d_T, n, d_offs, count, d_sa,
-                                                                        d_U, d_primary, d_err)));
+    if (symbytes == 1)
+        GSAIS_COUNTED((k_batch_outputs<uint8_t><<<stream_grid(n, 256), 256, 0, st>>>(
+            ws.sa, ws.rank, static_cast<const uint8_t *>(d_T), n, d_offs, count, d_sa, static_cast<uint8_t *>(d_U),
+            d_primary, d_err)));
+    else
+        GSAIS_COUNTED((k_batch_outputs<uint16_t><<<stream_grid(n, 256), 256, 0, st>>>(
+            ws.sa, ws.rank, static_cast<const uint16_t *>(d_T), n, d_offs, count, d_sa,
+            static_cast<uint16_t *>(d_U), d_primary, d_err)));
     return cudaGetLastError();
 }
 

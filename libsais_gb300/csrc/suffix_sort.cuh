@@ -102,18 +102,19 @@ cudaError_t early_sa_patch(const EarlySaCopy &ec, const uint32_t *d_sa, uint64_t
 cudaError_t suffix_sort(const void *d_T, int symbytes, uint64_t n, bool gsa, SortWorkspace &ws,
                         const SortOptions &opt, uint32_t *d_err, cudaStream_t st, SortStats *stats);
 
-// Batched suffix arrays of `count` independent uint8 strings concatenated in
-// d_T (string s = [offs[s], offs[s+1]), offs on the device, offs[count] = n),
-// all sorted in the same launches.  Workspace: batch_workspace_bytes.
+// Batched suffix arrays of `count` independent strings of 8- or 16-bit
+// symbols (symbytes 1 or 2) concatenated in d_T (string s = [offs[s],
+// offs[s+1]), offs on the device, offs[count] = n), all sorted in the same
+// launches.  Workspace: batch_workspace_bytes.
 // On return ws.sa holds the rows (rank coordinates) grouped by string.
 size_t batch_workspace_bytes(uint64_t n, uint32_t count);
-cudaError_t batch_suffix_sort(const uint8_t *d_T, uint64_t n, const uint64_t *d_offs, uint32_t count,
+cudaError_t batch_suffix_sort(const void *d_T, int symbytes, uint64_t n, const uint64_t *d_offs, uint32_t count,
                               SortWorkspace &ws, uint32_t *d_err, cudaStream_t st, SortStats *stats,
                               const Tuning *tuning = nullptr);
 // Per-string SA (relative to each string), BWT (libsais_bwt layout) and
 // primary indexes from a finished batch_suffix_sort.
-cudaError_t batch_outputs(const SortWorkspace &ws, const uint8_t *d_T, uint64_t n, const uint64_t *d_offs,
-                          uint32_t count, int32_t *d_sa, uint8_t *d_U, int32_t *d_primary, uint32_t *d_err,
+cudaError_t batch_outputs(const SortWorkspace &ws, const void *d_T, int symbytes, uint64_t n, const uint64_t *d_offs,
+                          uint32_t count, int32_t *d_sa, void *d_U, int32_t *d_primary, uint32_t *d_err,
                           cudaStream_t st);
 
 // Symbol histogram of a device text into d_hist and the pinned h_hist
