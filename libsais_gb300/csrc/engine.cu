@@ -10,6 +10,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <vector>
 
 #include "device_util.cuh"
 #include "engine.h"
@@ -803,18 +804,19 @@ int64_t gsais_batch_jobs(gsais_ctx *c, int32_t symbytes, int32_t count, const vo
     int32_t *d_SA = cv.take<int32_t>(total);
     uint8_t *d_U = cv.take<uint8_t>(total * sb);
     int32_t *d_P = cv.take<int32_t>(count);
-    // offsets and primary indexes through the pinned scratch (at most 32000 jobs)
-    if ((size_t)(count + 1) * 2 + 2 + (size_t)count > kSmallWords - 16) return -1;
-    uint64_t *h_offs = reinterpret_cast<uint64_t *>(c->h_small + 16);
-    h_offs[0] = 0;
+    // the offsets stay in host memory of their own (the sort reuses the
+    // context's pinned scratch); the primary indexes come back through it
+    // once the sort is done (at most 32000 jobs)
+    if ((size_t)count > kSmallWords - 16) return -1;
+    std::vector<uint64_t> h_offs((size_t)count + 1, 0);
     for (int32_t k = 0; k < count; ++k) h_offs[k + 1] = h_offs[k] + (uint64_t)n[k];
     // one copy per job straight from its buffer (DMA when the buffer is pinned)
     for (int32_t k = 0; k < count; ++k)
         GS_TRY(cudaMemcpyAsync(d_T + h_offs[k] * sb, T[k], (size_t)n[k] * sb, cudaMemcpyHostToDevice, st));
-    GS_TRY(cudaMemcpyAsync(d_offs, h_offs, (size_t)(count + 1) * 8, cudaMemcpyHostToDevice, st));
+    GS_TRY(cudaMemcpyAsync(d_offs, h_offs.data(), (size_t)(count + 1) * 8, cudaMemcpyHostToDevice, st));
     const int64_t rc = batch_run(c, d_T, symbytes, (int64_t)total, d_offs, count, d_SA, d_U, d_P, st, front);
     if (rc != 0) return rc;
-    int32_t *h_prim = reinterpret_cast<int32_t *>(c->h_small + 16 + 2 * (count + 1) + 2);
+    int32_t *h_prim = reinterpret_cast<int32_t *>(c->h_small + 16);
     for (int32_t k = 0; k < count; ++k) {
         GS_TRY(cudaMemcpyAsync(SA[k], d_SA + h_offs[k], (size_t)n[k] * 4, cudaMemcpyDeviceToHost, st));
         GS_TRY(cudaMemcpyAsync(U[k], d_U + h_offs[k] * sb, (size_t)n[k] * sb, cudaMemcpyDeviceToHost, st));

@@ -771,20 +771,8 @@ cudaError_t lcp_gather(const uint32_t *d_PLCP, const uint32_t *d_SA, uint32_t *d
                        cudaStream_t st)
 {
     if (n == 0) return cudaSuccess;
-    // The gather reads 4 bytes at random from PLCP: ask the L2 to fetch single
-    // 32-byte sectors on its misses for this launch (a per-context hint that
-    // ends with the process), then restore the previous setting.
-    size_t prev = 0;
-    const bool hint = cudaDeviceGetLimit(&prev, cudaLimitMaxL2FetchGranularity) == cudaSuccess &&
-                      cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, 32) == cudaSuccess;
-    cudaGetLastError();
     GSAIS_COUNTED((k_lcp<<<grid_for(n, 256), 256, 0, st>>>(d_PLCP, d_SA, d_LCP, n, err)));
-    const cudaError_t e = cudaGetLastError();
-    if (hint) {
-        cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, prev);
-        cudaGetLastError();
-    }
-    return e;
+    return cudaGetLastError();
 }
 
 }  // namespace gsais

@@ -120,14 +120,15 @@ std::vector<Job *> admit(Server *s, int w)
     const size_t others = s->reserved_total - me.reserved;   // reserved by the other workers
     const size_t avail = s->budget > others ? s->budget - others : 0;
     size_t need = footprint(first->n);
-    std::vector<std::deque<Job *>::iterator> picks;
+    std::vector<Job *> picks;   // small jobs of the same width behind the first, in queue order
+    size_t scanned = 1;
     if (first->n <= s->small_limit) {
-        for (auto it = std::next(s->queue.begin()); it != s->queue.end() && (int)picks.size() + 1 < s->max_batch;
-             ++it) {
-            Job *j = *it;
+        const size_t depth = std::min(s->queue.size(), (size_t)s->max_batch * 4);   // bounded look-ahead
+        for (; scanned < depth && (int)picks.size() + 1 < s->max_batch; ++scanned) {
+            Job *j = s->queue[scanned];
             if (j->symbytes == first->symbytes && j->n <= s->small_limit && need + footprint(j->n) <= avail) {
                 need += footprint(j->n);
-                picks.push_back(it);
+                picks.push_back(j);
             }
         }
     }
@@ -153,13 +154,14 @@ std::vector<Job *> admit(Server *s, int w)
         want = need;
     }
     if (s->reserved_total - me.reserved + want > s->budget) return batch;   // wait for running work
-    for (auto it = picks.rbegin(); it != picks.rend(); ++it) {
-        batch.push_back(**it);
-        s->queue.erase(*it);
-    }
-    std::reverse(batch.begin(), batch.end());
-    batch.insert(batch.begin(), first);
-    s->queue.pop_front();
+    batch.push_back(first);
+    batch.insert(batch.end(), picks.begin(), picks.end());
+    // drop the taken jobs from the scanned front of the queue (one pass, order kept)
+    for (Job *j : batch) j->batched = -1;   // mark
+    auto head_end = s->queue.begin() + (std::ptrdiff_t)scanned;
+    auto kept_end = std::remove_if(s->queue.begin(), head_end, [](Job *j) { return j->batched == -1; });
+    s->queue.erase(kept_end, head_end);
+    for (Job *j : batch) j->batched = 0;
     s->reserved_total += want - me.reserved;
     me.reserved = want;
     me.busy = true;

@@ -34,6 +34,7 @@ struct SortWorkspace {
     int pack_bits = 0;                       // 0 (not packed), 2 or 4
     uint16_t decode[16] = {0};               // symbol of each code when packed
     uint32_t *few = nullptr;                 // scratch of the large groups with few differing members
+    uint32_t *sg_tiles = nullptr;            // flags + list of a round's small-group tiles
     uint64_t n_cap = 0;                      // symbols the workspace was carved for
     RadixScratch radix;
     uint32_t *h_small = nullptr;             // pinned host scratch (kHostSmallWords words)
@@ -88,6 +89,7 @@ struct SortOptions {
     uint32_t raw_max = 0;     // 32-bit integer symbols: the largest symbol value
     EarlySaCopy *early = nullptr;
     bool hist_ready = false;  // ws.hist already holds the symbol histogram (symbol_histogram_part)
+    bool pair_chains = true;  // seed pairs ordered along chains of copies (one comparison per chain)
 };
 
 // Queues on `st`, behind the bulk copy (ec.copied), the writes of the
