@@ -163,10 +163,14 @@ def barrier(dist):
 
 
 def host_threads() -> int:
+    """All host CPUs: this process's CPU affinity is widened to every CPU first
+    (a parent that ran CUDA work may have left a narrower mask to its children)."""
+    n = os.cpu_count() or 1
     try:
+        os.sched_setaffinity(0, set(range(n)))
         return len(os.sched_getaffinity(0))
-    except AttributeError:
-        return os.cpu_count() or 1
+    except (AttributeError, OSError):
+        return n
 
 
 def bench_config(name: str, n: int) -> dict:
@@ -412,6 +416,8 @@ def run_batched(G, torch, count: int = 4096, steps: int = 3, warmup: int = 1, cp
     torch.cuda.synchronize()
     batched_ms = e0.elapsed_time(e1) / steps
     batched_launches = (G.launch_count() - launches0) / steps
+    split = _kernel_split(G, torch, lambda: G.batch_sa_bwt_device(dT, dO, dSA, dU, dP, stream=stream), steps=1)
+    bst = G.last_stats()
     # one call per string, same buffers
     pSA = torch.empty_like(dSA)
     pU = torch.empty_like(dU)
@@ -444,6 +450,8 @@ def run_batched(G, torch, count: int = 4096, steps: int = 3, warmup: int = 1, cp
     cpu_s = time.perf_counter() - t0
     return {"strings": count, "total_symbols": n, "batched_mb_s": round(n / 1e6 / (batched_ms / 1e3), 1),
             "batched_ms": round(batched_ms, 2), "batched_launches": batched_launches,
+            "rounds": bst["rounds"], "seed_symbols": bst["seed_symbols"], "active_total": bst["active_total"],
+            "large_total": bst["large_total"], "kernels_ms": split,
             "per_string_mb_s": round(n / 1e6 / per_string_s, 1), "per_string_ms": round(per_string_s * 1e3, 1),
             "per_string_launches": per_string_launches,
             "speedup_vs_per_string": round(per_string_s * 1e3 / batched_ms, 2),
@@ -624,6 +632,21 @@ def run_serving(G, torch, rates=SERVING_RATES, jobs_per_rate: int = 20000, seed:
     return out
 
 
+def _kernel_split(G, torch, fn, steps: int = 2):
+    """Per-kernel device time (CUDA events on the launching stream) of `steps`
+    calls of fn, in ms per call, largest first; with the rounds run."""
+    torch.cuda.synchronize()
+    G.profile_reset()
+    G.profile_enable(True)
+    for _ in range(steps):
+        fn()
+    torch.cuda.synchronize()
+    G.profile_enable(False)
+    prof = G.profile_read()
+    split = {k: round(v["total_ms"] / steps, 3) for k, v in prof.items() if v["launches"]}
+    return dict(sorted(split.items(), key=lambda kv: -kv[1]))
+
+
 def _timed(torch, fn, steps: int = 3, warmup: int = 1):
     for _ in range(warmup):
         rc = fn()
@@ -750,10 +773,14 @@ def run_gsa(G, torch, reads: int = 1 << 20):
     dSA = torch.empty(n, dtype=torch.int32, device="cuda")
     stream = torch.cuda.current_stream()
     sa_ms = _timed(torch, lambda: G.sa_device(dT, dSA, gsa=True, stream=stream))
+    split = _kernel_split(G, torch, lambda: G.sa_device(dT, dSA, gsa=True, stream=stream))
+    st = G.last_stats()
     O = Oracle()
     pl = run_plcp_lcp(G, torch, dT, dSA, n, T, O, gsa=True)
     ok_sa = O.check_sa(T, dSA.cpu().numpy().astype(np.int64), gsa=True)
     return {"reads": reads, "n": n, "gsa_mb_s": round(n / 1e6 / (sa_ms / 1e3), 1), "gsa_ms": round(sa_ms, 3),
+            "rounds": st["rounds"], "seed_symbols": st["seed_symbols"], "active_total": st["active_total"],
+            "large_total": st["large_total"], "kernels_ms": split,
             "plcp_gsa_mb_s": pl["plcp_mb_s"], "lcp_mb_s": pl["lcp_mb_s"], "sa_valid": bool(ok_sa),
             "plcp_matches_oracle": pl["plcp_equals_oracle"], "lcp_matches_oracle": pl["lcp_equals_oracle"]}
 

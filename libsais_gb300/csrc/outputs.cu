@@ -438,42 +438,60 @@ __global__ void __launch_bounds__(256) k_plcp_long(TextWords tw, uint64_t n, con
 
 // Kasai's carried length inside each chunk of kPlcpChunk positions, starting
 // from the exact value at the chunk start (src/libsais.c:8167 compute_plcp
-// restarts at block starts too).  A thread per chunk; Phi (read-only) and
-// PLCP are separate arrays, so the Phi sectors a lane walks stay in L1 while
-// its PLCP stores go out, and no shared memory limits the threads in flight
-// (each thread's steps form one dependent chain of text reads).
-constexpr uint32_t kPlcpChunk = 64;
+// restarts at block starts too).  A CTA stages the Phi values of its chunks
+// in shared memory with coalesced streaming loads (evict-first, so they do
+// not push the packed text out of L2), each thread walks its chunk -- one
+// dependent chain of text reads, so the short chunk keeps the shared memory
+// per chain small and many chains in flight -- and the PLCP values leave
+// coalesced, streamed as well.
+constexpr uint32_t kPlcpChunk = 32;
+constexpr int kKasaiThreads = 128;
+constexpr int kKasaiStride = kPlcpChunk + 1;   // padded rows: no bank conflicts
 
 template <typename Sym, bool GSA, int PB>
-__global__ void __launch_bounds__(256) k_plcp_kasai(TextWords tw, uint64_t n, uint64_t nchunks,
-                                                    const uint32_t *__restrict__ sparse,
-                                                    const uint32_t *__restrict__ phi, uint32_t *__restrict__ plcp,
-                                                    uint32_t *__restrict__ err)
+__global__ void __launch_bounds__(kKasaiThreads) k_plcp_kasai(TextWords tw, uint64_t n, uint64_t nchunks,
+                                                              const uint32_t *__restrict__ sparse,
+                                                              const uint32_t *__restrict__ phi,
+                                                              uint32_t *__restrict__ plcp, uint32_t *__restrict__ err)
 {
-    const uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nchunks) return;
-    const uint64_t a = k * kPlcpChunk;
-    const uint64_t e = a + kPlcpChunk < n ? a + kPlcpChunk : n;
-    uint64_t l = sparse[k];
-    plcp[a] = (uint32_t)l;
+    __shared__ uint32_t s[kKasaiThreads * kKasaiStride];
+    const uint64_t tile0 = (uint64_t)blockIdx.x * kKasaiThreads * kPlcpChunk;
+    for (uint32_t e = threadIdx.x; e < kKasaiThreads * kPlcpChunk; e += kKasaiThreads) {
+        const uint64_t x = tile0 + e;
+        if (x < n) s[(e / kPlcpChunk) * kKasaiStride + (e % kPlcpChunk)] = __ldcs(phi + x);
+    }
+    __syncthreads();
+    const uint64_t k = (uint64_t)blockIdx.x * kKasaiThreads + threadIdx.x;
     bool bad = false;
-    for (uint64_t x = a + 1; x < e; ++x) {
-        uint64_t b = __ldg(phi + x);
-        if (b > n) {
-            bad = true;
-            b = n;
+    if (k < nchunks) {
+        uint32_t *row = s + threadIdx.x * kKasaiStride;
+        const uint64_t a = k * kPlcpChunk;
+        const uint64_t e = a + kPlcpChunk < n ? a + kPlcpChunk : n;
+        uint64_t l = sparse[k];
+        row[0] = (uint32_t)l;
+        for (uint64_t x = a + 1; x < e; ++x) {
+            uint64_t b = row[x - a];
+            if (b > n) {
+                bad = true;
+                b = n;
+            }
+            if (b == n) {
+                l = 0;
+            } else {
+                l = l ? l - 1 : 0;
+                const uint64_t m = n - (x > b ? x : b);
+                if (l > m) l = m;
+                l = extend_thread<Sym, GSA, PB>(tw, x, b, l, m);
+            }
+            row[x - a] = (uint32_t)l;
         }
-        if (b == n) {
-            l = 0;
-        } else {
-            l = l ? l - 1 : 0;
-            const uint64_t m = n - (x > b ? x : b);
-            if (l > m) l = m;
-            l = extend_thread<Sym, GSA, PB>(tw, x, b, l, m);
-        }
-        plcp[x] = (uint32_t)l;
     }
     if (bad) atomicOr(err, GSAIS_ERR_BOUNDS);
+    __syncthreads();
+    for (uint32_t e = threadIdx.x; e < kKasaiThreads * kPlcpChunk; e += kKasaiThreads) {
+        const uint64_t x = tile0 + e;
+        if (x < n) __stcs(plcp + x, s[(e / kPlcpChunk) * kKasaiStride + (e % kPlcpChunk)]);
+    }
 }
 
 // LCP[i] = PLCP[SA[i]] (src/libsais.c:8311 compute_lcp).  Bytes: 12 per row.
@@ -607,8 +625,8 @@ cudaError_t plcp_run(const Sym *T, const uint32_t *SA, uint64_t n, uint32_t *plc
         GSAIS_COUNTED((k_plcp_long<Sym, GSA, PB><<<lg, 256, 0, st>>>(tw, n, phi, kPlcpChunk, sparse, long_list,
                                                                      counts + level)));
     }
-    GSAIS_COUNTED((k_plcp_kasai<Sym, GSA, PB><<<(unsigned)((nchunks + 255) / 256), 256, 0, st>>>(
-        tw, n, nchunks, sparse, phi, plcp, err)));
+    GSAIS_COUNTED((k_plcp_kasai<Sym, GSA, PB><<<(unsigned)((nchunks + kKasaiThreads - 1) / kKasaiThreads),
+                                                kKasaiThreads, 0, st>>>(tw, n, nchunks, sparse, phi, plcp, err)));
     return cudaGetLastError();
 }
 

@@ -1873,30 +1873,46 @@ __global__ void __launch_bounds__(256) k_chain_collect(const uint32_t *__restric
     }
 }
 
-// Every other link takes its chain end's outcome: the pair's order into SA
-// (and the seed round's list or ranks, as k_pair_compare writes them), or,
-// when the end stayed equal, back to the active list as a two-member group.
-__global__ void __launch_bounds__(256) k_chain_apply(const uint32_t *__restrict__ end, const uint8_t *__restrict__ outcome,
-                                                     const uint32_t *__restrict__ sx, const uint32_t *__restrict__ sy,
-                                                     const uint32_t *__restrict__ sP, uint64_t count, uint64_t n,
-                                                     uint32_t *__restrict__ sa, uint32_t *__restrict__ rank,
-                                                     uint32_t *__restrict__ list_pos, uint32_t *__restrict__ list_rank,
-                                                     uint32_t *__restrict__ slot0, uint32_t *__restrict__ out_i,
-                                                     uint32_t *__restrict__ out_pos, uint32_t *__restrict__ out_gid,
-                                                     uint32_t *__restrict__ gstart_out,
-                                                     unsigned long long *__restrict__ counter,
-                                                     uint32_t *__restrict__ err)
+// Every link's outcome to its place in the pair list (res[j], j = the pair's
+// index there): its chain end's outcome, or 3 for the ends themselves, which
+// the comparison has already written.  One byte per pair, written at random.
+__global__ void __launch_bounds__(256) k_chain_spread(const uint32_t *__restrict__ end, const uint8_t *__restrict__ outcome,
+                                                      const uint32_t *__restrict__ sv, uint64_t count,
+                                                      uint8_t *__restrict__ res)
 {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < count; q += stride) {
         const uint64_t e = end[q];
-        if (e == q) continue;   // compared directly
-        const uint32_t x = sx[q], y = sy[q], P = sP[q];
-        if (e >= count || x >= n || y >= n || (uint64_t)P + 1 >= n) {
+        const uint32_t j = sv[q];
+        if (j >= count) continue;
+        res[j] = e == q ? 3 : (e < count ? outcome[e] : 3);
+    }
+}
+
+// The other links in pair-list order (slot order, so SA and the seed round's
+// list are written near-sequentially, as k_pair_compare writes them): the
+// pair's order into SA and the list or ranks, or, when its chain end stayed
+// equal, back to the active list as a two-member group.
+__global__ void __launch_bounds__(256) k_chain_apply(const uint32_t *__restrict__ pairs, const uint8_t *__restrict__ res,
+                                                     uint64_t count, uint64_t n, uint32_t *__restrict__ sa,
+                                                     uint32_t *__restrict__ rank, uint32_t *__restrict__ list_pos,
+                                                     uint32_t *__restrict__ list_rank, uint32_t *__restrict__ slot0,
+                                                     uint32_t *__restrict__ out_i, uint32_t *__restrict__ out_pos,
+                                                     uint32_t *__restrict__ out_gid, uint32_t *__restrict__ gstart_out,
+                                                     unsigned long long *__restrict__ counter,
+                                                     uint32_t *__restrict__ err)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < count; j += stride) {
+        const uint8_t o = res[j];
+        if (o == 3) continue;   // a chain end: compared and written directly
+        const uint32_t P = pairs[j];
+        if ((uint64_t)P + 1 >= n) {
             atomicOr(err, GSAIS_ERR_BOUNDS);
             continue;
         }
-        const uint8_t o = outcome[e];
+        const uint32_t a = sa[P], b = sa[P + 1];
+        const uint32_t x = a < b ? a : b, y = a < b ? b : a;
         if (o == 2) {
             const unsigned long long r = atomicAdd(counter, (1ull << 32) | 2ull);
             const uint32_t cc = (uint32_t)r, g = (uint32_t)(r >> 32);
@@ -2546,9 +2562,10 @@ static cudaError_t run_seed_pair_chains(SortWorkspace &ws, const PairSource &ps,
                               list_rank, slot0, ws.counters + 6, list_q, outcome)) != cudaSuccess)
         return e;
     ev = prof ? prof->begin(st) : nullptr;
-    GSAIS_COUNTED((k_chain_apply<<<g, 256, 0, st>>>(end, outcome, sx, sy, sP, count, n, ws.sa, ws.rank, list_pos,
-                                                    list_rank, slot0, out_i, out_pos, out_gid, gstart_out,
-                                                    ws.counters, d_err)));
+    uint8_t *res = reinterpret_cast<uint8_t *>(sy);   // y is no longer needed
+    GSAIS_COUNTED((k_chain_spread<<<g, 256, 0, st>>>(end, outcome, sv, count, res)));
+    GSAIS_COUNTED((k_chain_apply<<<g, 256, 0, st>>>(pairs, res, count, n, ws.sa, ws.rank, list_pos, list_rank, slot0,
+                                                    out_i, out_pos, out_gid, gstart_out, ws.counters, d_err)));
     if (ev) prof->end(KK_PAIRS, ev, st, count * 28);
     *done = true;
     return cudaGetLastError();
