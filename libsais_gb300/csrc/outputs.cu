@@ -5,6 +5,7 @@
 // n before it is used as an address; a bad index raises GSAIS_ERR_BOUNDS in
 // the context's error word and the access is skipped, so a malformed caller
 // array becomes a -2 return instead of a device fault.
+#include <cstring>
 #include <type_traits>
 #include <vector>
 
@@ -621,13 +622,53 @@ cudaError_t plcp_run(const Sym *T, const uint32_t *SA, uint64_t n, uint32_t *plc
         const unsigned blocks = (unsigned)((count + 255) / 256);
         GSAIS_COUNTED((k_plcp_level<Sym, GSA, PB><<<blocks, 256, 0, st>>>(tw, n, phi, kPlcpChunk, nchunks, half,
                                                                            sparse, long_list, counts + level, err)));
-        const unsigned lg = (unsigned)(count < (uint64_t)sm_count() * 2 ? count : (uint64_t)sm_count() * 2);
+        // long extensions are few: a small persistent grid (mostly an empty launch)
+        const unsigned lg = (unsigned)(count < 64 ? count : 64);
         GSAIS_COUNTED((k_plcp_long<Sym, GSA, PB><<<lg, 256, 0, st>>>(tw, n, phi, kPlcpChunk, sparse, long_list,
                                                                      counts + level)));
     }
     GSAIS_COUNTED((k_plcp_kasai<Sym, GSA, PB><<<(unsigned)((nchunks + kKasaiThreads - 1) / kKasaiThreads),
                                                 kKasaiThreads, 0, st>>>(tw, n, nchunks, sparse, phi, plcp, err)));
     return cudaGetLastError();
+}
+
+// Which byte values occur in an 8-bit text: bit c of the 256-bit map (eight
+// words).  Each thread ORs its symbols into eight registers, a warp reduces
+// them, and a block does one atomicOr per word.  Bytes per symbol: 1 read.
+__global__ void __launch_bounds__(256) k_presence_u8(const uint8_t *__restrict__ T, uint64_t n,
+                                                     uint32_t *__restrict__ present)
+{
+    __shared__ uint32_t sm[8];
+    if (threadIdx.x < 8) sm[threadIdx.x] = 0;
+    __syncthreads();
+    uint32_t m[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    const uint64_t head = (16 - (reinterpret_cast<uintptr_t>(T) & 15)) & 15;
+    const uint64_t h = head < n ? head : n;
+    const uint64_t vecs = (n - h) / 16;
+    const uint4 *V = reinterpret_cast<const uint4 *>(T + h);
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < vecs; v += stride) {
+        const uint4 w = __ldcs(V + v);
+        const uint32_t words[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+                const uint32_t c = (words[q] >> (8 * b)) & 255u;
+                m[c >> 5] |= 1u << (c & 31);
+            }
+    }
+    if (blockIdx.x == 0 && threadIdx.x < 32) {   // the unaligned head and the tail
+        for (uint64_t i = threadIdx.x; i < h; i += 32) m[T[i] >> 5] |= 1u << (T[i] & 31);
+        for (uint64_t i = h + vecs * 16 + threadIdx.x; i < n; i += 32) m[T[i] >> 5] |= 1u << (T[i] & 31);
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const uint32_t r = __reduce_or_sync(GSAIS_FULL_MASK, m[q]);
+        if ((threadIdx.x & 31) == 0 && r) atomicOr(&sm[q], r);
+    }
+    __syncthreads();
+    if (threadIdx.x < 8 && sm[threadIdx.x]) atomicOr(&present[threadIdx.x], sm[threadIdx.x]);
 }
 
 // Packs an 8- or 16-bit text into dense 2- or 4-bit codes when its alphabet
@@ -641,8 +682,22 @@ cudaError_t pack_for_plcp(const Sym *T, uint64_t n, uint32_t *scratch, uint32_t 
     if (!h_hist || n < (1u << 16)) return cudaSuccess;   // small texts: the raw text is cache-resident anyway
     const PlcpLayout L = plcp_scratch_layout(n);
     const int nsym = sizeof(Sym) == 1 ? 256 : 65536;
-    cudaError_t e = symbol_histogram(T, (int)sizeof(Sym), n, scratch + L.o_hist, h_hist, st);
-    if (e != cudaSuccess) return e;
+    cudaError_t e;
+    if (sizeof(Sym) == 1) {
+        // only which symbols occur matters here: a 256-bit presence map
+        uint32_t *d_map = scratch + L.o_hist;
+        if ((e = cudaMemsetAsync(d_map, 0, 32, st)) != cudaSuccess) return e;
+        GSAIS_COUNTED((k_presence_u8<<<grid_for(n / 16 + 1, 256), 256, 0, st>>>(
+            reinterpret_cast<const uint8_t *>(T), n, d_map)));
+        if ((e = cudaMemcpyAsync(h_hist, d_map, 32, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+            (e = cudaStreamSynchronize(st)) != cudaSuccess)
+            return e;
+        uint32_t map[8];
+        std::memcpy(map, h_hist, 32);
+        for (int c = 0; c < 256; ++c) h_hist[c] = (map[c >> 5] >> (c & 31)) & 1u;
+    } else if ((e = symbol_histogram(T, (int)sizeof(Sym), n, scratch + L.o_hist, h_hist, st)) != cudaSuccess) {
+        return e;
+    }
     std::vector<uint16_t> codes(nsym, 0);
     uint32_t sigma = 0;
     for (int c = 0; c < nsym; ++c) {
