@@ -1571,13 +1571,8 @@ __global__ void __launch_bounds__(256) k_pair_compare(const uint32_t *__restrict
                                                       uint32_t *__restrict__ out_gid,
                                                       uint32_t *__restrict__ gstart_out,
                                                       unsigned long long *__restrict__ counter,
-                                                      uint32_t *__restrict__ err,
-                                                      const uint32_t *__restrict__ pair_tag,
-                                                      uint8_t *__restrict__ outcome)
+                                                      uint32_t *__restrict__ err)
 {
-    // pair_tag / outcome (optional): outcome[pair_tag[jj]] receives 0 when
-    // the first of the pair's two sorted members (the smaller position) is
-    // the smaller suffix, 1 when the other is, 2 when they are still equal
     constexpr uint32_t SPW = 32 / PB;   // symbols per 32-bit word
     constexpr uint32_t STEP = 4 * kPairBlocks * SPW;
     constexpr uint32_t CM = (1u << PB) - 1;
@@ -1587,7 +1582,7 @@ __global__ void __launch_bounds__(256) k_pair_compare(const uint32_t *__restrict
     const int lane = threadIdx.x & 31;
 
     bool live = false, finished = false, at_end = false;
-    uint32_t P = 0, a = 0, b = 0, rem = 0, tag = 0;   // rem: symbols left before `stop`
+    uint32_t P = 0, a = 0, b = 0, rem = 0;   // rem: symbols left before `stop`
     PairSide A{}, B{};
     auto init_side = [&](PairSide &s, uint64_t x) {
         const uint64_t q = x / SPW;   // word holding symbol x
@@ -1613,7 +1608,6 @@ __global__ void __launch_bounds__(256) k_pair_compare(const uint32_t *__restrict
                     finished = true;
                 } else {
                     P = pairs[jj];
-                    if (outcome) tag = pair_tag[jj];
                     const bool okp = (uint64_t)P + 1 < n;
                     a = okp ? sa[P] : 0u;
                     b = okp ? sa[P + 1] : 0u;
@@ -1664,7 +1658,6 @@ __global__ void __launch_bounds__(256) k_pair_compare(const uint32_t *__restrict
             }
         }
         if (res == 0) continue;
-        if (outcome) outcome[tag] = res == 2 ? 2 : (uint8_t)(((res < 0 ? a : b) < (res < 0 ? b : a)) ? 0 : 1);
         if (res != 2) {
             const uint32_t lo = res < 0 ? a : b, hi = res < 0 ? b : a;
             sa[P] = lo;
@@ -1690,253 +1683,6 @@ __global__ void __launch_bounds__(256) k_pair_compare(const uint32_t *__restrict
             gstart_out[g] = cc;
         }
         live = false;
-    }
-}
-
-// ---- chains of seed pairs.  A copied segment of length L makes L seed pairs
-// {x+k, y+k}, k = 0..L-1, and all of them are ordered alike: the two suffixes
-// first differ at the same text positions.  Pairs sorted by their smaller
-// member x put a chain's links next to each other (each position is in at
-// most one pair, so the pair holding x+1 is the next entry exactly when it
-// is {x+1, y+1}); only each chain's last link -- where the common prefix is
-// shortest -- is compared, and its outcome is copied back along the chain.
-constexpr int kChainTile = 4096;   // entries per CTA of the end-of-chain scan (256 x 16)
-
-// Per pair j: key = its smaller member (n for a malformed pair: sorts last),
-// value j.  Bytes per pair: 4 + 8 read, 8 written.
-__global__ void __launch_bounds__(256) k_chain_keys(const uint32_t *__restrict__ pairs, uint64_t count,
-                                                    const uint32_t *__restrict__ sa, uint64_t n,
-                                                    uint32_t *__restrict__ ck, uint32_t *__restrict__ cv)
-{
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < count; j += stride) {
-        const uint64_t P = pairs[j];
-        uint32_t x = (uint32_t)n;
-        if (P + 1 < n) {
-            const uint32_t a = sa[P], b = sa[P + 1];
-            if (a < n && b < n && a != b) x = a < b ? a : b;
-        }
-        ck[j] = x;
-        cv[j] = (uint32_t)j;
-    }
-}
-
-// In x order: the larger member y and the slot P of every pair, and the
-// chain breaks: brk[q] = q where the next entry is not {x+1, y+1}, else ~0.
-__global__ void __launch_bounds__(256) k_chain_y(const uint32_t *__restrict__ sx, const uint32_t *__restrict__ cv,
-                                                 uint64_t count, const uint32_t *__restrict__ pairs,
-                                                 const uint32_t *__restrict__ sa, uint64_t n,
-                                                 uint32_t *__restrict__ sy, uint32_t *__restrict__ sP)
-{
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < count; q += stride) {
-        const uint32_t P = pairs[cv[q]];
-        uint32_t y = (uint32_t)n;
-        if (sx[q] < n && (uint64_t)P + 1 < n) {
-            const uint32_t a = sa[P], b = sa[P + 1];
-            y = a > b ? a : b;
-        }
-        sy[q] = y;
-        sP[q] = P;
-    }
-}
-
-__global__ void __launch_bounds__(256) k_chain_breaks(const uint32_t *__restrict__ sx, const uint32_t *__restrict__ sy,
-                                                      uint64_t count, uint64_t n, uint32_t *__restrict__ brk)
-{
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < count; q += stride) {
-        const bool link = q + 1 < count && sx[q] < n && sx[q + 1] == sx[q] + 1 && sy[q + 1] == sy[q] + 1;
-        brk[q] = link ? 0xFFFFFFFFu : (uint32_t)q;
-    }
-}
-
-// end[q] = min over q' >= q of brk[q'] (the chain's last link), in three
-// steps: per-tile minima, their suffix minima over tiles, then per tile.
-__global__ void __launch_bounds__(256) k_chain_tile_min(const uint32_t *__restrict__ brk, uint64_t count,
-                                                        uint32_t *__restrict__ tile_min)
-{
-    __shared__ uint32_t s_w[8];
-    const uint64_t t0 = (uint64_t)blockIdx.x * kChainTile;
-    uint32_t m = 0xFFFFFFFFu;
-    for (int k = 0; k < kChainTile / 256; ++k) {
-        const uint64_t q = t0 + (uint64_t)k * 256 + threadIdx.x;
-        if (q < count) m = min(m, brk[q]);
-    }
-    m = __reduce_min_sync(GSAIS_FULL_MASK, m);
-    if ((threadIdx.x & 31) == 0) s_w[threadIdx.x >> 5] = m;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        uint32_t r = s_w[0];
-        for (int w = 1; w < 8; ++w) r = min(r, s_w[w]);
-        tile_min[blockIdx.x] = r;
-    }
-}
-
-__global__ void __launch_bounds__(1024) k_chain_tile_carry(const uint32_t *__restrict__ tile_min, uint64_t tiles,
-                                                           uint32_t *__restrict__ carry)
-{
-    // carry[t] = min over tiles after t; one CTA walks the tiles from the end
-    __shared__ uint32_t s_w[32];
-    __shared__ uint32_t s_run;
-    if (threadIdx.x == 0) s_run = 0xFFFFFFFFu;
-    __syncthreads();
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (uint64_t top = tiles; top > 0;) {
-        const uint64_t lo = top > 1024 ? top - 1024 : 0;
-        // thread i takes tile top - 1 - i (reverse order): inclusive prefix min
-        const uint64_t t = top - 1 - threadIdx.x;
-        uint32_t v = (threadIdx.x < top - lo) ? tile_min[t] : 0xFFFFFFFFu;
-        uint32_t inc = v;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t u = __shfl_up_sync(GSAIS_FULL_MASK, inc, o);
-            if (lane >= o) inc = min(inc, u);
-        }
-        if (lane == 31) s_w[warp] = inc;
-        __syncthreads();
-        uint32_t before = s_run;
-        for (int w = 0; w < warp; ++w) before = min(before, s_w[w]);
-        uint32_t exc = __shfl_up_sync(GSAIS_FULL_MASK, inc, 1);
-        exc = lane == 0 ? before : min(before, exc);
-        if (threadIdx.x < top - lo) carry[t] = exc;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            uint32_t r = s_run;
-            for (int w = 0; w < 32; ++w) r = min(r, s_w[w]);
-            s_run = r;
-        }
-        __syncthreads();
-        top = lo;
-    }
-}
-
-__global__ void __launch_bounds__(256) k_chain_ends(const uint32_t *__restrict__ brk, uint64_t count,
-                                                    const uint32_t *__restrict__ carry, uint32_t *__restrict__ end)
-{
-    // thread i holds entries [16 i, 16 i + 16) of the tile; suffix minima
-    // inside the thread, then over the threads after it (reverse scan)
-    constexpr int PER = kChainTile / 256;
-    __shared__ uint32_t s_w[8];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint64_t t0 = (uint64_t)blockIdx.x * kChainTile + (uint64_t)threadIdx.x * PER;
-    uint32_t v[PER];
-    uint32_t m = 0xFFFFFFFFu;
-#pragma unroll
-    for (int r = PER - 1; r >= 0; --r) {
-        const uint64_t q = t0 + r;
-        v[r] = q < count ? brk[q] : 0xFFFFFFFFu;
-        m = min(m, v[r]);
-        v[r] = m;   // suffix minimum inside the thread
-    }
-    // exclusive suffix minimum over the threads after this one
-    uint32_t inc = m;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t u = __shfl_down_sync(GSAIS_FULL_MASK, inc, o);
-        if (lane + o < 32) inc = min(inc, u);
-    }
-    if (lane == 0) s_w[warp] = inc;   // the warp's minimum
-    __syncthreads();
-    uint32_t after = carry[blockIdx.x];
-    for (int w = warp + 1; w < 8; ++w) after = min(after, s_w[w]);
-    uint32_t exc = __shfl_down_sync(GSAIS_FULL_MASK, inc, 1);
-    exc = lane == 31 ? after : min(after, exc);
-#pragma unroll
-    for (int r = 0; r < PER; ++r) {
-        const uint64_t q = t0 + r;
-        if (q < count) end[q] = min(v[r], exc);
-    }
-}
-
-// The chains' last links go to the comparison list (slot and entry index).
-__global__ void __launch_bounds__(256) k_chain_collect(const uint32_t *__restrict__ end, const uint32_t *__restrict__ sx,
-                                                       const uint32_t *__restrict__ sP, uint64_t count, uint64_t n,
-                                                       uint32_t *__restrict__ list_P, uint32_t *__restrict__ list_q,
-                                                       unsigned long long *__restrict__ list_count)
-{
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    const uint64_t c_round = (count + 31) & ~31ull;
-    for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < c_round; q += stride) {
-        const bool is_end = q < count && end[q] == q && sx[q] < n;
-        const uint32_t m = __ballot_sync(GSAIS_FULL_MASK, is_end);
-        if (!m) continue;
-        const int lead = __ffs(m) - 1;
-        unsigned long long base = 0;
-        if ((int)(threadIdx.x & 31) == lead) base = atomicAdd(list_count, (unsigned long long)__popc(m));
-        base = __shfl_sync(GSAIS_FULL_MASK, base, lead);
-        if (is_end) {
-            const uint64_t c = base + __popc(m & lanemask_lt());
-            list_P[c] = sP[q];
-            list_q[c] = (uint32_t)q;
-        }
-    }
-}
-
-// Every link's outcome to its place in the pair list (res[j], j = the pair's
-// index there): its chain end's outcome, or 3 for the ends themselves, which
-// the comparison has already written.  One byte per pair, written at random.
-__global__ void __launch_bounds__(256) k_chain_spread(const uint32_t *__restrict__ end, const uint8_t *__restrict__ outcome,
-                                                      const uint32_t *__restrict__ sv, uint64_t count,
-                                                      uint8_t *__restrict__ res)
-{
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < count; q += stride) {
-        const uint64_t e = end[q];
-        const uint32_t j = sv[q];
-        if (j >= count) continue;
-        res[j] = e == q ? 3 : (e < count ? outcome[e] : 3);
-    }
-}
-
-// The other links in pair-list order (slot order, so SA and the seed round's
-// list are written near-sequentially, as k_pair_compare writes them): the
-// pair's order into SA and the list or ranks, or, when its chain end stayed
-// equal, back to the active list as a two-member group.
-__global__ void __launch_bounds__(256) k_chain_apply(const uint32_t *__restrict__ pairs, const uint8_t *__restrict__ res,
-                                                     uint64_t count, uint64_t n, uint32_t *__restrict__ sa,
-                                                     uint32_t *__restrict__ rank, uint32_t *__restrict__ list_pos,
-                                                     uint32_t *__restrict__ list_rank, uint32_t *__restrict__ slot0,
-                                                     uint32_t *__restrict__ out_i, uint32_t *__restrict__ out_pos,
-                                                     uint32_t *__restrict__ out_gid, uint32_t *__restrict__ gstart_out,
-                                                     unsigned long long *__restrict__ counter,
-                                                     uint32_t *__restrict__ err)
-{
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < count; j += stride) {
-        const uint8_t o = res[j];
-        if (o == 3) continue;   // a chain end: compared and written directly
-        const uint32_t P = pairs[j];
-        if ((uint64_t)P + 1 >= n) {
-            atomicOr(err, GSAIS_ERR_BOUNDS);
-            continue;
-        }
-        const uint32_t a = sa[P], b = sa[P + 1];
-        const uint32_t x = a < b ? a : b, y = a < b ? b : a;
-        if (o == 2) {
-            const unsigned long long r = atomicAdd(counter, (1ull << 32) | 2ull);
-            const uint32_t cc = (uint32_t)r, g = (uint32_t)(r >> 32);
-            out_i[cc] = x;
-            out_i[cc + 1] = y;
-            out_pos[cc] = P;
-            out_pos[cc + 1] = P + 1;
-            out_gid[cc] = g;
-            out_gid[cc + 1] = g;
-            gstart_out[g] = cc;
-            continue;
-        }
-        const uint32_t lo = o == 0 ? x : y, hi = o == 0 ? y : x;
-        sa[P] = lo;
-        sa[P + 1] = hi;
-        if (slot0 && (lo == 0 || hi == 0)) *slot0 = P + (lo == 0 ? 1u : 2u);
-        if (list_rank) {
-            list_pos[P] = lo;
-            list_pos[P + 1] = hi;
-            list_rank[P + 1] = P + 2;
-        } else {
-            rank[lo] = P + 1;
-            rank[hi] = P + 2;
-        }
     }
 }
 
@@ -2438,22 +2184,19 @@ static cudaError_t run_pair_compare(SortWorkspace &ws, const PairSource &ps, con
                                     uint64_t skip, uint32_t *out_i, uint32_t *out_pos, uint32_t *out_gid,
                                     uint32_t *gstart_out, uint32_t *d_err, cudaStream_t st,
                                     uint32_t *list_pos = nullptr, uint32_t *list_rank = nullptr,
-                                    uint32_t *slot0 = nullptr, unsigned long long *pair_count = nullptr,
-                                    const uint32_t *pair_tag = nullptr, uint8_t *outcome = nullptr)
+                                    uint32_t *slot0 = nullptr)
 {
-    if (!pair_count) pair_count = ws.counters + 3;
+    unsigned long long *pair_count = ws.counters + 3;
     cudaEvent_t ev_pc = ws.radix.prof ? ws.radix.prof->begin(st) : nullptr;
     const unsigned grid = (unsigned)stream_grid(max_pairs, 256);
     if (ps.pack_bits == 2)
         GSAIS_COUNTED((k_pair_compare<2><<<grid, 256, 0, st>>>(pairs, pair_count, ws.counters + 4, ps.words, ps.n,
                                                               skip, kPairLimit, ws.sa, ws.rank, list_pos, list_rank,
-                                                              slot0, out_i, out_pos, out_gid, gstart_out, ws.counters, d_err,
-                                                              pair_tag, outcome)));
+                                                              slot0, out_i, out_pos, out_gid, gstart_out, ws.counters, d_err)));
     else
         GSAIS_COUNTED((k_pair_compare<4><<<grid, 256, 0, st>>>(pairs, pair_count, ws.counters + 4, ps.words, ps.n,
                                                               skip, kPairLimit, ws.sa, ws.rank, list_pos, list_rank,
-                                                              slot0, out_i, out_pos, out_gid, gstart_out, ws.counters, d_err,
-                                                              pair_tag, outcome)));
+                                                              slot0, out_i, out_pos, out_gid, gstart_out, ws.counters, d_err)));
     if (ev_pc) ws.radix.prof->end(KK_PAIRS, ev_pc, st, 0);
     return cudaGetLastError();
 }
@@ -2511,63 +2254,6 @@ static cudaError_t large_few_others(SortWorkspace &ws, uint64_t NL, uint64_t LG,
                                                                           d_err)));
     }
     S.few_rounds += 1;
-    return cudaGetLastError();
-}
-
-// The seed round's tied pairs, ordered along their chains: sorted by their
-// smaller member, chain ends found by adjacency, only the ends compared
-// (k_pair_compare with an outcome per end), the outcome copied to every other
-// link.  Uses buffers the seed round has consumed: keys[w] (the sorted seed
-// keys), lvals[0..1] and lpos.  Returns false (nothing done) when the pairs
-// are too few to pay for the sort or do not fit those buffers.
-static cudaError_t run_seed_pair_chains(SortWorkspace &ws, const PairSource &ps, const uint32_t *pairs,
-                                        uint64_t count, uint64_t n, int w, uint64_t skip, uint32_t *out_i,
-                                        uint32_t *out_pos, uint32_t *out_gid, uint32_t *gstart_out,
-                                        uint32_t *list_pos, uint32_t *list_rank, uint32_t *slot0, uint32_t *d_err,
-                                        cudaStream_t st, SortStats &S, bool *done)
-{
-    cudaError_t e;
-    *done = false;
-    const uint64_t hc = (count + 63) & ~63ull;
-    const uint64_t tiles = (count + kChainTile - 1) / kChainTile;
-    if (count < (1u << 16) || 2 * hc > n || 2 * tiles + 64 > 5 * few_group_words(ws.n_cap)) return cudaSuccess;
-    KernelProfiler *prof = ws.radix.prof;
-    cudaEvent_t ev = prof ? prof->begin(st) : nullptr;
-    uint32_t *ck[2] = {ws.lvals[0], ws.lvals[0] + hc};
-    uint32_t *cv[2] = {ws.lvals[1], ws.lvals[1] + hc};
-    uint32_t *sy = ws.lpos, *sP = ws.lpos + hc;
-    uint32_t *K32 = reinterpret_cast<uint32_t *>(ws.keys[w]);
-    uint32_t *end = K32, *list_P = K32 + hc, *list_q = K32 + 2 * hc;
-    uint32_t *tile_min = ws.few, *carry = ws.few + tiles + 32;
-    const unsigned g = (unsigned)stream_grid(count, 256);
-    GSAIS_COUNTED((k_chain_keys<<<g, 256, 0, st>>>(pairs, count, ws.sa, n, ck[0], cv[0])));
-    int which = 0, ran = 0;
-    if ((e = radix_sort_pairs32(ck, cv, count, gsais_bits_for(n), ws.radix, d_err, st, &which, &ran, false)) !=
-        cudaSuccess)
-        return e;
-    S.radix_passes += ran;
-    const uint32_t *sx = ck[which], *sv = cv[which];
-    uint32_t *brk = ck[which ^ 1];
-    uint8_t *outcome = reinterpret_cast<uint8_t *>(cv[which ^ 1]);
-    GSAIS_COUNTED((k_chain_y<<<g, 256, 0, st>>>(sx, sv, count, pairs, ws.sa, n, sy, sP)));
-    GSAIS_COUNTED((k_chain_breaks<<<g, 256, 0, st>>>(sx, sy, count, n, brk)));
-    GSAIS_COUNTED((k_chain_tile_min<<<(unsigned)tiles, 256, 0, st>>>(brk, count, tile_min)));
-    GSAIS_COUNTED((k_chain_tile_carry<<<1, 1024, 0, st>>>(tile_min, tiles, carry)));
-    GSAIS_COUNTED((k_chain_ends<<<(unsigned)tiles, 256, 0, st>>>(brk, count, carry, end)));
-    if ((e = cudaMemsetAsync(ws.counters + 6, 0, sizeof(unsigned long long), st)) != cudaSuccess) return e;
-    GSAIS_COUNTED((k_chain_collect<<<g, 256, 0, st>>>(end, sx, sP, count, n, list_P, list_q, ws.counters + 6)));
-    if (ev) prof->end(KK_PAIRS, ev, st, count * 56);
-    // the chain ends, compared directly; every end gets an outcome
-    if ((e = run_pair_compare(ws, ps, list_P, count, skip, out_i, out_pos, out_gid, gstart_out, d_err, st, list_pos,
-                              list_rank, slot0, ws.counters + 6, list_q, outcome)) != cudaSuccess)
-        return e;
-    ev = prof ? prof->begin(st) : nullptr;
-    uint8_t *res = reinterpret_cast<uint8_t *>(sy);   // y is no longer needed
-    GSAIS_COUNTED((k_chain_spread<<<g, 256, 0, st>>>(end, outcome, sv, count, res)));
-    GSAIS_COUNTED((k_chain_apply<<<g, 256, 0, st>>>(pairs, res, count, n, ws.sa, ws.rank, list_pos, list_rank, slot0,
-                                                    out_i, out_pos, out_gid, gstart_out, ws.counters, d_err)));
-    if (ev) prof->end(KK_PAIRS, ev, st, count * 28);
-    *done = true;
     return cudaGetLastError();
 }
 
@@ -2939,19 +2625,7 @@ cudaError_t suffix_sort(const void *d_T, int symbytes, uint64_t n, bool gsa, Sor
         if ((e = cudaMemcpyAsync(ws.counters, h, sizeof(unsigned long long), cudaMemcpyHostToDevice, st)) !=
             cudaSuccess)
             return e;
-        bool chained = false;
-        if (opt.pair_chains) {
-            if ((e = read_back(ws.h_small, ws.counters + 3, sizeof(unsigned long long), st)) != cudaSuccess ||
-                (e = cudaStreamSynchronize(st)) != cudaSuccess)
-                return e;
-            const uint64_t npairs = reinterpret_cast<const unsigned long long *>(ws.h_small)[0];
-            if ((e = run_seed_pair_chains(ws, ps, a.pairs, npairs, n, w, (uint64_t)K, ws.vals[av], ws.pos[pg],
-                                          ws.gid[pg], ws.gstart[pg], a.rank_out ? ws.vals[w] : nullptr, a.rank_out,
-                                          ws.slot0, d_err, st, S, &chained)) != cudaSuccess)
-                return e;
-        }
-        if (!chained &&
-            (e = run_pair_compare(ws, ps, a.pairs, n / 2, (uint64_t)K, ws.vals[av], ws.pos[pg], ws.gid[pg],
+        if ((e = run_pair_compare(ws, ps, a.pairs, n / 2, (uint64_t)K, ws.vals[av], ws.pos[pg], ws.gid[pg],
                                   ws.gstart[pg], d_err, st, a.rank_out ? ws.vals[w] : nullptr, a.rank_out,
                                   ws.slot0)) != cudaSuccess)
             return e;

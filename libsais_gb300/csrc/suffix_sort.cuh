@@ -89,7 +89,6 @@ struct SortOptions {
     uint32_t raw_max = 0;     // 32-bit integer symbols: the largest symbol value
     EarlySaCopy *early = nullptr;
     bool hist_ready = false;  // ws.hist already holds the symbol histogram (symbol_histogram_part)
-    bool pair_chains = true;  // seed pairs ordered along chains of copies (one comparison per chain)
 };
 
 // Queues on `st`, behind the bulk copy (ec.copied), the writes of the
