@@ -526,10 +526,18 @@ def sa_bwt(T, width=4, freq=True, ctx=None):
     return int(rc), SA[:n], U[:n], F
 
 
+_CUDA_STREAM_LEGACY = 1   # cudaStreamLegacy
+
+
 def _stream_handle(stream):
+    """None: the context's own stream.  A torch stream (or a raw handle): that
+    stream; torch's default stream has handle 0, which the C entry points
+    read as "the context's stream", so it is passed as cudaStreamLegacy to
+    keep the call ordered after the work already queued there."""
     if stream is None:
         return None
-    return getattr(stream, "cuda_stream", stream)
+    h = getattr(stream, "cuda_stream", stream)
+    return _CUDA_STREAM_LEGACY if h == 0 and hasattr(stream, "cuda_stream") else h
 
 
 def sa_device(T, SA, gsa=False, ctx=None, stream=None):

@@ -571,13 +571,15 @@ int64_t gsais_run_lcp(gsais_ctx *c, const void *PLCP, const void *SA, void *LCP,
     if (!ctx_init(c)) return fail(cudaErrorUnknown);
     DeviceGuard g(c->device);
     cudaStream_t st = c->stream;
-    const size_t total = 3 * align_up(n * 4) + (idx_bytes == 8 ? align_up(n * 8) : 0);
+    const size_t total = 3 * align_up(n * 4) + (idx_bytes == 8 ? align_up(n * 8) : 0) +
+                         align_up(lcp_scratch_words(n) * 4);
     if (!ensure_arena(c, total)) return -2;
     Carver cv(c->arena);
     uint32_t *d_P = cv.take<uint32_t>(n);
     uint32_t *d_SA = cv.take<uint32_t>(n);
     uint32_t *d_L = cv.take<uint32_t>(n);
     int64_t *d_wide = idx_bytes == 8 ? cv.take<int64_t>(n) : nullptr;
+    uint32_t *d_scratch = lcp_scratch_words(n) ? cv.take<uint32_t>(lcp_scratch_words(n)) : nullptr;
     if (!clear_err(c, st)) return fail(cudaErrorUnknown);
     if (idx_bytes == 8) {
         GS_TRY(cudaMemcpyAsync(d_wide, PLCP, n * 8, cudaMemcpyHostToDevice, st));
@@ -588,7 +590,7 @@ int64_t gsais_run_lcp(gsais_ctx *c, const void *PLCP, const void *SA, void *LCP,
         GS_TRY(cudaMemcpyAsync(d_P, PLCP, n * 4, cudaMemcpyHostToDevice, st));
         GS_TRY(cudaMemcpyAsync(d_SA, SA, n * 4, cudaMemcpyHostToDevice, st));
     }
-    GS_TRY(lcp_gather(d_P, d_SA, d_L, n, c->d_misc, st));
+    GS_TRY(lcp_gather(d_P, d_SA, d_L, n, d_scratch, c->d_misc, st));
     if (idx_bytes == 8) {
         GS_TRY(widen_u32_to_i64(d_L, d_wide, n, st));
         GS_TRY(cudaMemcpyAsync(LCP, d_wide, n * 8, cudaMemcpyDeviceToHost, st));
@@ -702,16 +704,20 @@ int64_t gsais_lcp_device(void *ctx, const void *PLCP, const void *SA, void *LCP,
     DeviceGuard g(c->device);
     cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : c->stream;
     if (!clear_err(c, st)) return fail(cudaErrorUnknown);
+    const size_t sw = lcp_scratch_words(n);
     if (idx_bytes == 4) {
+        if (sw && !ensure_arena(c, align_up(sw * 4))) return -2;
+        uint32_t *scratch = sw ? Carver(c->arena).take<uint32_t>(sw) : nullptr;
         GS_TRY(lcp_gather(static_cast<const uint32_t *>(PLCP), static_cast<const uint32_t *>(SA),
-                          static_cast<uint32_t *>(LCP), n, c->d_misc, st));
+                          static_cast<uint32_t *>(LCP), n, scratch, c->d_misc, st));
     } else {
-        if (!ensure_arena(c, 3 * align_up(n * 4))) return -2;
+        if (!ensure_arena(c, 3 * align_up(n * 4) + align_up(sw * 4))) return -2;
         Carver cv(c->arena);
         uint32_t *p = cv.take<uint32_t>(n), *s = cv.take<uint32_t>(n), *l = cv.take<uint32_t>(n);
+        uint32_t *scratch = sw ? cv.take<uint32_t>(sw) : nullptr;
         GS_TRY(narrow_i64_to_u32(static_cast<const int64_t *>(PLCP), p, n, c->d_misc, st));
         GS_TRY(narrow_i64_to_u32(static_cast<const int64_t *>(SA), s, n, c->d_misc, st));
-        GS_TRY(lcp_gather(p, s, l, n, c->d_misc, st));
+        GS_TRY(lcp_gather(p, s, l, n, scratch, c->d_misc, st));
         GS_TRY(widen_u32_to_i64(l, static_cast<int64_t *>(LCP), n, st));
     }
     GS_TRY(sync_checked(c, st));

@@ -52,8 +52,10 @@ cudaError_t int_alphabet_scan(const void *d_T, int tbytes, uint64_t n, int64_t k
 // Integer symbols copied to obytes-wide unsigned symbols (values already checked to fit).
 cudaError_t int_narrow(const void *d_T, int tbytes, uint64_t n, void *d_out, int obytes, cudaStream_t st);
 
-// LCP[i] = PLCP[SA[i]].
-cudaError_t lcp_gather(const uint32_t *d_PLCP, const uint32_t *d_SA, uint32_t *d_LCP, uint64_t n, uint32_t *err,
-                       cudaStream_t st);
+// LCP[i] = PLCP[SA[i]].  scratch: lcp_scratch_words(n) words (0 for texts
+// whose PLCP array stays in L2; a null scratch takes the direct gather).
+size_t lcp_scratch_words(uint64_t n);
+cudaError_t lcp_gather(const uint32_t *d_PLCP, const uint32_t *d_SA, uint32_t *d_LCP, uint64_t n, uint32_t *scratch,
+                       uint32_t *err, cudaStream_t st);
 
 }  // namespace gsais

@@ -305,6 +305,32 @@ def test_lcp_may_alias_sa(oracle):
     assert rc == 0 and np.array_equal(buf.astype(np.int64), expect)
 
 
+@pytest.mark.parametrize("n", [(1 << 24) + 12345, 1 << 26, (1 << 26) + 12345])
+def test_lcp_partitioned_gather(n):
+    """From 2^26 rows on, LCP[i] = PLCP[SA[i]] goes through position buckets
+    (partition, in-place fetch, place); below, a direct gather.  Checked
+    against plain indexing on any permutation and any PLCP values, in place
+    over SA, for int64 arrays and through the host entry point."""
+    torch = pytest.importorskip("torch")
+    g = torch.Generator(device="cuda").manual_seed(n)
+    dSA = torch.randperm(n, device="cuda", generator=g).to(torch.int32)
+    dP = torch.randint(0, n, (n,), device="cuda", generator=g, dtype=torch.int32)   # PLCP values are < n
+    expect = dP[dSA.long()]
+    st = torch.cuda.current_stream()   # the inputs were made on this stream
+    dL = torch.full_like(dSA, -1)
+    assert G.lcp_device(dP, dSA, dL, stream=st) == 0
+    assert torch.equal(dL, expect)
+    buf = dSA.clone()
+    assert G.lcp_device(dP, buf, buf, stream=st) == 0   # LCP may be the SA buffer
+    assert torch.equal(buf, expect)
+    dL64 = torch.empty(n, dtype=torch.int64, device="cuda")
+    assert G.lcp_device(dP.long(), dSA.long(), dL64, stream=st) == 0
+    assert torch.equal(dL64, expect.long())
+    if n == (1 << 26) + 12345:
+        rc, L = G.libsais_lcp(dP.cpu().numpy(), dSA.cpu().numpy())
+        assert rc == 0 and np.array_equal(L, expect.cpu().numpy())
+
+
 def test_combined_sa_bwt(oracle):
     T = textgen.genome_like(1 << 20, seed=12)
     prim, SA, U, F = G.sa_bwt(T)
