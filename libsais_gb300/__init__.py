@@ -186,7 +186,7 @@ class GsaisTuning(ctypes.Structure):
                 ("medium_max", _i32), ("large_few_others", _i32)]
 
 
-TUNING_DEFAULTS = {"digit_bits": 8, "radix_items32": 24, "radix_items64": 16, "medium_small": 512,
+TUNING_DEFAULTS = {"digit_bits": 8, "radix_items32": 20, "radix_items64": 16, "medium_small": 512,
                    "medium_max": 4096, "large_few_others": 1}
 
 

@@ -44,7 +44,7 @@ CANDIDATES = {
     "medium_max": [1024, 2048, 4096],
     "large_few_others": [1, 0],
 }
-DEFAULTS = {"digit_bits": 8, "radix_items32": 24, "radix_items64": 16, "medium_small": 512, "medium_max": 4096,
+DEFAULTS = {"digit_bits": 8, "radix_items32": 20, "radix_items64": 16, "medium_small": 512, "medium_max": 4096,
             "large_few_others": 1}
 
 

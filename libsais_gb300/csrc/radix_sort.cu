@@ -230,11 +230,26 @@ __global__ void __launch_bounds__(PassShape<K, ITEMS>::kThreads, PassShape<K, IT
     // ---- rank inside each warp, in input order (stable).  Lanes with equal
     // digits are found with eight ballots; the lowest such lane advances the
     // warp's counter for that digit after every lane has read it.
+    // The implicit-value pass is the first pass that moves entries: its input
+    // order only matters among equal keys, which the doubling rounds order
+    // later, except for the suffixes shorter than a seed (the first slots,
+    // in tile 0), whose padded keys tie with longer suffixes and must stay
+    // first.  So its other tiles rank by shared-memory atomics (unstable).
     K kr[ITEMS];
     uint32_t vr[ITEMS];
     uint16_t rk[ITEMS];
     const int wbase = warp * ITEMS * 32;
-    if (full) {
+    if (full && implicit && tile != 0) {
+#pragma unroll
+        for (int k = 0; k < ITEMS; ++k) {
+            const int idx = wbase + k * 32 + lane;
+            const K key = s_keys[idx];
+            kr[k] = key;
+            vr[k] = vbase - (uint32_t)idx;
+            const uint32_t d = (uint32_t)(key >> shift) & mask;
+            rk[k] = (uint16_t)atomicAdd(&s_whist[warp][d], 1u);
+        }
+    } else if (full) {
 #pragma unroll
         for (int k = 0; k < ITEMS; ++k) {
             const int idx = wbase + k * 32 + lane;

@@ -6,7 +6,7 @@ namespace gsais {
 
 struct Tuning {
     int digit_bits = 8;        // radix digit width (the compiled passes rank 8-bit digits)
-    int radix_items32 = 24;    // keys per thread of a digit pass over 32-bit keys: 16, 20, 24, 28
+    int radix_items32 = 20;    // keys per thread of a digit pass over 32-bit keys: 16, 20, 24, 28
     int radix_items64 = 16;    // the same for 64-bit keys: 12, 16, 20
     int medium_small = 512;    // groups of 33..medium_small members: 128-thread CTA sort
     int medium_max = 4096;     // groups up to medium_max: 256-thread CTA sort; larger: global radix sort

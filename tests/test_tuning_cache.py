@@ -10,7 +10,7 @@ from libsais_gb300 import autotune
 def test_cache_round_trip(tmp_path):
     path = str(tmp_path / "t.json")
     good = dict(autotune.DEFAULTS, gpu="NVIDIA GB300", n_log2=28, bits=2, ms=16.9)
-    other = dict(good, radix_items32=20, n_log2=20)
+    other = dict(good, radix_items32=16, n_log2=20)
     bad = dict(good, radix_items32=17, n_log2=24)   # no such instance: skipped when loaded
     autotune.write_cache(path, good)
     autotune.write_cache(path, other)
