@@ -401,6 +401,68 @@ __global__ void __launch_bounds__(256) k_plcp_level(TextWords tw, uint64_t n, co
     }
 }
 
+// The same level with a warp per chunk start, for the levels whose bounds come
+// from far away (half * chunk symbols back: the bound is loose and the start
+// extends by about its whole PLCP value): lane j compares two windows at
+// l + j * (two windows), so a step covers 32 x 2 windows and most starts
+// finish in one step instead of a chain of dependent window reads.  Starts
+// still matching after kLevelWarpSteps steps go to the long list.
+constexpr int kLevelWarpSteps = 4;
+
+template <typename Sym, bool GSA, int PB>
+__global__ void __launch_bounds__(256) k_plcp_level_warp(TextWords tw, uint64_t n, const uint32_t *__restrict__ phi,
+                                                         uint32_t chunk, uint64_t nchunks, uint64_t half,
+                                                         uint32_t *__restrict__ sparse,
+                                                         uint2 *__restrict__ long_list,
+                                                         uint32_t *__restrict__ long_count,
+                                                         uint32_t *__restrict__ err)
+{
+    constexpr int PER2 = 2 * 64 / SymBits<Sym, PB>::value;
+    const int lane = threadIdx.x & 31;
+    const uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t k = (2 * w + 1) * half;
+    if (k >= nchunks) return;   // the same for the whole warp
+    const uint64_t a = k * chunk;
+    uint64_t b = phi[a];
+    if (b > n) {
+        if (lane == 0) atomicOr(err, GSAIS_ERR_BOUNDS);
+        b = n;
+    }
+    uint64_t l = 0;
+    bool done = true;
+    if (b != n) {
+        const uint64_t kp = k - half;
+        const uint64_t d = a - kp * chunk;
+        const uint64_t lp = sparse[kp];
+        const uint64_t m = n - (a > b ? a : b);
+        l = lp > d ? lp - d : 0;
+        if (l > m) l = m;
+        done = false;
+        for (int it = 0; it < kLevelWarpSteps; ++it) {
+            // lane_window is 0 at or past m, so the first such lane ends the scan at m
+            const uint64_t o = l + (uint64_t)lane * PER2;
+            const uint32_t c = lane_window<Sym, GSA, PB>(tw, a, b, o, m);
+            const uint32_t stop = __ballot_sync(GSAIS_FULL_MASK, c < (uint32_t)PER2);
+            if (stop) {
+                const int f = __ffs(stop) - 1;
+                l += (uint64_t)f * PER2 + __shfl_sync(GSAIS_FULL_MASK, c, f);
+                if (l > m) l = m;
+                done = true;
+                break;
+            }
+            l += 32ull * PER2;
+        }
+    }
+    if (lane == 0) {
+        if (done) {
+            sparse[k] = (uint32_t)l;
+        } else {
+            const uint32_t slot = atomicAdd(long_count, 1u);
+            long_list[slot] = make_uint2((uint32_t)k, (uint32_t)l);
+        }
+    }
+}
+
 // The long extensions of one level: a CTA per listed start, 256 threads x two
 // windows per step.
 template <typename Sym, bool GSA, int PB>
@@ -858,11 +920,20 @@ cudaError_t plcp_run(const Sym *T, const uint32_t *SA, uint64_t n, uint32_t *plc
     for (uint64_t half = top >> 1; half >= 1; half >>= 1, ++level) {
         const uint64_t count = nchunks > half ? (nchunks - half + 2 * half - 1) / (2 * half) : 0;
         if (count == 0) continue;
-        const unsigned blocks = (unsigned)((count + 255) / 256);
-        GSAIS_COUNTED((k_plcp_level<Sym, GSA, PB><<<blocks, 256, 0, st>>>(tw, n, phi, kPlcpChunk, nchunks, half,
-                                                                           sparse, long_list, counts + level, err)));
-        // long extensions are few: a small persistent grid (mostly an empty launch)
-        const unsigned lg = (unsigned)(count < 64 ? count : 64);
+        if (half * kPlcpChunk > 256) {   // loose bounds: a warp per start
+            const unsigned blocks = (unsigned)((count + 7) / 8);
+            GSAIS_COUNTED((k_plcp_level_warp<Sym, GSA, PB><<<blocks, 256, 0, st>>>(
+                tw, n, phi, kPlcpChunk, nchunks, half, sparse, long_list, counts + level, err)));
+        } else {
+            const unsigned blocks = (unsigned)((count + 255) / 256);
+            GSAIS_COUNTED((k_plcp_level<Sym, GSA, PB><<<blocks, 256, 0, st>>>(
+                tw, n, phi, kPlcpChunk, nchunks, half, sparse, long_list, counts + level, err)));
+        }
+        // the long list is empty at most levels and holds thousands of starts
+        // at the last ones: a grid-stride loop over it, CTAs that find no
+        // entry exit at once
+        const uint64_t lcap = (uint64_t)sm_count() * 8;
+        const unsigned lg = (unsigned)(count < lcap ? count : lcap);
         GSAIS_COUNTED((k_plcp_long<Sym, GSA, PB><<<lg, 256, 0, st>>>(tw, n, phi, kPlcpChunk, sparse, long_list,
                                                                      counts + level)));
     }
