@@ -800,6 +800,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--seed-key-bits", type=int, default=0)
     ap.add_argument("--no-extras", action="store_true", help="skip the measurements beside the headline")
+    ap.add_argument("--extras", default="all",
+                    help="comma-separated subset of plcp_lcp,unbwt,stress,gsa,batched,serving (default all)")
     ap.add_argument("--batch-strings", type=int, default=4096)
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (built-in tuning defaults)")
     ap.add_argument("--serving-jobs", type=int, default=20000, help="jobs per arrival rate of the serving stream")
@@ -962,22 +964,31 @@ def main():
         cpu = cpu_baseline_child(name, n)
 
     extras = {}
+    want = {"plcp_lcp", "unbwt", "stress", "gsa", "batched", "serving"}
+    if args.extras != "all":
+        want &= set(args.extras.split(","))
     if rank == 0 and world == 1 and not args.no_extras:
         from oracle.oracle import Oracle
         O = Oracle()
-        extras["plcp_lcp"] = run_plcp_lcp(G, torch, dT, dSA, n, T, O)
-        extras["unbwt"] = run_unbwt(G, dU.cpu().numpy(), prim, T)
+        if "plcp_lcp" in want:
+            extras["plcp_lcp"] = run_plcp_lcp(G, torch, dT, dSA, n, T, O)
+        if "unbwt" in want:
+            extras["unbwt"] = run_unbwt(G, dU.cpu().numpy(), prim, T)
         del dT, dSA, dU
         G.release_workspace()
         torch.cuda.empty_cache()
-        extras["stress"] = run_stress(G, torch)
-        extras["gsa"] = run_gsa(G, torch)
+        if "stress" in want:
+            extras["stress"] = run_stress(G, torch)
+        if "gsa" in want:
+            extras["gsa"] = run_gsa(G, torch)
         G.release_workspace()
-        extras["batched"] = run_batched(G, torch, count=args.batch_strings)
+        if "batched" in want:
+            extras["batched"] = run_batched(G, torch, count=args.batch_strings)
         G.release_workspace()
         torch.cuda.empty_cache()
-        extras["serving"] = run_serving(G, torch, jobs_per_rate=args.serving_jobs)
-        extras["serving"]["cpu_reference"] = serving_cpu_child(40, args.serving_jobs)
+        if "serving" in want:
+            extras["serving"] = run_serving(G, torch, jobs_per_rate=args.serving_jobs)
+            extras["serving"]["cpu_reference"] = serving_cpu_child(40, args.serving_jobs)
 
     if rank == 0:
         line = {

@@ -503,6 +503,98 @@ __global__ void __launch_bounds__(1024) k_tile_scan(const uint32_t *__restrict__
     }
 }
 
+// The same scan over many CTAs (the seed round has up to 2^21 assign tiles, a
+// long sequential pass for one CTA): k_scan_up reduces kScanSpan tiles per
+// CTA, k_scan_top scans those aggregates from the base (one CTA), k_scan_down
+// rescans each CTA's tiles from its aggregate's prefix.  agg holds the
+// aggregates, then their prefixes.
+constexpr int kScanThreads = 256, kScanPer = 8, kScanSpan = kScanThreads * kScanPer;
+
+__device__ __forceinline__ void scan_load(const uint4 *in4, uint64_t tiles, uint64_t t0, uint4 (&x)[kScanPer],
+                                          uint32_t &m, uint32_t &k, uint32_t &h, uint32_t &p)
+{
+    m = k = h = p = 0;
+#pragma unroll
+    for (int i = 0; i < kScanPer; ++i) {
+        x[i] = t0 + i < tiles ? in4[t0 + i] : make_uint4(0, 0, 0, 0);
+        m = lastnz(m, x[i].x);
+        k += x[i].y;
+        h += x[i].z;
+        p += x[i].w;
+    }
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_up(const uint32_t *__restrict__ info, uint64_t tiles,
+                                                          uint4 *__restrict__ agg)
+{
+    __shared__ uint32_t wb[4][kScanThreads / 32 + 1];
+    const uint64_t t0 = (uint64_t)blockIdx.x * kScanSpan + (uint64_t)threadIdx.x * kScanPer;
+    uint4 x[kScanPer];
+    uint32_t m, k, h, p, tm, tk, th, tp;
+    scan_load(reinterpret_cast<const uint4 *>(info), tiles, t0, x, m, k, h, p);
+    block_exclusive_lastnz<kScanThreads>(m, wb[0], tm);
+    block_exclusive_sum<uint32_t, kScanThreads>(k, wb[1], tk);
+    block_exclusive_sum<uint32_t, kScanThreads>(h, wb[2], th);
+    block_exclusive_sum<uint32_t, kScanThreads>(p, wb[3], tp);
+    if (threadIdx.x == 0) agg[blockIdx.x] = make_uint4(tm, tk, th, tp);
+}
+
+__global__ void __launch_bounds__(1024) k_scan_top(uint4 *__restrict__ agg, uint32_t blocks,
+                                                   uint32_t *__restrict__ totals,
+                                                   const unsigned long long *__restrict__ base,
+                                                   unsigned long long *__restrict__ pair_total)
+{
+    __shared__ uint32_t wb[4][33];
+    const unsigned long long b0 = base ? *base : 0ull;
+    uint32_t cm = 0, ck = (uint32_t)b0, ch = (uint32_t)(b0 >> 32), cp = 0;
+    for (uint32_t c0 = 0; c0 < blocks; c0 += 1024) {
+        const uint32_t i = c0 + threadIdx.x;
+        const uint4 x = i < blocks ? agg[i] : make_uint4(0, 0, 0, 0);
+        uint32_t tm, tk, th, tp;
+        const uint32_t em = block_exclusive_lastnz<1024>(x.x, wb[0], tm);
+        const uint32_t ek = block_exclusive_sum<uint32_t, 1024>(x.y, wb[1], tk);
+        const uint32_t eh = block_exclusive_sum<uint32_t, 1024>(x.z, wb[2], th);
+        const uint32_t ep = block_exclusive_sum<uint32_t, 1024>(x.w, wb[3], tp);
+        if (i < blocks) agg[blocks + i] = make_uint4(lastnz(cm, em), ck + ek, ch + eh, cp + ep);
+        cm = lastnz(cm, tm);
+        ck += tk;
+        ch += th;
+        cp += tp;
+    }
+    if (threadIdx.x == 0) {
+        totals[0] = ck;
+        totals[1] = ch;
+        if (pair_total) *pair_total = cp;
+    }
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_down(const uint32_t *__restrict__ info, uint64_t tiles,
+                                                            const uint4 *__restrict__ prefix,
+                                                            uint32_t *__restrict__ carry)
+{
+    __shared__ uint32_t wb[4][kScanThreads / 32 + 1];
+    const uint64_t t0 = (uint64_t)blockIdx.x * kScanSpan + (uint64_t)threadIdx.x * kScanPer;
+    uint4 x[kScanPer];
+    uint32_t m, k, h, p, tm, tk, th, tp;
+    scan_load(reinterpret_cast<const uint4 *>(info), tiles, t0, x, m, k, h, p);
+    const uint32_t em = block_exclusive_lastnz<kScanThreads>(m, wb[0], tm);
+    const uint32_t ek = block_exclusive_sum<uint32_t, kScanThreads>(k, wb[1], tk);
+    const uint32_t eh = block_exclusive_sum<uint32_t, kScanThreads>(h, wb[2], th);
+    const uint32_t ep = block_exclusive_sum<uint32_t, kScanThreads>(p, wb[3], tp);
+    const uint4 b = prefix[blockIdx.x];
+    uint32_t rm = lastnz(b.x, em), rk = b.y + ek, rh = b.z + eh, rp = b.w + ep;
+    uint4 *out4 = reinterpret_cast<uint4 *>(carry);
+#pragma unroll
+    for (int i = 0; i < kScanPer; ++i) {
+        if (t0 + i >= tiles) break;
+        out4[t0 + i] = make_uint4(rm, rk, rh, rp);
+        rm = lastnz(rm, x[i].x);
+        rk += x[i].y;
+        rh += x[i].z;
+        rp += x[i].w;
+    }
+}
+
 // Assign new ranks, emit singletons, compact the survivors.  Flags come from
 // the head bits (one word per 32 entries, rows aligned to words), values and
 // slots are read in place; nothing is staged.
@@ -1876,6 +1968,7 @@ size_t sort_workspace_bytes(uint64_t n, int symbytes)
     s += 3 * align_up(n * 4, A);                   // large list: values x2, slots
     s += align_up(8 * 8, A);                       // round counters
     s += 2 * align_up(tiles * 16, A);              // tile info + carry
+    s += align_up((2 * (tiles / kScanSpan) + 4) * 16, A);   // tile-scan aggregates + their prefixes
     s += align_up((tiles * kAssignTile / 32 + 2) * 4, A);   // head bits of the assign tiles
     s += align_up(16 * 4, A);                      // totals
     s += align_up(65536 * 4, A);                   // hist
@@ -1912,6 +2005,7 @@ void sort_workspace_carve(SortWorkspace &ws, void *base, uint64_t n, int symbyte
     ws.slot0 = reinterpret_cast<uint32_t *>(ws.counters + 7);
     ws.tile_info = reinterpret_cast<uint32_t *>(take(tiles * 16));
     ws.tile_carry = reinterpret_cast<uint32_t *>(take(tiles * 16));
+    ws.tile_agg = reinterpret_cast<uint32_t *>(take((2 * (tiles / kScanSpan) + 4) * 16));
     ws.heads = reinterpret_cast<uint32_t *>(take((tiles * kAssignTile / 32 + 2) * 4));
     ws.totals = reinterpret_cast<uint32_t *>(take(16 * 4));
     ws.hist = reinterpret_cast<uint32_t *>(take(65536 * 4));
@@ -2019,8 +2113,18 @@ static cudaError_t run_assign(const TileArgs &a, SortWorkspace &ws, uint32_t *ou
     GSAIS_COUNTED((k_tile_summary<MODE><<<(unsigned)((tiles + 7) / 8), 256, 0, st>>>(a, ws.heads, ws.tile_info)));
     if (ev) prof->end(KK_SUMMARY, ev, st, a.N * (MODE == MODE_ROUND ? 12 : 16));
     ev = prof ? prof->begin(st) : nullptr;   // the tile scan is timed with the assign
-    GSAIS_COUNTED((k_tile_scan<<<1, 1024, 0, st>>>(ws.tile_info, ws.tile_carry, tiles, ws.totals, base,
-                                                   a.pairs ? a.pair_count : nullptr)));
+    if (tiles <= 4 * (uint64_t)kScanSpan) {
+        GSAIS_COUNTED((k_tile_scan<<<1, 1024, 0, st>>>(ws.tile_info, ws.tile_carry, tiles, ws.totals, base,
+                                                       a.pairs ? a.pair_count : nullptr)));
+    } else {
+        const uint32_t blocks = (uint32_t)((tiles + kScanSpan - 1) / kScanSpan);
+        uint4 *agg = reinterpret_cast<uint4 *>(ws.tile_agg);
+        GSAIS_COUNTED((k_scan_up<<<blocks, kScanThreads, 0, st>>>(ws.tile_info, tiles, agg)));
+        GSAIS_COUNTED((k_scan_top<<<1, 1024, 0, st>>>(agg, blocks, ws.totals, base,
+                                                      a.pairs ? a.pair_count : nullptr)));
+        GSAIS_COUNTED((k_scan_down<<<blocks, kScanThreads, 0, st>>>(ws.tile_info, tiles, agg + blocks,
+                                                                    ws.tile_carry)));
+    }
     GSAIS_COUNTED((k_assign<MODE><<<(unsigned)tiles, kAssignThreads, 0, st>>>(
         a, ws.tile_carry, ws.heads, ws.rank, ws.sa, out_i, out_pos, out_gid, gstart_out)));
     // algorithmic bytes: key 8 + value 4 + slot 4 read, rank 4 scattered, and

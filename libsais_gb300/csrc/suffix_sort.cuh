@@ -27,6 +27,7 @@ struct SortWorkspace {
     uint32_t *slot0 = nullptr;               // (in counters[7]) 1 + SA slot of suffix 0 after the seed round
     uint32_t *tile_info = nullptr;           // 3 words per assign tile
     uint32_t *tile_carry = nullptr;          // 3 words per assign tile
+    uint32_t *tile_agg = nullptr;            // tile-scan aggregates of kScanSpan tiles, then their prefixes
     uint32_t *totals = nullptr;              // [4] kept entries, kept groups, ...
     uint32_t *hist = nullptr;                // symbol histogram (256 or 65536)
     uint16_t *codes = nullptr;               // dense symbol codes (256 or 65536)
