@@ -1606,7 +1606,7 @@ struct PackedWords {
 // then take their next pairs together from a global cursor, so the refill
 // code runs rarely and work stays balanced.  A pair still equal after
 // `limit` more symbols goes back to the active list as a two-member group.
-constexpr int kPairBlocks = 2;   // 16-byte blocks per side per step
+constexpr int kPairBlocks = 2;   // 16-byte blocks per side per step (3 and 4 measured no faster)
 
 struct PairSide {
     uint4 prev;               // block holding the window's first word
