@@ -196,6 +196,21 @@ inline size_t early_bytes(void *SA, int sa_bytes, uint64_t n)
     return sa_bytes == 4 && pinned_view(SA) ? align_up((n + 31) / 32 * 4) : 0;
 }
 
+// A BWT-only call (no SA wanted) into a pinned U: the early point copies no
+// SA, but the BWT is gathered and leaves while the rounds run, and the slots
+// the rounds still write are recorded for the patch of their BWT rows.
+bool early_setup_bwt_only(gsais_ctx *c, EarlySaCopy &ec, uint64_t n, Carver &cv)
+{
+    ec.host = nullptr;
+    ec.host_dev = nullptr;
+    ec.stream = c->copy_stream;
+    ec.ready = c->early_ev;
+    ec.copied = c->copied_ev;
+    ec.patch_cap = early_patch_cap(n);
+    ec.bits = cv.take<uint32_t>((n + 31) / 32);
+    return true;
+}
+
 // Waits for a stream when it goes out of scope.
 struct StreamJoin {
     cudaStream_t s;
@@ -430,8 +445,11 @@ int64_t gsais_run_bwt(gsais_ctx *c, const void *T, int symbytes, int64_t n_, voi
     DeviceGuard g(c->device);
     cudaStream_t st = c->stream;
     const uint64_t icount = r > 0 ? (n - 1) / (uint64_t)r + 1 : 0;
+    void *U_pin = pinned_view(U);
+    const bool bwt_only_early = !SA && U_pin;
     const size_t extra = align_up(n * symbytes) * 2 + (r > 0 ? align_up(icount * idx_bytes) : 0) +
-                         (SA && sa_bytes == 8 ? align_up(n * 8) : 0) + early_bytes(SA, sa_bytes, n);
+                         (SA && sa_bytes == 8 ? align_up(n * 8) : 0) + early_bytes(SA, sa_bytes, n) +
+                         (bwt_only_early ? align_up((n + 31) / 32 * 4) : 0);
     const SortPlan plan = plan_sort(n, symbytes, extra);
     if (!ensure_arena(c, plan.total)) return -2;
     Carver cv(c->arena);
@@ -440,8 +458,8 @@ int64_t gsais_run_bwt(gsais_ctx *c, const void *T, int symbytes, int64_t n_, voi
     void *d_I = r > 0 ? (void *)cv.take<uint8_t>(icount * idx_bytes) : nullptr;
     int64_t *d_wide = (SA && sa_bytes == 8) ? cv.take<int64_t>(n) : nullptr;
     EarlySaCopy ec;
-    const bool early = early_setup(c, ec, SA, sa_bytes, n, cv);
-    void *U_dev = early ? pinned_view(U) : nullptr;   // an early BWT needs U pinned too
+    const bool early = bwt_only_early ? early_setup_bwt_only(c, ec, n, cv) : early_setup(c, ec, SA, sa_bytes, n, cv);
+    void *U_dev = early ? U_pin : nullptr;   // an early BWT needs U pinned too
     SortWorkspace ws;
     sort_workspace_carve(ws, cv.p, n, symbytes, c->h_small, c->h_hist);
     if (!clear_err(c, st)) return fail(cudaErrorUnknown);

@@ -2746,15 +2746,17 @@ cudaError_t suffix_sort(const void *d_T, int symbytes, uint64_t n, bool gsa, Sor
 
     // ---- SA leaves for the host while the rank scatter and the rounds run
     // (the slots the rounds write are patched afterwards)
-    if (opt.early && opt.early->host && kept > 0 && kept <= opt.early->patch_cap) {
+    if (opt.early && (opt.early->host || opt.early->on_start) && kept > 0 && kept <= opt.early->patch_cap) {
         EarlySaCopy &ec = *opt.early;
         if ((e = cudaMemsetAsync(ec.bits, 0, (n + 31) / 32 * 4, st)) != cudaSuccess) return e;
         GSAIS_COUNTED((k_mark_slots<<<stream_grid(kept, 256), 256, 0, st>>>(ws.pos[pg], kept, n, ec.bits)));
         if ((e = cudaEventRecord(ec.ready, st)) != cudaSuccess) return e;
-        if ((e = cudaStreamWaitEvent(ec.stream, ec.ready, 0)) != cudaSuccess) return e;
-        if ((e = cudaMemcpyAsync(ec.host, ws.sa, n * 4, cudaMemcpyDeviceToHost, ec.stream)) != cudaSuccess)
-            return e;
-        if ((e = cudaEventRecord(ec.copied, ec.stream)) != cudaSuccess) return e;
+        if (ec.host) {
+            if ((e = cudaStreamWaitEvent(ec.stream, ec.ready, 0)) != cudaSuccess) return e;
+            if ((e = cudaMemcpyAsync(ec.host, ws.sa, n * 4, cudaMemcpyDeviceToHost, ec.stream)) != cudaSuccess)
+                return e;
+            if ((e = cudaEventRecord(ec.copied, ec.stream)) != cudaSuccess) return e;
+        }
         ec.patch_n = kept;
         ec.started = true;
         S.early_patch = kept;

@@ -67,7 +67,8 @@ constexpr size_t kHostSmallWords = 16 + 65536 + 32768 + kHostEdgeWords;
 // merged) leave as coalesced writes: the host link takes scattered 4-byte
 // writes at only a few billion a second.
 struct EarlySaCopy {
-    int32_t *host = nullptr;       // destination (the caller's pinned buffer)
+    int32_t *host = nullptr;       // destination (the caller's pinned buffer); null: no SA copy,
+                                   // only the slot bits and on_start (a BWT-only call)
     int32_t *host_dev = nullptr;   // the same buffer as the device addresses it
     cudaStream_t stream = nullptr;
     cudaEvent_t ready = nullptr;   // recorded on the sort's stream when the copy may start

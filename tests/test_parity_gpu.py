@@ -153,12 +153,12 @@ def test_pinned_host_buffers_early_copy(oracle):
     """Host calls whose SA buffer is pinned: SA leaves for the host while the
     doubling rounds run and the slots the rounds write are patched afterwards
     (early_patch > 0 when that path ran).  SA, BWT and primary index must
-    equal the oracle's, for libsais and the combined SA + BWT call (and
-    libsais_bwt, which returns no SA); a periodic text leaves too many
-    unresolved suffixes and takes the plain copy.  With U pinned too, the
-    BWT is taken at the same point and its unresolved rows rewritten later,
-    including texts whose suffix 0 is still unresolved then (a tied pair, a
-    group of three)."""
+    equal the oracle's, for libsais, the combined SA + BWT call and
+    libsais_bwt (which returns no SA: with U pinned only the BWT is taken
+    early); a periodic text leaves too many unresolved suffixes and takes the
+    plain copy.  With U pinned, the BWT is taken at the same point and its
+    unresolved rows rewritten later, including texts whose suffix 0 is still
+    unresolved then (a tied pair, a group of three)."""
     torch = pytest.importorskip("torch")
     lib = G.load()
     rng = np.random.default_rng(23)
@@ -188,9 +188,9 @@ def test_pinned_host_buffers_early_copy(oracle):
                 assert lib.libsais_bwt(hT.data_ptr(), hU.data_ptr(), hSA.data_ptr(), n, 0, None) == p
             else:
                 assert lib.gsais_sa_bwt(None, hT.data_ptr(), 1, n, hSA.data_ptr(), 4, hU.data_ptr(), None, 4) == p
-            early = G.last_stats()["early_patch"]   # libsais_bwt returns no SA: never early
+            early = G.last_stats()["early_patch"]
             if expect_early is not None:
-                assert (early > 0) == (expect_early and call != "bwt"), (call, n, early)
+                assert (early > 0) == expect_early, (call, n, early)
             if call != "bwt":
                 assert np.array_equal(hSA.numpy().astype(np.int64), oSA), (call, n)
             if call != "sa":
