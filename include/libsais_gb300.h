@@ -145,7 +145,8 @@ extern "C" {
 
     int32_t gsais_last_stats(void * ctx, gsais_stats * out);
 
-    /** Seed key width in bits (32 or 64) used by later sorts on ctx; returns the previous width. */
+    /** Seed key width in bits used by later sorts on ctx: 32, 64, or 0 (the default: 64 when the
+     *  text's codes take 3 or 4 bits, else 32); returns the previous setting, -1 for other values. */
     int32_t gsais_set_seed_key_bits(void * ctx, int32_t bits);
 
     /**

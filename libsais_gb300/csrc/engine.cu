@@ -913,7 +913,7 @@ int32_t gsais_last_stats(void *ctx, gsais_stats *out)
 int32_t gsais_set_seed_key_bits(void *ctx, int32_t bits)
 {
     gsais_ctx *c = resolve(ctx);
-    if (!c || (bits != 32 && bits != 64)) return -1;
+    if (!c || (bits != 0 && bits != 32 && bits != 64)) return -1;
     std::lock_guard<std::mutex> lock(c->mu);
     const int32_t prev = c->opt.seed_key_bits;
     c->opt.seed_key_bits = bits;

@@ -2569,7 +2569,12 @@ cudaError_t suffix_sort(const void *d_T, int symbytes, uint64_t n, bool gsa, Sor
     ws.radix.items32 = tn.radix_items32;
     ws.radix.items64 = tn.radix_items64;
     S.tuning = tn;
-    int K = (opt.seed_key_bits <= 32 ? 32 : 64) / bits;
+    // 3- and 4-bit codes: a 32-bit key holds 10 or 8 symbols, so on read sets
+    // and small alphabets most suffixes stay in large seed groups; 64-bit keys
+    // cost four more digit passes and save doubling rounds (GSA of 2^20 reads:
+    // 41.9 vs 51.6 ms).  2-bit codes (16 symbols) and wide alphabets keep 32.
+    const int key_bits = opt.seed_key_bits ? opt.seed_key_bits : ((bits == 3 || bits == 4) ? 64 : 32);
+    int K = (key_bits <= 32 ? 32 : 64) / bits;
     if (K < 2 && bits <= 32) K = 64 / bits;   // wide symbols: at least two per key
     if (K < 1) K = 1;
     if (K > 64) K = 64;

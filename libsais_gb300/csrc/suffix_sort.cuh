@@ -87,7 +87,8 @@ struct EarlySaCopy {
 struct SortOptions {
     Tuning tuning;            // used when tuning_set; otherwise tuning_lookup(n, code bits)
     bool tuning_set = false;
-    int seed_key_bits = 32;   // width of the packed seed prefix (32 or 64)
+    int seed_key_bits = 0;    // width of the packed seed prefix: 32, 64, or 0 (64 when the codes
+                              // take 3 or 4 bits, whose 32-bit keys hold only 10 or 8 symbols)
     uint32_t raw_max = 0;     // 32-bit integer symbols: the largest symbol value
     EarlySaCopy *early = nullptr;
     bool hist_ready = false;  // ws.hist already holds the symbol histogram (symbol_histogram_part)

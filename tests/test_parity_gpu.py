@@ -331,6 +331,26 @@ def test_lcp_partitioned_gather(n):
         assert rc == 0 and np.array_equal(L, expect.cpu().numpy())
 
 
+@pytest.mark.parametrize("key_bits", [32, 64, 0])
+def test_seed_key_widths(oracle, key_bits):
+    """32- and 64-bit seed keys and the automatic choice (64 bits for 3- and
+    4-bit codes) give the same outputs: a DNA text with 1 % 'N' (5 symbols,
+    3-bit codes), a repetitive 9-symbol text (4-bit codes) and a read set
+    (GSA, the separator and ACGT: 3-bit codes)."""
+    prev = G.set_seed_key_bits(key_bits)
+    try:
+        rng = np.random.default_rng(41)
+        nine = (rng.integers(0, 9, 300_000) + 97).astype(np.uint8)
+        nine[150_000:] = nine[:150_000]   # one long copy
+        check_all(oracle, textgen.dna_with_n(1 << 19, seed=9), plcp=True, r=4)
+        check_all(oracle, nine, plcp=False, r=0)
+        reads = textgen.reads_gsa(4000, ref_len=100_000, seed=11)
+        check_all(oracle, reads, gsa=True, plcp=True)
+        assert G.last_stats()["seed_symbols"] == (10 if key_bits == 32 else 21)
+    finally:
+        G.set_seed_key_bits(prev)
+
+
 def test_combined_sa_bwt(oracle):
     T = textgen.genome_like(1 << 20, seed=12)
     prim, SA, U, F = G.sa_bwt(T)
