@@ -1269,6 +1269,85 @@ __global__ void __launch_bounds__(256) k_round_r2(const uint32_t *__restrict__ a
 // reservation per CTA of (groups, entries), which keeps group ids increasing
 // with list position.  Bytes per suffix: 16 read, rank scatter 4, SA 4 or
 // survivors 12-16 written.
+// Ranks inside the owned groups of a 64-entry warp window (entry o = e * 32 +
+// lane holds the values of offset o) by a bitonic sort of the keys
+// (group start, r2, offset) -- unique, so the order is total -- with the
+// entries of groups the warp does not own sorted past the end.  In sorted
+// order a group's members are contiguous and ordered by (r2, offset), so
+// before = position - group start, lt = start of the run of equal r2 -
+// group start and eq = the run's length; they go back to their entries
+// through shared memory (s: 3 x 64 words of this warp).  About 21 exchange
+// stages, against maxsz steps of all-pairs comparison: used for warps whose
+// largest owned group has more than kSmallSortMin members.
+constexpr int kSmallSortMin = 16;
+
+__device__ __forceinline__ void window_rank_sort(const bool (&own)[2], const int (&gs)[2], uint32_t r0, uint32_t r1,
+                                                 uint32_t (&lt)[2], uint32_t (&eq)[2], uint32_t (&before)[2],
+                                                 uint32_t *s)
+{
+    const int lane = threadIdx.x & 31;
+    uint64_t k[2];
+    k[0] = own[0] ? ((uint64_t)gs[0] << 38) | ((uint64_t)r0 << 6) | (uint64_t)lane : ~0ull;
+    k[1] = own[1] ? ((uint64_t)gs[1] << 38) | ((uint64_t)r1 << 6) | (uint64_t)(32 + lane) : ~0ull;
+#pragma unroll
+    for (int kk = 2; kk <= 64; kk <<= 1) {
+#pragma unroll
+        for (int j = kk >> 1; j > 0; j >>= 1) {
+            if (j == 32) {   // kk == 64: entries lane and 32 + lane, ascending
+                const uint64_t a = k[0] < k[1] ? k[0] : k[1], b = k[0] < k[1] ? k[1] : k[0];
+                k[0] = a;
+                k[1] = b;
+            } else {
+#pragma unroll
+                for (int e = 0; e < 2; ++e) {
+                    const uint64_t o = __shfl_xor_sync(GSAIS_FULL_MASK, k[e], j);
+                    const bool asc = ((e * 32 + lane) & kk) == 0;
+                    const bool lower = (lane & j) == 0;
+                    const bool take_min = lower == asc;
+                    k[e] = take_min ? (o < k[e] ? o : k[e]) : (o > k[e] ? o : k[e]);
+                }
+            }
+        }
+    }
+    // boundaries in sorted order: group heads, heads of runs of equal r2, the valid range
+    const uint64_t p0 = __shfl_up_sync(GSAIS_FULL_MASK, k[0], 1);
+    uint64_t p1 = __shfl_up_sync(GSAIS_FULL_MASK, k[1], 1);
+    const uint64_t last0 = __shfl_sync(GSAIS_FULL_MASK, k[0], 31);
+    if (lane == 0) p1 = last0;
+    const bool v0 = k[0] != ~0ull, v1 = k[1] != ~0ull;
+    const bool gh0 = v0 && (lane == 0 || (p0 >> 38) != (k[0] >> 38));
+    const bool gh1 = v1 && (p1 >> 38) != (k[1] >> 38);
+    const bool vh0 = v0 && (lane == 0 || (p0 >> 6) != (k[0] >> 6));
+    const bool vh1 = v1 && (p1 >> 6) != (k[1] >> 6);
+    const uint64_t GH = (uint64_t)__ballot_sync(GSAIS_FULL_MASK, gh0) | ((uint64_t)__ballot_sync(GSAIS_FULL_MASK, gh1) << 32);
+    const uint64_t VH = (uint64_t)__ballot_sync(GSAIS_FULL_MASK, vh0) | ((uint64_t)__ballot_sync(GSAIS_FULL_MASK, vh1) << 32);
+    const uint64_t INV = ~((uint64_t)__ballot_sync(GSAIS_FULL_MASK, v0) | ((uint64_t)__ballot_sync(GSAIS_FULL_MASK, v1) << 32));
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+        if (!(e ? v1 : v0)) continue;
+        const int p = e * 32 + lane;
+        const uint64_t upto = p == 63 ? ~0ull : ((2ull << p) - 1);
+        const int g0 = 63 - __clzll((long long)(GH & upto));
+        const int vs = 63 - __clzll((long long)(VH & upto));
+        const uint64_t above = (VH | INV) & ~upto;
+        const int ve = above ? __ffsll((long long)above) - 1 : 64;
+        const uint32_t o = (uint32_t)(k[e] & 63);
+        s[o] = (uint32_t)(vs - g0);
+        s[64 + o] = (uint32_t)(ve - vs);
+        s[128 + o] = (uint32_t)(p - g0);
+    }
+    __syncwarp();
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+        if (!own[e]) continue;
+        const int o = e * 32 + lane;
+        lt[e] = s[o];
+        eq[e] = s[64 + o];
+        before[e] = s[128 + o];
+    }
+    __syncwarp();
+}
+
 __global__ void __launch_bounds__(256) k_small_groups(const uint32_t *__restrict__ act_i,
                                                       const uint32_t *__restrict__ act_pos,
                                                       const uint32_t *__restrict__ act_gid,
@@ -1286,6 +1365,7 @@ __global__ void __launch_bounds__(256) k_small_groups(const uint32_t *__restrict
     constexpr int WARPS = 8;
     __shared__ uint32_t s_we[WARPS], s_wg[WARPS];
     __shared__ unsigned long long s_base;
+    __shared__ uint32_t s_rk[WARPS][3 * 64];   // window_rank_sort results by window offset
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     // a resident grid walks the 256-entry tiles in which a small group starts
     // (listed by k_classify / k_collect_tiles); a tile whose warps own no
@@ -1355,6 +1435,8 @@ __global__ void __launch_bounds__(256) k_small_groups(const uint32_t *__restrict
 
     uint32_t lt[2] = {0, 0}, eq[2] = {0, 0}, before[2] = {0, 0};
     const uint32_t myr[2] = {rr0, rr1};
+    if (maxsz > kSmallSortMin) window_rank_sort(own, gs, rr0, rr1, lt, eq, before, s_rk[warp]);
+    else
     for (int t = 0; t < maxsz; ++t) {
         for (int e = 0; e < 2; ++e) {
             const int src = (gs[e] < 0 ? 0 : gs[e]) + t;
