@@ -837,14 +837,35 @@ __global__ void __launch_bounds__(256) k_pack_codes(const Sym *__restrict__ T, u
                                                     uint64_t words)
 {
     constexpr int SPW = 64 / B;
+    // 8-bit texts: the code table in shared memory and the word's SPW bytes in
+    // 16-byte loads (a warp reads 32 x SPW contiguous bytes)
+    constexpr bool BYTES = sizeof(Sym) == 1;
+    __shared__ uint8_t s_codes[BYTES ? 256 : 1];
+    if (BYTES) {
+        for (int c = threadIdx.x; c < 256; c += blockDim.x) s_codes[c] = (uint8_t)codes[c];
+        __syncthreads();
+    }
+    const bool vec = BYTES && (reinterpret_cast<uintptr_t>(T) & 15) == 0;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; w < words; w += stride) {
         uint64_t v = 0;
         const uint64_t p0 = w * SPW;
+        if (vec && p0 + SPW <= n) {
+            const uint4 *src = reinterpret_cast<const uint4 *>(reinterpret_cast<const uint8_t *>(T) + p0);
+#pragma unroll
+            for (int q = 0; q < SPW / 16; ++q) {
+                const uint4 x = __ldcs(src + q);
+                const uint32_t xs[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+                for (int j = 0; j < 16; ++j)
+                    v |= (uint64_t)s_codes[(xs[j >> 2] >> (8 * (j & 3))) & 255u] << ((q * 16 + j) * B);
+            }
+        } else {
 #pragma unroll 8
-        for (int k = 0; k < SPW; ++k) {
-            const uint64_t p = p0 + k;
-            if (p < n) v |= (uint64_t)__ldg(codes + T[p]) << (k * B);
+            for (int k = 0; k < SPW; ++k) {
+                const uint64_t p = p0 + k;
+                if (p < n) v |= (uint64_t)(BYTES ? s_codes[(uint32_t)T[p]] : __ldg(codes + T[p])) << (k * B);
+            }
         }
         packed[w] = v;
     }
@@ -943,15 +964,28 @@ cudaError_t plcp_run(const Sym *T, const uint32_t *SA, uint64_t n, uint32_t *plc
 }
 
 // Which byte values occur in an 8-bit text: bit c of the 256-bit map (eight
-// words).  Each thread ORs its symbols into eight registers, a warp reduces
-// them, and a block does one atomicOr per word.  Bytes per symbol: 1 read.
+// words).  Each thread keeps one 32-symbol block of the map in a register (the
+// block of the last symbol it met outside it): texts of a few symbols in one
+// block (DNA) never leave it, other symbols go to the CTA's map by a
+// shared-memory atomicOr; a block does one atomicOr per word at the end.
+// Bytes per symbol: 1 read.
 __global__ void __launch_bounds__(256) k_presence_u8(const uint8_t *__restrict__ T, uint64_t n,
                                                      uint32_t *__restrict__ present)
 {
     __shared__ uint32_t sm[8];
     if (threadIdx.x < 8) sm[threadIdx.x] = 0;
     __syncthreads();
-    uint32_t m[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    uint32_t cur_q = 0, cur_m = 0;
+    auto add = [&](uint32_t c) {
+        const uint32_t q = c >> 5, bit = 1u << (c & 31);
+        if (q == cur_q) {
+            cur_m |= bit;
+        } else {
+            if (cur_m) atomicOr(&sm[cur_q], cur_m);
+            cur_q = q;
+            cur_m = bit;
+        }
+    };
     const uint64_t head = (16 - (reinterpret_cast<uintptr_t>(T) & 15)) & 15;
     const uint64_t h = head < n ? head : n;
     const uint64_t vecs = (n - h) / 16;
@@ -963,20 +997,13 @@ __global__ void __launch_bounds__(256) k_presence_u8(const uint8_t *__restrict__
 #pragma unroll
         for (int q = 0; q < 4; ++q)
 #pragma unroll
-            for (int b = 0; b < 4; ++b) {
-                const uint32_t c = (words[q] >> (8 * b)) & 255u;
-                m[c >> 5] |= 1u << (c & 31);
-            }
+            for (int b = 0; b < 4; ++b) add((words[q] >> (8 * b)) & 255u);
     }
     if (blockIdx.x == 0 && threadIdx.x < 32) {   // the unaligned head and the tail
-        for (uint64_t i = threadIdx.x; i < h; i += 32) m[T[i] >> 5] |= 1u << (T[i] & 31);
-        for (uint64_t i = h + vecs * 16 + threadIdx.x; i < n; i += 32) m[T[i] >> 5] |= 1u << (T[i] & 31);
+        for (uint64_t i = threadIdx.x; i < h; i += 32) add(T[i]);
+        for (uint64_t i = h + vecs * 16 + threadIdx.x; i < n; i += 32) add(T[i]);
     }
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-        const uint32_t r = __reduce_or_sync(GSAIS_FULL_MASK, m[q]);
-        if ((threadIdx.x & 31) == 0 && r) atomicOr(&sm[q], r);
-    }
+    if (cur_m) atomicOr(&sm[cur_q], cur_m);
     __syncthreads();
     if (threadIdx.x < 8 && sm[threadIdx.x]) atomicOr(&present[threadIdx.x], sm[threadIdx.x]);
 }
