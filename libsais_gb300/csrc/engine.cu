@@ -275,8 +275,11 @@ cudaError_t upload_text(gsais_ctx *c, void *d_T, const void *T, int symbytes, ui
     return cudaSuccess;
 }
 
+// counts: the caller returns symbol counts (freq); without them an 8-bit
+// text's codes come from a presence map.
 int64_t run_sort(gsais_ctx *c, const void *d_T, int symbytes, uint64_t n, bool gsa, SortWorkspace &ws,
-                 cudaStream_t st, uint32_t raw_max = 0, EarlySaCopy *early = nullptr, bool hist_ready = false)
+                 cudaStream_t st, uint32_t raw_max = 0, EarlySaCopy *early = nullptr, bool hist_ready = false,
+                 bool counts = true)
 {
     if (gsa) {
         bool valid = true;
@@ -288,6 +291,7 @@ int64_t run_sort(gsais_ctx *c, const void *d_T, int symbytes, uint64_t n, bool g
     opt.raw_max = raw_max;
     opt.early = early;
     opt.hist_ready = hist_ready;
+    opt.presence_only = !counts;
     GS_TRY(suffix_sort(d_T, symbytes, n, gsa, ws, opt, c->d_misc, st, &c->stats));
     return 0;
 }
@@ -639,7 +643,7 @@ int64_t gsais_sa_device(void *ctx, const void *T, int32_t symbytes, int64_t n_, 
     sort_workspace_carve(ws, c->arena, n, symbytes, c->h_small, c->h_hist);
     if (sa_bytes == 4) ws.sa = static_cast<uint32_t *>(SA);
     if (!clear_err(c, st)) return fail(cudaErrorUnknown);
-    const int64_t rc = run_sort(c, T, symbytes, n, gsa != 0, ws, st);
+    const int64_t rc = run_sort(c, T, symbytes, n, gsa != 0, ws, st, 0, nullptr, false, false);
     if (rc != 0) return rc;
     if (sa_bytes == 8) GS_TRY(widen_u32_to_i64(ws.sa, static_cast<int64_t *>(SA), n, st));
     GS_TRY(sync_checked(c, st));
@@ -665,7 +669,7 @@ int64_t gsais_sa_bwt_device(void *ctx, const void *T, int32_t symbytes, int64_t 
     sort_workspace_carve(ws, c->arena, n, symbytes, c->h_small, c->h_hist);
     if (SA && sa_bytes == 4) ws.sa = static_cast<uint32_t *>(SA);
     if (!clear_err(c, st)) return fail(cudaErrorUnknown);
-    const int64_t rc = run_sort(c, T, symbytes, n, false, ws, st);
+    const int64_t rc = run_sort(c, T, symbytes, n, false, ws, st, 0, nullptr, false, false);
     if (rc != 0) return rc;
     cudaEvent_t ev_bwt = c->prof.begin(st);
     GS_TRY(bwt_gather(T, symbytes, ws.sa, ws.rank, n, U, packed_of(ws), c->d_misc, st));

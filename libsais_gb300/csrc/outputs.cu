@@ -1145,6 +1145,14 @@ cudaError_t plcp_build(const void *d_T, int symbytes, const uint32_t *d_SA, uint
                : plcp_dispatch<uint16_t, false>(T, d_SA, n, d_PLCP, d_sparse, h_hist, err, st);
 }
 
+cudaError_t byte_presence(const uint8_t *d_T, uint64_t n, uint32_t *d_map, cudaStream_t st)
+{
+    cudaError_t e = cudaMemsetAsync(d_map, 0, 8 * sizeof(uint32_t), st);
+    if (e != cudaSuccess || n == 0) return e;
+    GSAIS_COUNTED((k_presence_u8<<<grid_for(n / 16 + 1, 256), 256, 0, st>>>(d_T, n, d_map)));
+    return cudaGetLastError();
+}
+
 cudaError_t int_alphabet_scan(const void *d_T, int tbytes, uint64_t n, int64_t k, unsigned long long *d_out,
                               cudaStream_t st)
 {

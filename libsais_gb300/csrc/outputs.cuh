@@ -45,6 +45,9 @@ size_t plcp_sparse_words(uint64_t n);
 cudaError_t plcp_build(const void *d_T, int symbytes, const uint32_t *d_SA, uint64_t n, bool gsa, uint32_t *d_PLCP,
                        uint32_t *d_sparse, uint32_t *h_hist, uint32_t *err, cudaStream_t st);
 
+// d_map (eight words) = the 256-bit map of the byte values that occur in T.
+cudaError_t byte_presence(const uint8_t *d_T, uint64_t n, uint32_t *d_map, cudaStream_t st);
+
 // Integer alphabets (int32 or int64 symbols, tbytes 4 or 8): d_out[0] = the
 // largest value, d_out[1] = 1 if some value lies outside [0, k).
 cudaError_t int_alphabet_scan(const void *d_T, int tbytes, uint64_t n, int64_t k, unsigned long long *d_out,

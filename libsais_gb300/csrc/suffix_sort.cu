@@ -30,6 +30,7 @@
 
 #include "device_util.cuh"
 #include "engine.h"
+#include "outputs.cuh"
 #include "radix_hist.cuh"
 #include "suffix_sort.cuh"
 
@@ -2635,6 +2636,16 @@ cudaError_t suffix_sort(const void *d_T, int symbytes, uint64_t n, bool gsa, Sor
             if ((e = cudaMemcpyAsync(h_hist, ws.hist, (size_t)nsym * 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
                 (e = cudaStreamSynchronize(st)) != cudaSuccess)
                 return e;
+        } else if (opt.presence_only && symbytes == 1) {
+            // the codes only need which bytes occur: h_hist[c] = 1 for those
+            cudaEvent_t ev_h = ws.radix.prof ? ws.radix.prof->begin(st) : nullptr;
+            uint32_t *h_map = h_hist + 256;
+            if ((e = byte_presence(static_cast<const uint8_t *>(d_T), n, ws.hist, st)) != cudaSuccess ||
+                (e = read_back(h_map, ws.hist, 8 * sizeof(uint32_t), st)) != cudaSuccess ||
+                (e = cudaStreamSynchronize(st)) != cudaSuccess)
+                return e;
+            if (ev_h) ws.radix.prof->end(KK_HIST, ev_h, st, n);
+            for (int c = 0; c < 256; ++c) h_hist[c] = (h_map[c >> 5] >> (c & 31)) & 1u;
         } else {
             cudaEvent_t ev_h = ws.radix.prof ? ws.radix.prof->begin(st) : nullptr;
             if ((e = symbol_histogram(d_T, symbytes, n, ws.hist, h_hist, st)) != cudaSuccess) return e;

@@ -92,6 +92,7 @@ struct SortOptions {
     uint32_t raw_max = 0;     // 32-bit integer symbols: the largest symbol value
     EarlySaCopy *early = nullptr;
     bool hist_ready = false;  // ws.hist already holds the symbol histogram (symbol_histogram_part)
+    bool presence_only = false;   // no caller wants the counts (freq): 8-bit texts take a presence map
 };
 
 // Queues on `st`, behind the bulk copy (ec.copied), the writes of the
