@@ -196,3 +196,21 @@ def test_python_structs_match_the_header(tmp_path):
         assert got[(cname, "size")] == ctypes.sizeof(py), cname
         for fname, _ in py._fields_:
             assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
+
+
+def test_stream_handles_passed_to_the_c_entry_points():
+    """None stays NULL (the context's own stream); a raw handle passes as is;
+    a torch stream passes its handle, except torch's default stream (handle
+    0), which the C entry points would read as "the context's stream": it
+    goes as cudaStreamLegacy (1), so the call is ordered after the work
+    already queued there."""
+    import libsais_gb300 as G
+
+    class FakeStream:
+        def __init__(self, h):
+            self.cuda_stream = h
+
+    assert G._stream_handle(None) is None
+    assert G._stream_handle(0x7F00) == 0x7F00
+    assert G._stream_handle(FakeStream(0x5000)) == 0x5000
+    assert G._stream_handle(FakeStream(0)) == 1
