@@ -967,11 +967,15 @@ def main():
         e2e = {"value": round(world * n / 1e6 / dt, 3), "unit": UNIT, "h2d_bytes_per_step": 2 * n,
                "d2h_bytes_per_step": n * 4 + n, "ms_per_step": round(dt * 1e3, 3),
                "step_ms_min_max": [round(min(step_ms), 3), round(max(step_ms), 3)],
-               "api": "libsais() then libsais_bwt() on pinned host buffers (two sorts; the text goes up twice)"}
+               "step_ms_median": round(statistics.median(step_ms), 3),
+               "api": "libsais() then libsais_bwt() on pinned host buffers (two sorts; the text goes up twice)",
+               "note": "value = mean over the timed steps; host-side steps of the shared box vary more than "
+                       "device ones (see the median and the fastest step)"}
         dt, step_ms = res["one_sort"]
         e2e_one_sort = {"value": round(world * n / 1e6 / dt, 3), "unit": UNIT, "h2d_bytes_per_step": n,
                         "d2h_bytes_per_step": n * 4 + n, "ms_per_step": round(dt * 1e3, 3),
                         "step_ms_min_max": [round(min(step_ms), 3), round(max(step_ms), 3)],
+                        "step_ms_median": round(statistics.median(step_ms), 3),
                         "api": "gsais_sa_bwt (SA and BWT from one sort) on pinned host buffers"}
 
     cpu = None
